@@ -1,0 +1,572 @@
+"""Benchmark of the evoxels time-stepping hot path on GB300.
+
+Default workload (the headline metric): Cahn-Hilliard 256^3, fp32, periodic,
+seeded c0 = 0.5 + 0.1*U[0,1) (seed 6), reference defaults eps=3, D=1, dt=0.1.
+One bench step = one gradient evaluation of an inversion: 10 IMEX steps
+forward (trajectory kept in HBM), the MSE loss against a seeded target and its
+gradient, then 10 adjoint steps giving dL/dc0, dL/dD and dL/deps.  A
+voxel-step counts one forward plus one adjoint step of one voxel.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch128_inversion]
+
+``--impl reference`` times the CPU oracle (the operation-by-operation torch
+restatement of the reference's own torch path; the reference itself is pure
+Python/torch) on the host cores with all threads, on the same workload; each
+step is a bounded sample (one forward + one adjoint step at the same size).
+
+Multi-GPU (torchrun): single-grid workloads run as independent replicas, one
+per rank (weak scaling, no collective on the data path).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "voxel-steps/s fwd+adjoint CH 256³: batched/fused vs plain, same GPU, ≤1e-5 err"
+FALLBACK_HBM_GBS = 6800.0
+
+# DRAM bytes per launch measured with ncu on small captures (see profiles/), per
+# voxel of the launch; None where no capture exists yet.
+NCU_DRAM_BYTES_PER_VOXEL = {}
+
+
+def algorithmic_bytes(slot, n, nspec):
+    """Compulsory HBM bytes of one launch of each kernel slot (fp32 fields, complex64 spectra)."""
+    table = {
+        "ch_rhs_fused": 16 * n,     # read u_{n-1}, update; write u_n, r
+        "ch_rhs": 8 * n,            # read u; write r
+        "ch_axpy": 16 * n,          # read u, update; write u_out and the trajectory slot
+        "ch_kspace_fwd": 16 * nspec,  # read + write the half spectrum
+        "ch_kspace_adj": 24 * nspec,  # read lam_hat; write g_hat, h_hat
+        "ch_pullback_grads": 24 * n,  # read u_s, g, lam, h, u_{s+1}; write lam_s
+        "ch_pullback": 16 * n,
+        "mse_grad": 12 * n,
+        "cufft_r2c": 4 * n + 8 * nspec,
+        "cufft_c2r": 8 * nspec + 4 * n,
+        "cufft_c2r_x2": 16 * nspec + 8 * n,
+        "fd_step": 8 * n,
+        "fd_tblock2": 8 * n,
+        "fd_tblock4": 8 * n,
+    }
+    return table.get(slot)
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", FALLBACK_HBM_GBS)), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_id):
+        self.device_id = device_id
+        self.proc = None
+        self.lines = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device_id}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workloads (our arm)
+# ---------------------------------------------------------------------------
+
+class ChFwdAdj:
+    """CH 256^3 (or other size) forward + adjoint gradient evaluation."""
+
+    def __init__(self, torch, device, n=256, steps_per=10, seed=6, grads=True):
+        from evoxels_gb300.adjoint import CahnHilliardAdjoint
+        from evoxels_gb300.voxelfields import VoxelFields
+        from evoxels_gb300.voxelgrid import VoxelGridGB300
+        self.torch = torch
+        self.shape = (n, n, n)
+        self.n = n ** 3
+        self.nspec = n * n * (n // 2 + 1)
+        self.T = steps_per
+        self.grads = grads
+        vf = VoxelFields(self.shape, domain_size=self.shape)
+        self.vg = VoxelGridGB300(vf.grid_info(), device=device)
+        self.runner = CahnHilliardAdjoint(self.vg, dt=0.1)
+        rng_c0 = 0.5 + 0.1 * np.random.default_rng(seed).random(self.shape)
+        rng_t = 0.5 + 0.1 * np.random.default_rng(seed + 100).random(self.shape)
+        self.c0_host = torch.tensor(rng_c0, dtype=torch.float32).unsqueeze(0).pin_memory()
+        self.t_host = torch.tensor(rng_t, dtype=torch.float32).unsqueeze(0).pin_memory()
+        self.traj = torch.empty((self.T + 1,) + self.shape, dtype=torch.float32, device=device)
+        self.c0 = self.traj[0:1]          # the initial state lives in trajectory slot 0
+        self.c0.copy_(self.c0_host)
+        self.target = self.t_host.to(device)
+        self.lam = torch.empty((1,) + self.shape, dtype=torch.float32, device=device)
+        self.g_host = torch.empty((1,) + self.shape, dtype=torch.float32).pin_memory()
+        self.units_per_step = self.n * self.T
+        self.config = {"workload": f"ch{n}_fwd_adj", "grid": list(self.shape), "fwd_adj_steps_per_bench_step": self.T,
+                       "dt": 0.1, "eps": 3.0, "D": 1.0, "A": 0.25, "bc": "periodic", "seed_c0": seed,
+                       "seed_target": seed + 100, "param_grads": grads,
+                       "l2": "inputs larger than L2: the kept trajectory is %.2f GB" % ((self.T + 1) * 4 * self.n / 1e9)}
+
+    def step(self):
+        """Device-resident step: forward (trajectory kept), loss gradient, adjoint."""
+        r = self.runner
+        r.forward(self.traj[0:1], self.T, 1.0, 3.0, traj=self.traj[1:])
+        loss = r.mse(self.traj[self.T:self.T + 1], self.target, self.lam)
+        grads = self.torch.zeros(3, dtype=self.torch.float64, device=self.c0.device) if self.grads else None
+        g0 = r.adjoint(self.traj, self.T, self.lam, 1.0, 3.0, grads)
+        return loss, g0, grads
+
+    def step_e2e(self):
+        """Same step from host buffers: H2D of c0 and target, D2H of dL/dc0, loss and grads."""
+        self.c0.copy_(self.c0_host, non_blocking=True)
+        self.target.copy_(self.t_host, non_blocking=True)
+        loss, g0, grads = self.step()
+        self.g_host.copy_(g0, non_blocking=True)
+        out = self.torch.cat([loss, grads]).cpu()
+        return out
+
+    def e2e_bytes(self):
+        return 2 * 4 * self.n, 4 * self.n + 8 * 4
+
+
+class ChForward:
+    """Plain CH forward steps (configs 1 and 5)."""
+
+    def __init__(self, torch, device, n=100, steps_per=100, seed=1):
+        from evoxels_gb300.problem_definition import CahnHilliard
+        from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+        from evoxels_gb300.voxelfields import VoxelFields
+        from evoxels_gb300.voxelgrid import VoxelGridGB300
+        self.torch = torch
+        self.shape = (n, n, n)
+        self.n = n ** 3
+        self.nspec = n * n * (n // 2 + 1)
+        self.T = steps_per
+        vf = VoxelFields(self.shape, domain_size=self.shape)
+        vg = VoxelGridGB300(vf.grid_info(), device=device)
+        self.st = PseudoSpectralIMEX(CahnHilliard(vg), 0.1)
+        c0 = 0.5 + 0.1 * np.random.default_rng(seed).random(self.shape)
+        self.c0_host = torch.tensor(c0, dtype=torch.float32).unsqueeze(0).pin_memory()
+        self.c0 = self.c0_host.to(device)
+        self.out_host = torch.empty_like(self.c0_host).pin_memory()
+        self.units_per_step = self.n * self.T
+        self.config = {"workload": f"ch{n}_fwd", "grid": list(self.shape), "imex_steps_per_bench_step": self.T,
+                       "dt": 0.1, "eps": 3.0, "D": 1.0, "bc": "periodic", "seed": seed,
+                       "l2": "working set (state, update, rhs, spectrum) %s L2" %
+                             ("larger than" if 16 * self.n > 129e6 else "fits in")}
+
+    def step(self):
+        return self.st.advance(self.c0, self.T)
+
+    def step_e2e(self):
+        self.c0.copy_(self.c0_host, non_blocking=True)
+        u = self.step()
+        self.out_host.copy_(u, non_blocking=True)
+        self.torch.cuda.current_stream().synchronize()
+
+    def e2e_bytes(self):
+        return 4 * self.n, 4 * self.n
+
+
+class FdForward:
+    """Explicit FD diffusion, 512^3, Dirichlet x / Neumann y,z, dt = 1/60 (config 2)."""
+
+    def __init__(self, torch, device, n=512, steps_per=100, seed=2, spp=4):
+        import warnings
+        from evoxels_gb300.problem_definition import ReactionDiffusion
+        from evoxels_gb300.timesteppers import ForwardEuler
+        from evoxels_gb300.voxelfields import VoxelFields
+        from evoxels_gb300.voxelgrid import VoxelGridGB300
+        self.torch = torch
+        self.shape = (n, n, n)
+        self.n = n ** 3
+        self.nspec = 0
+        self.T = steps_per
+        vf = VoxelFields(self.shape, domain_size=self.shape)
+        vg = VoxelGridGB300(vf.grid_info(), device=device)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            prob = ReactionDiffusion(vg, D=1.0, bc=(("dirichlet", (0, 0)), "neumann", "neumann"))
+        self.st = ForwardEuler(prob, 0.1 / 6, steps_per_pass=spp)
+        u0 = np.random.default_rng(seed).random(self.shape)
+        self.c0_host = torch.tensor(u0, dtype=torch.float32).unsqueeze(0).pin_memory()
+        self.c0 = self.c0_host.to(device)
+        self.out_host = torch.empty_like(self.c0_host).pin_memory()
+        self.units_per_step = self.n * self.T
+        self.config = {"workload": f"fd{n}", "grid": list(self.shape), "fe_steps_per_bench_step": self.T,
+                       "dt": 0.1 / 6, "D": 1.0, "bc": "dirichlet(0,0) x, neumann y, z", "steps_per_pass": spp,
+                       "seed": seed, "l2": "inputs larger than L2 (%.2f GB per field)" % (4 * self.n / 1e9)}
+
+    def step(self):
+        return self.st.advance(self.c0, self.T)
+
+    def step_e2e(self):
+        self.c0.copy_(self.c0_host, non_blocking=True)
+        u = self.step()
+        self.out_host.copy_(u, non_blocking=True)
+        self.torch.cuda.current_stream().synchronize()
+
+    def e2e_bytes(self):
+        return 4 * self.n, 4 * self.n
+
+
+def make_workload(name, torch, device):
+    if name == "ch256_fwd_adj":
+        return ChFwdAdj(torch, device, 256, 10, 6)
+    if name == "ch128_inversion":
+        return ChFwdAdj(torch, device, 128, 200, 3)
+    if name == "ch100_fwd":
+        return ChForward(torch, device, 100, 100, 1)
+    if name == "ch512_fwd":
+        return ChForward(torch, device, 512, 20, 5)
+    if name == "fd512":
+        return FdForward(torch, device, 512, 100, 2)
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ---------------------------------------------------------------------------
+# CPU baselines (the oracle port of the reference's torch path)
+# ---------------------------------------------------------------------------
+
+def cpu_sample(workload_name, torch, seconds_cap=30.0):
+    """Time the oracle (torch CPU, all host threads) on a bounded sample of the workload."""
+    import oracle
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    if workload_name in ("ch256_fwd_adj", "ch128_inversion"):
+        n = 256 if workload_name == "ch256_fwd_adj" else 128
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_ch_field(shape, 6), dtype=torch.float32).unsqueeze(0)
+        lam = torch.tensor(oracle.seeded_unit_field(shape, 7) - 0.5, dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            oracle.ch_imex_run(u0, 1, 0.1)                   # forward step
+            oracle.ch_imex_vjp(u0, lam, 0.1, 3.0, 1.0)       # adjoint step (autograd through the step)
+        units = n ** 3
+        sample = f"{n}^3, 1 forward IMEX step + 1 adjoint step (torch autograd), fp32"
+    elif workload_name in ("ch100_fwd", "ch512_fwd"):
+        n = 100 if workload_name == "ch100_fwd" else 512
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_ch_field(shape, 1), dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            oracle.ch_imex_run(u0, 1, 0.1)
+        units = n ** 3
+        sample = f"{n}^3, 1 IMEX step, fp32"
+    else:
+        n = 512
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_unit_field(shape, 2), dtype=torch.float32).unsqueeze(0)
+        bc = (("dirichlet", (0, 0)), "neumann", "neumann")
+
+        def one():
+            oracle.rd_fe_run(u0, 1, 0.1 / 6, 1.0, bc)
+        units = n ** 3
+        sample = f"{n}^3, 1 forward-Euler step, fp32"
+    one()  # warm-up
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        one()
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > seconds_cap / 3 or reps >= 5:
+            break
+    return {"value": units * reps / el, "unit": "voxel-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{sample}; {reps} reps after 1 warm-up, {el:.1f} s"}, el / reps, units
+
+
+# ---------------------------------------------------------------------------
+# main
+# ---------------------------------------------------------------------------
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ch256_fwd_adj")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    warmup = max(3, args.warmup)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        return run_reference(args, torch, warmup)
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    device = torch.device("cuda", local_rank if world > 1 else torch.cuda.current_device())
+    torch.cuda.set_device(device)
+
+    from evoxels_gb300 import _lib
+    L = _lib.lib()
+    wl = make_workload(args.workload, torch, device)
+
+    for _ in range(warmup):
+        wl.step()
+    torch.cuda.synchronize()
+
+    # ---- timed region (device-resident inputs) ------------------------------------
+    props = torch.cuda.get_device_properties(device)
+    dev_id = getattr(props, "uuid", None)
+    dev_id = f"GPU-{dev_id}" if dev_id is not None else str(device.index)
+    sampler = ClockSampler(dev_id)
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = L.evx_launch_count()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        wl.step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = L.evx_launch_count() - launches0
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    units_total = wl.units_per_step * args.steps * world
+    value = units_total / (ms / 1e3)
+
+    # ---- end to end: host buffers through the public API -------------------------
+    for _ in range(2):
+        wl.step_e2e()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        wl.step_e2e()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t)
+    h2d, d2h = wl.e2e_bytes()
+    e2e = {"value": units_total / e2e_s, "unit": "voxel-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+
+    # ---- per-kernel breakdown (separate pass, CUDA events on the launching stream) --
+    L.evx_prof_reset()
+    L.evx_prof_enable(1)
+    nprof = 3
+    for _ in range(nprof):
+        wl.step()
+    torch.cuda.synchronize()
+    L.evx_prof_enable(0)
+    prof = _lib.prof_read()
+    peak, peak_kind = read_peaks()
+    breakdown = {}
+    total_ms = sum(v[0] for v in prof.values()) or 1.0
+    for slot, (tms, cnt) in sorted(prof.items(), key=lambda kv: -kv[1][0]):
+        b = algorithmic_bytes(slot, wl.n, wl.nspec)
+        avg = tms / max(cnt, 1)
+        breakdown[slot] = {"launches": cnt // nprof, "avg_us": round(avg * 1e3, 2),
+                           "share": round(tms / total_ms, 4),
+                           "achieved_gbs": round(b / (avg / 1e3) / 1e9, 1) if b else None}
+    ours = {k: v for k, v in prof.items() if not k.startswith("cufft")}
+    dom = max(ours, key=lambda k: ours[k][0]) if ours else None
+    roofline = None
+    if dom:
+        tms, cnt = ours[dom]
+        b = algorithmic_bytes(dom, wl.n, wl.nspec)
+        achieved = b / (tms / cnt / 1e3) / 1e9
+        tr = NCU_DRAM_BYTES_PER_VOXEL.get(dom)
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                    "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                    "algorithmic_bytes_per_launch": b,
+                    "traffic": (tr * wl.n) if tr is not None else None}
+    step_bytes = None
+    if args.workload in ("ch256_fwd_adj", "ch128_inversion"):
+        step_bytes = 64 * wl.units_per_step    # 32 B forward + 32 B adjoint per voxel-step
+    elif args.workload.startswith("ch"):
+        step_bytes = 32 * wl.units_per_step
+    elif args.workload.startswith("fd"):
+        step_bytes = 8 * wl.units_per_step
+    step_roofline = None
+    if step_bytes:
+        gbs = step_bytes * args.steps / (ms / 1e3) / 1e9
+        step_roofline = {"achieved": round(gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
+                         "bytes_per_voxel_step": step_bytes // wl.units_per_step}
+
+    out = {
+        "metric": METRIC if args.workload == "ch256_fwd_adj" else f"voxel-steps/s {args.workload}",
+        "value": round(value, 1),
+        "unit": "voxel-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": warmup,
+        "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded U[0,1) fields, no dataset)",
+        "config": dict(wl.config, parallelism=("replicas x%d" % world) if world > 1 else "single GPU"),
+        "roofline": roofline,
+        "step_roofline": step_roofline,
+        "kernel_breakdown": breakdown,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb, _, _ = cpu_sample(args.workload, torch)
+        out["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_reference(args, torch, warmup):
+    """Reference arm: the oracle port of the reference's torch path on host cores."""
+    import oracle
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    wl = args.workload
+    if wl in ("ch256_fwd_adj", "ch128_inversion"):
+        n = 256 if wl == "ch256_fwd_adj" else 128
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_ch_field(shape, 6), dtype=torch.float32).unsqueeze(0)
+        lam = torch.tensor(oracle.seeded_unit_field(shape, 7) - 0.5, dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            u1 = oracle.ch_imex_run(u0, 1, 0.1)
+            oracle.ch_imex_vjp(u0, lam, 0.1, 3.0, 1.0)
+            return u1
+        sample = f"{n}^3: 1 forward IMEX step + 1 adjoint step (torch autograd) per bench step, fp32"
+    elif wl.startswith("ch"):
+        n = 100 if wl == "ch100_fwd" else 512
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_ch_field(shape, 1), dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            return oracle.ch_imex_run(u0, 1, 0.1)
+        sample = f"{n}^3: 1 IMEX step per bench step, fp32"
+    else:
+        n = 512
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_unit_field(shape, 2), dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            return oracle.rd_fe_run(u0, 1, 0.1 / 6, 1.0, (("dirichlet", (0, 0)), "neumann", "neumann"))
+        sample = f"{n}^3: 1 forward-Euler step per bench step, fp32"
+    for _ in range(warmup):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one()
+    el = time.perf_counter() - t0
+    value = n ** 3 * args.steps / el
+    out = {
+        "metric": METRIC if wl == "ch256_fwd_adj" else f"voxel-steps/s {wl}",
+        "impl": "reference",
+        "value": round(value, 1),
+        "unit": "voxel-steps/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": warmup,
+        "ms_per_step": round(el / args.steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded U[0,1) fields, no dataset)",
+        "config": {"workload": wl, "grid": list(shape)},
+        "cpu_baseline": {"value": round(value, 1), "unit": "voxel-steps/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 1), "unit": "voxel-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

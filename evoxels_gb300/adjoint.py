@@ -1,0 +1,195 @@
+"""Differentiable Cahn-Hilliard IMEX trajectories on the GPU.
+
+The reference differentiates its spectral solver with JAX/diffrax forward mode
+for parameter estimation (evoxels/inversion.py:51-124).  Here the gradient
+comes from a hand-written adjoint of each IMEX step (``evx_ch_adjoint``), with
+gradients with respect to the initial field, the mobility ``D`` and the
+gradient-energy parameter ``eps`` (``kappa = 2*eps``; the default bulk term
+``18/eps`` also depends on ``eps`` unless ``mu_hom`` pins it).
+
+Memory: states are checkpointed every ``checkpoint_every`` steps during the
+forward pass; the backward pass recomputes one segment at a time into a
+``(K+1)``-state buffer and runs the adjoint through it.  With
+``checkpoint_every >= nsteps`` the whole trajectory is kept and nothing is
+recomputed.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .problem_definition import CahnHilliard
+from .timesteppers import get_plan
+from .voxelgrid import VoxelGridGB300, cuda_stream
+
+
+class CahnHilliardAdjoint:
+    """Forward trajectory + adjoint driver on one grid.
+
+    ``pinned_w``: when given, the bulk term is ``pinned_w*c(1-c)(1-2c)``
+    independent of ``eps`` (the reference's callable ``mu_hom`` pinned to a
+    fixed coefficient); otherwise it is ``18/eps*c(1-c)(1-2c)``.
+    """
+
+    def __init__(self, vg: VoxelGridGB300, dt=0.1, A=0.25, pinned_w=None):
+        self.vg = vg
+        self.dt = float(dt)
+        self.A = float(A)
+        self.pinned_w = pinned_w
+        self.plan = get_plan(vg, grads=True)
+        self.n = int(np.prod(vg.shape))
+        self._pcache = {}
+        self._mse_scratch = torch.empty(int(_lib.lib().evx_mse_scratch_bytes(self.n)), dtype=torch.uint8,
+                                        device=vg.device)
+
+    def params(self, D, eps):
+        key = (float(D), float(eps))
+        p = self._pcache.get(key)
+        if p is None:
+            p = self._pcache[key] = self._make_params(*key)
+        return p
+
+    def _make_params(self, D, eps):
+        mu = None if self.pinned_w is None else (lambda c, lib=None, w=self.pinned_w: w * c * (1 - c) * (1 - 2 * c))
+        prob = CahnHilliard(self.vg, eps=float(eps), D=float(D), mu_hom=mu, A=self.A)
+        return prob.evx_params(self.dt)
+
+    def forward(self, u0, nsteps, D, eps, traj=None):
+        """``nsteps`` IMEX steps; ``traj`` (optional) receives u_1..u_n."""
+        out = torch.empty_like(u0)
+        p = self.params(D, eps)
+        _lib.check(_lib.lib().evx_ch_forward(self.plan.handle, u0.data_ptr(), out.data_ptr(), int(nsteps),
+                                             traj.data_ptr() if traj is not None else None, p, None,
+                                             self.plan.workspace.data_ptr(), cuda_stream()), "evx_ch_forward")
+        return out
+
+    def adjoint(self, states, nsteps, lam, D, eps, grads):
+        """Adjoint through ``states`` (``nsteps+1`` consecutive fields); accumulates into ``grads``."""
+        out = torch.empty_like(lam)
+        p = self.params(D, eps)
+        _lib.check(_lib.lib().evx_ch_adjoint(self.plan.handle, states.data_ptr(), int(nsteps), lam.data_ptr(),
+                                             out.data_ptr(), p, grads.data_ptr() if grads is not None else None,
+                                             self.plan.workspace.data_ptr(), cuda_stream()), "evx_ch_adjoint")
+        return out
+
+    def mse(self, u, target, lam=None):
+        """Device loss ``mean((u-target)^2)`` (float64 tensor) and optional gradient into ``lam``."""
+        loss = torch.empty(1, dtype=torch.float64, device=u.device)
+        _lib.check(_lib.lib().evx_mse_grad(u.data_ptr(), target.data_ptr(), self.n,
+                                           lam.data_ptr() if lam is not None else None, loss.data_ptr(),
+                                           self._mse_scratch.data_ptr(), self._mse_scratch.numel(),
+                                           cuda_stream()), "evx_mse_grad")
+        return loss
+
+    # ------------------------------------------------------------------------
+    def run_forward_checkpointed(self, c0, nsteps, D, eps, K):
+        """Forward pass.  Returns ``(u_T, saved)``; ``saved`` holds either the whole
+        trajectory (K >= nsteps) or the states every K steps."""
+        if K >= nsteps:
+            traj = torch.empty((nsteps + 1,) + tuple(c0.shape[1:]), dtype=torch.float32, device=c0.device)
+            traj[0].copy_(c0[0])
+            self.forward(traj[0:1], nsteps, D, eps, traj=traj[1:])
+            return traj[nsteps:nsteps + 1], {"traj": traj}
+        cps = [c0]
+        u = c0
+        s = 0
+        while s < nsteps:
+            m = min(K, nsteps - s)
+            u = self.forward(u, m, D, eps)
+            s += m
+            if s < nsteps:
+                cps.append(u)
+        return u, {"cps": cps}
+
+    def backward_checkpointed(self, saved, nsteps, lam_T, D, eps, K, want_params=True):
+        """Adjoint through all steps; segments are recomputed from their checkpoints."""
+        grads = torch.zeros(3, dtype=torch.float64, device=lam_T.device) if want_params else None
+        if "traj" in saved:
+            return self.adjoint(saved["traj"], nsteps, lam_T, D, eps, grads), grads
+        cps = saved["cps"]
+        seg_buf = torch.empty((K + 1,) + tuple(lam_T.shape[1:]), dtype=torch.float32, device=lam_T.device)
+        lam = lam_T
+        for si in range(len(cps) - 1, -1, -1):
+            m = min(K, nsteps - si * K)
+            seg_buf[0].copy_(cps[si][0])
+            self.forward(seg_buf[0:1], m, D, eps, traj=seg_buf[1:m + 1])
+            lam = self.adjoint(seg_buf[:m + 1], m, lam, D, eps, grads)
+        return lam, grads
+
+    def param_grads(self, grads, eps):
+        """Map (dL/dD, dL/dkappa, dL/dw) to (dL/dD, dL/deps)."""
+        gD, gK, gW = (float(x) for x in grads.tolist())
+        geps = 2.0 * gK
+        if self.pinned_w is None:
+            geps += -18.0 / float(eps) ** 2 * gW
+        return gD, geps
+
+    def loss_and_grads(self, c0, target, nsteps, D, eps, checkpoint_every=None):
+        """MSE loss of u_T against ``target`` and gradients w.r.t. c0, D, eps."""
+        K = nsteps if not checkpoint_every else int(checkpoint_every)
+        uT, saved = self.run_forward_checkpointed(c0, nsteps, D, eps, K)
+        lam = torch.empty_like(uT)
+        loss = self.mse(uT, target, lam)
+        g0, grads = self.backward_checkpointed(saved, nsteps, lam, D, eps, K)
+        gD, geps = self.param_grads(grads, eps)
+        return float(loss), g0, gD, geps
+
+
+class CahnHilliardIMEXFunction(torch.autograd.Function):
+    """``u_T = IMEX^n(c0; D, eps)`` with the hand-written adjoint as its backward.
+
+    ``apply(c0, D, eps, runner, nsteps, checkpoint_every)``: ``c0`` is a
+    ``(1, Nx, Ny, Nz)`` float32 CUDA tensor, ``D``/``eps`` 0-d tensors (or
+    floats).  Gradients flow to all three.
+    """
+
+    @staticmethod
+    def forward(ctx, c0, D, eps, runner, nsteps, checkpoint_every):
+        Df, ef = float(D), float(eps)
+        K = nsteps if not checkpoint_every else int(checkpoint_every)
+        c0 = c0.detach().contiguous()
+        uT, saved = runner.run_forward_checkpointed(c0, nsteps, Df, ef, K)
+        ctx.runner, ctx.nsteps, ctx.K, ctx.Df, ctx.ef = runner, nsteps, K, Df, ef
+        ctx.saved = saved
+        ctx.D_is_tensor = isinstance(D, torch.Tensor)
+        ctx.e_is_tensor = isinstance(eps, torch.Tensor)
+        return uT
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        r = ctx.runner
+        lam, grads = r.backward_checkpointed(ctx.saved, ctx.nsteps, grad_out.contiguous().float(), ctx.Df, ctx.ef,
+                                             ctx.K, want_params=ctx.needs_input_grad[1] or ctx.needs_input_grad[2])
+        gD = geps = None
+        if grads is not None:
+            d, e = r.param_grads(grads, ctx.ef)
+            gD = torch.tensor(d, dtype=torch.float32) if ctx.D_is_tensor else None
+            geps = torch.tensor(e, dtype=torch.float32) if ctx.e_is_tensor else None
+        ctx.saved = None
+        return lam, gD, geps, None, None, None
+
+
+def ch_imex_trajectory(c0, D, eps, nsteps, runner, checkpoint_every=None):
+    """Differentiable ``nsteps`` IMEX steps (see ``CahnHilliardIMEXFunction``)."""
+    return CahnHilliardIMEXFunction.apply(c0, D, eps, runner, int(nsteps), checkpoint_every)
+
+
+def default_checkpoint_interval(vg, nsteps, budget_bytes=None):
+    """Largest K whose (K+1)-state segment buffer plus n/K checkpoints fit the budget.
+
+    Default budget: half of the device's free memory.
+    """
+    field = 4 * int(np.prod(vg.shape))
+    if budget_bytes is None:
+        free, _ = torch.cuda.mem_get_info(vg.device)
+        budget_bytes = free // 2
+    best = 1
+    for K in range(1, nsteps + 1):
+        need = (K + 1) * field + math.ceil(nsteps / K) * field
+        if need <= budget_bytes:
+            best = K
+    return best

@@ -1,0 +1,57 @@
+// Internal definition of evx_ch_plan, shared by the forward and adjoint units.
+#pragma once
+
+#include <cufft.h>
+
+#include "evx_common.cuh"
+#include "evx_prof.cuh"
+
+struct evx_ch_plan {
+    evx_grid g;
+    int nzh;                 // nz/2 + 1
+    size_t n;                // nx*ny*nz
+    size_t nspec;            // nx*ny*nzh complex values
+    cufftHandle r2c = 0, c2r = 0, c2r2 = 0;
+    bool has_c2r2 = false;
+    size_t ws_fft = 0;       // cuFFT work area (max over plans)
+    float* kx2 = nullptr;    // device k^2 tables
+    float* ky2 = nullptr;
+    float* kz2 = nullptr;
+    // workspace layout (byte offsets)
+    size_t off_fft, off_r, off_upd, off_spec, off_u, off_lam, off_part, total;
+    int n_part;              // capacity of the partial-sum array (blocks)
+};
+
+namespace evx {
+
+// Kernel-side Cahn-Hilliard parameters.
+struct ChP {
+    float D, kappa, w, A, sym_coef, dt;
+};
+
+inline ChP make_chp(const evx_ch_params* p) {
+    ChP o;
+    o.D = p->D; o.kappa = p->kappa; o.w = p->w; o.A = p->A; o.sym_coef = p->sym_coef; o.dt = p->dt;
+    return o;
+}
+
+inline char* ws_at(void* ws, size_t off) { return static_cast<char*>(ws) + off; }
+
+int check_cufft(cufftResult r, const char* where);
+int ch_validate_params(const evx_ch_params* p);
+int ch_plan_bind(evx_ch_plan* plan, void* workspace, cudaStream_t st, bool need_c2r2);
+
+// FFT helpers (stream already bound by ch_plan_bind)
+int ch_r2c(evx_ch_plan* plan, const float* in, float2* out, cudaStream_t st);
+int ch_c2r(evx_ch_plan* plan, float2* in, float* out, bool batch2, cudaStream_t st);
+
+// Forward k-space multiply: spec *= prefac(k) then * invN (in that order).
+int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st);
+
+// Tile shape shared by the rhs and pullback stencil kernels.
+constexpr int CH_TZ = 32;           // tile extent along z (= warp width)
+constexpr int CH_TY = 16;           // tile extent along y
+constexpr int CH_THREADS = 256;     // 32 x 8 threads
+int ch_stencil_grid(const evx_grid* g, dim3* grid, int* LX);
+
+}  // namespace evx

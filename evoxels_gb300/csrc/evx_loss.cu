@@ -1,0 +1,81 @@
+// Mean-squared-error loss between a final state and a target field, and its
+// gradient: loss = mean((u - t)^2), lam = 2*(u - t)/n.  This seeds the adjoint
+// of an inversion (the loss the reference's parameter-estimation workflow
+// minimises between simulated and observed fields, evoxels/inversion.py:105-124).
+// Per-block partial sums go to caller scratch and one block reduces them in a
+// fixed order, so the loss is deterministic.
+#include <algorithm>
+
+#include "evx_common.cuh"
+#include "evx_prof.cuh"
+
+namespace evx {
+namespace {
+
+constexpr int MSE_THREADS = 256;
+constexpr int MSE_MAX_BLOCKS = 152 * 8;
+
+__global__ void __launch_bounds__(MSE_THREADS)
+mse_grad_kernel(const float* __restrict__ u, const float* __restrict__ t, size_t n, float scale,
+                float* __restrict__ lam, double* __restrict__ part) {
+    __shared__ double red[MSE_THREADS / 32];
+    double acc = 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+        const float d = __ldg(u + e) - __ldg(t + e);
+        if (lam) lam[e] = scale * d;
+        acc += (double)d * (double)d;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < MSE_THREADS / 32; ++w) s += red[w];
+        part[blockIdx.x] = s;
+    }
+}
+
+__global__ void mse_reduce_kernel(const double* __restrict__ part, int nblk, double inv_n, double* __restrict__ loss) {
+    __shared__ double s[256];
+    double a = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += 256) a += part[b];
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *loss = s[0] * inv_n;
+}
+
+int mse_blocks(size_t n) {
+    return (int)std::max<size_t>(1, std::min<size_t>((n + MSE_THREADS - 1) / MSE_THREADS, MSE_MAX_BLOCKS));
+}
+
+}  // namespace
+}  // namespace evx
+
+using namespace evx;
+
+extern "C" {
+
+size_t evx_mse_scratch_bytes(size_t n) { return (size_t)mse_blocks(n) * sizeof(double); }
+
+int evx_mse_grad(const float* u, const float* target, size_t n, float* lam, double* loss, void* scratch,
+                 size_t scratch_bytes, void* stream) {
+    if (!u || !target || !loss) return fail(EVX_ERR_BAD_ARG, "NULL pointer");
+    if (n == 0) return fail(EVX_ERR_BAD_SHAPE, "empty field");
+    const int nb = mse_blocks(n);
+    if (!scratch || scratch_bytes < (size_t)nb * sizeof(double))
+        return fail(EVX_ERR_WORKSPACE, "scratch needs %zu bytes", (size_t)nb * sizeof(double));
+    cudaStream_t st = as_stream(stream);
+    double* part = static_cast<double*>(scratch);
+    const float scale = (float)(2.0 / (double)n);
+    EVX_TIMED("mse_grad", st, mse_grad_kernel<<<nb, MSE_THREADS, 0, st>>>(u, target, n, scale, lam, part));
+    EVX_TIMED("mse_reduce", st, mse_reduce_kernel<<<1, 256, 0, st>>>(part, nb, 1.0 / (double)n, loss));
+    count_launch(2);
+    return check_launch("evx_mse_grad");
+}
+
+}  // extern "C"

@@ -1,0 +1,183 @@
+"""Problem definitions whose right-hand sides run in the CUDA library.
+
+Same constructor signatures, attributes and error behaviour as the reference's
+``CahnHilliard`` (evoxels/problem_definition.py:290-371) and
+``ReactionDiffusion`` (evoxels/problem_definition.py:191-229); ``rhs(t, u)``
+calls ``evx_ch_rhs`` / ``evx_rd_rhs`` on the grid's CUDA device.
+
+Scope of the CUDA kernels:
+* ``CahnHilliard.mu_hom`` must be ``None`` (the default ``18/eps*c(1-c)(1-2c)``)
+  or a callable equal to ``w*c*(1-c)*(1-2c)`` for some constant ``w`` - the
+  form the reference uses when the bulk energy is pinned independently of
+  ``eps``.  The callable is probed once on CPU to find ``w``.
+* ``ReactionDiffusion.f`` must be ``None`` or a callable returning ``0``.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Any, Callable
+
+import numpy as np
+import torch
+
+from . import _lib
+from .voxelgrid import VoxelGridGB300, cuda_stream, evx_bc, normalize_bc
+
+
+def _eval_callable(fn, *args):
+    try:
+        return fn(*args, torch)
+    except TypeError:
+        return fn(*args)
+
+
+def double_well_coefficient(mu_hom, eps):
+    """Return ``w`` such that ``mu_hom(c) == w*c*(1-c)*(1-2c)``, or raise.
+
+    ``None`` gives the reference default ``w = 18/eps``
+    (evoxels/problem_definition.py:304-305).
+    """
+    if mu_hom is None:
+        return 18 / eps
+    c = torch.tensor([0.0, 0.05, 0.1, 0.25, 0.3, 0.5, 0.6, 0.8, 0.9, 1.0], dtype=torch.float64)
+    basis = c * (1 - c) * (1 - 2 * c)
+    try:
+        vals = _eval_callable(mu_hom, c)
+        vals = torch.as_tensor(vals, dtype=torch.float64).expand_as(c)
+    except Exception as e:  # noqa: BLE001 - any failure means: not a supported form
+        raise NotImplementedError(f"mu_hom could not be evaluated on a probe tensor: {e}") from e
+    w = float(vals[3] / basis[3])
+    if not torch.allclose(vals, w * basis, rtol=1e-12, atol=1e-12 * max(1.0, abs(w))):
+        raise NotImplementedError(
+            "evoxels_gb300 supports mu_hom of the form w*c*(1-c)*(1-2c) only "
+            "(the reference default 18/eps*c*(1-c)*(1-2c) or a pinned coefficient)")
+    return w
+
+
+class _BCMixin:
+    def initialize_boundary_conditions(self):
+        """(evoxels/problem_definition.py:60-115); ghosts are applied in-kernel."""
+        self.bc = normalize_bc(getattr(self, "bc", None), self.vg.convention)
+        self._evx_bc = evx_bc(self.bc)
+
+    @property
+    def bc_type(self):
+        return tuple(axis_bc[0] for axis_bc in self.bc)
+
+    def pad_bc(self, u):
+        return self.vg.bc.pad_bc(u, self.bc)
+
+    def verify_fft_bc_config(self):
+        """(evoxels/problem_definition.py:138-167)."""
+        nonperiodic = tuple(a for a, k in zip(("x", "y", "z"), self.bc_type) if k != "periodic")
+        if len(nonperiodic) > 1:
+            raise ValueError("FFT-based timesteppers currently support at most one non-periodic axis, "
+                             f"got {self.bc_type}.")
+        if len(nonperiodic) == 1 and nonperiodic[0] != "x":
+            raise NotImplementedError(
+                "FFT-based timesteppers currently only implement the single non-periodic axis "
+                f"case for x; got {self.bc_type}. Axis permutation is not implemented yet.")
+        if len(nonperiodic) == 1:
+            raise NotImplementedError("evoxels_gb300 implements the periodic spectral step only; "
+                                      "the mirrored-x extension for non-periodic x is not built")
+        self._pad_fft_bc = self.vg.bc.pad_fft_periodic
+
+    def pad_fft_bc(self, u):
+        return self._pad_fft_bc(u)
+
+    def k_squared(self):
+        return self.vg.rfft_k_squared()
+
+
+@dataclass
+class CahnHilliard(_BCMixin):
+    vg: VoxelGridGB300
+    eps: float = 3.0
+    D: float = 1.0
+    mu_hom: Callable | None = None
+    A: float = 0.25
+    bc: tuple = ("periodic", "periodic", "periodic")
+    _fourier_symbol: Any = field(init=False, repr=False, default=None)
+
+    def __post_init__(self):
+        self.initialize_boundary_conditions()
+        self._w = double_well_coefficient(self.mu_hom, self.eps)
+        if self.mu_hom is None:
+            eps = self.eps
+            self.mu_hom = lambda c, lib=None: 18 / eps * c * (1 - c) * (1 - 2 * c)
+
+    @property
+    def order(self):
+        return 2
+
+    @property
+    def fourier_symbol(self):
+        """``-2*eps*D*A*(k^2)^2`` as a tensor (evoxels/problem_definition.py:303)."""
+        if self._fourier_symbol is None:
+            self._fourier_symbol = -2 * self.eps * self.D * self.A * self.k_squared() ** 2
+        return self._fourier_symbol
+
+    def evx_params(self, dt=0.0):
+        """float32 roundings of the python-double constants the reference evaluates."""
+        p = _lib.EvxChParams()
+        f = lambda x: float(np.float32(x))  # noqa: E731
+        p.D = f(self.D)
+        p.kappa = f(2 * self.eps)
+        p.w = f(self._w)
+        p.A = f(self.A)
+        p.sym_coef = f(-2 * self.eps * self.D * self.A)
+        p.dt = f(dt)
+        return p
+
+    def rhs(self, t, u):
+        """``CahnHilliard.rhs`` on the GPU (evoxels/problem_definition.py:328-371)."""
+        u = self.vg.check_field(u)
+        out = torch.empty_like(u)
+        g = self.vg.evx_grid()
+        p = self.evx_params()
+        L = _lib.lib()
+        for ch in range(u.shape[0]):
+            _lib.check(L.evx_ch_rhs(u[ch].data_ptr(), out[ch].data_ptr(), g, self._evx_bc, p, cuda_stream()),
+                       "evx_ch_rhs")
+        return out
+
+
+@dataclass
+class ReactionDiffusion(_BCMixin):
+    vg: VoxelGridGB300
+    D: float
+    f: Callable | None = None
+    A: float = 0.25
+    bc: tuple = ("periodic", "periodic", "periodic")
+    _fourier_symbol: Any = field(init=False, repr=False, default=None)
+
+    def __post_init__(self):
+        if self.f is not None:
+            probe = _eval_callable(self.f, 0.0, torch.zeros(2, dtype=torch.float64))
+            if not (isinstance(probe, (int, float)) and probe == 0):
+                raise NotImplementedError("evoxels_gb300 implements ReactionDiffusion with f = 0 only")
+        else:
+            self.f = lambda c=None, t=None, lib=None: 0
+        self.initialize_boundary_conditions()
+
+    @property
+    def order(self):
+        return 2
+
+    @property
+    def fourier_symbol(self):
+        if self._fourier_symbol is None:
+            self._fourier_symbol = -self.D * self.A * self.k_squared()
+        return self._fourier_symbol
+
+    def rhs(self, t, u):
+        """``D*laplace(pad_bc(u)) + 0`` on the GPU (evoxels/problem_definition.py:226-229)."""
+        u = self.vg.check_field(u)
+        out = torch.empty_like(u)
+        g = self.vg.evx_grid()
+        L = _lib.lib()
+        for ch in range(u.shape[0]):
+            _lib.check(L.evx_rd_rhs(u[ch].data_ptr(), out[ch].data_ptr(), g, self._evx_bc,
+                                    float(np.float32(self.D)), cuda_stream()), "evx_rd_rhs")
+        return out

@@ -1,0 +1,134 @@
+"""Solver loop: the reference's ``TimeDependentSolver`` on the CUDA backend.
+
+Same dataclass fields, ``solve`` keywords, frame schedule, NaN abort and
+printed timing line as evoxels/solvers.py:12-208.  Between output frames the
+loop hands whole runs of steps to the stepper's ``advance`` (one library call
+per frame interval) when the stepper has one; a user ``step_fn`` is called
+step by step exactly as in the reference.
+"""
+
+from __future__ import annotations
+
+import sys
+from dataclasses import dataclass
+from timeit import default_timer as timer
+from typing import Any, Callable
+
+import numpy as np
+import torch
+
+from .voxelgrid import VoxelGridGB300
+
+
+class TorchMemoryProfiler:
+    """Wall-time and device-memory report (evoxels/profiler.py:44-81, GPU branch)."""
+
+    def __init__(self, device):
+        self.device = device
+        torch.cuda.reset_peak_memory_stats(device=device)
+
+    def update_memory_stats(self):
+        pass
+
+    def print_memory_stats(self, start, end, iters):
+        print(f"Wall time: {np.around(end - start, 4)} s after {iters} iterations "
+              f"({np.around((end - start) / iters, 4)} s/iter)")
+        print(f"GPU-RAM (torch)       current: "
+              f"{torch.cuda.memory_allocated(self.device) / 1024**2:.2f} MB "
+              f"({torch.cuda.max_memory_allocated(self.device) / 1024**2:.2f} MB max, "
+              f"{torch.cuda.max_memory_reserved(self.device) / 1024**2:.2f} MB reserved)")
+
+
+@dataclass
+class BaseSolver:
+    """Generic wrapper for solving one or more fields with a time stepper (evoxels/solvers.py:12-114)."""
+    vf: Any
+    fieldnames: Any
+    backend: str
+    problem_cls: Any = None
+    timestepper_cls: Any = None
+    step_fn: Callable | None = None
+    device: str = "cuda"
+
+    def __post_init__(self):
+        if self.backend not in ("torch", "gb300"):
+            raise ValueError(f"Unsupported backend: {self.backend}")
+        self.vg = VoxelGridGB300(self.vf.grid_info(), precision=self.vf.precision, device=self.device)
+        self.profiler = TorchMemoryProfiler(self.vg.device)
+        if isinstance(self.fieldnames, str):
+            self.fieldnames = [self.fieldnames]
+        else:
+            self.fieldnames = list(self.fieldnames)
+
+    def _init_fields(self):
+        u_list = [self.vg.init_scalar_field(self.vf.fields[name]) for name in self.fieldnames]
+        u = self.vg.concatenate(u_list, 0)
+        return self.vg.bc.trim_boundary_nodes(u)
+
+    def _init_stepper(self, time_increment, problem_kwargs, jit):
+        """``jit`` is accepted for signature parity; the step is compiled CUDA already."""
+        problem_kwargs = problem_kwargs or {}
+        self._stepper = None
+        if self.step_fn is not None:
+            self.problem = None
+            return self.step_fn
+        if self.problem_cls is None or self.timestepper_cls is None:
+            raise ValueError("Either provide step_fn or both problem_cls and timestepper_cls")
+        self.problem = self.problem_cls(self.vg, **problem_kwargs)
+        self._stepper = self.timestepper_cls(self.problem, time_increment)
+        return self._stepper.step
+
+    def solve(self, time_increment=0.1, frames=10, max_iters=100, problem_kwargs=None, jit=True,
+              verbose=True, vtk_out=False, plot_bounds=None, colormap="viridis"):
+        u = self._init_fields()
+        step = self._init_stepper(time_increment, problem_kwargs, jit)
+        torch.cuda.synchronize(self.vg.device)
+        start = timer()
+        u = self._run_loop(u, step, time_increment, frames, max_iters, vtk_out, verbose, plot_bounds, colormap)
+        torch.cuda.synchronize(self.vg.device)
+        end = timer()
+        self.computation_time = end - start
+        if verbose:
+            self.profiler.print_memory_stats(start, end, max_iters)
+
+    def _export_fields(self, u_out):
+        for i, name in enumerate(self.fieldnames):
+            self.vf.set_field(name, self.vg.export_scalar_field_to_numpy(u_out[i:i + 1]))
+
+    def _handle_outputs(self, u, frame, time, vtk_out, verbose, plot_bounds, colormap):
+        """Export, NaN abort, optional VTK (evoxels/solvers.py:152-187; no plotting)."""
+        u_out = u  # trim_ghost_nodes(pad_bc(u)) == u for cell-centred grids
+        self._export_fields(u_out)
+        if any(np.isnan(self.vf.fields[name]).any() for name in self.fieldnames):
+            print(f"NaN detected in frame {frame} at time {time}. Aborting simulation.")
+            sys.exit(1)
+        if vtk_out:
+            cls = self.problem_cls.__name__ if self.problem_cls is not None else "step_fn"
+            filename = cls + "_" + self.fieldnames[0] + f"_{frame:03d}.vtk"
+            self.vf.export_to_vtk(filename=filename, field_names=self.fieldnames)
+
+
+@dataclass
+class TimeDependentSolver(BaseSolver):
+    """Fixed-step time loop with ``frames`` evenly spaced exports (evoxels/solvers.py:189-208)."""
+
+    def _run_loop(self, u, step, time_increment, frames, max_iters, vtk_out, verbose, plot_bounds, colormap):
+        n_out = max_iters // frames
+        frame = 0
+        advance = getattr(self._stepper, "advance", None)
+        i = 0
+        while i < max_iters:
+            time = i * time_increment
+            if i % n_out == 0:
+                self._handle_outputs(u, frame, time, vtk_out, verbose, plot_bounds, colormap)
+                frame += 1
+            if advance is not None:
+                n = min(n_out - i % n_out, max_iters - i)
+                u = advance(u, n)
+                i += n
+            else:
+                u = step(time, u)
+                i += 1
+        time = max_iters * time_increment
+        self._handle_outputs(u, frame, time, vtk_out, verbose, plot_bounds, colormap)
+        return u

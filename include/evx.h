@@ -1,0 +1,179 @@
+/*
+ * evx.h - C ABI of the GB300 (sm_103a) evoxels time-stepping library (libevx.so).
+ *
+ * Plain pointers and sizes only.  Field arguments are device pointers to
+ * C-contiguous float32 arrays of shape (Nx, Ny, Nz), z fastest - one channel
+ * of the reference's (C, Nx, Ny, Nz) torch layout (evoxels/voxelgrid.py:126-130).
+ * Every call is stream-ordered on the cudaStream_t it is given (passed as
+ * void*; NULL = legacy default stream) and returns an int status (EVX_OK = 0);
+ * evx_last_error() gives the message of the last failure on the calling
+ * thread.  No C++ exception crosses this boundary.  Calls never mutate their
+ * input fields (the reference's steps are functional: evoxels/solvers.py:204).
+ *
+ * Workspaces are caller-allocated device memory; the library allocates no
+ * device memory of its own except inside evx_ch_plan_create (k^2 tables).
+ */
+#ifndef EVX_H
+#define EVX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define EVX_OK               0
+#define EVX_ERR_BAD_SHAPE    1  /* reference: ValueError (evoxels/boundary_conditions.py:76-82) */
+#define EVX_ERR_BAD_ARG      2
+#define EVX_ERR_BAD_BC       3  /* reference: ValueError (evoxels/problem_definition.py:67-102) */
+#define EVX_ERR_CUFFT        4
+#define EVX_ERR_CUDA         5
+#define EVX_ERR_NONFINITE    6  /* reference: NaN abort (evoxels/solvers.py:163-165) */
+#define EVX_ERR_TOO_LARGE    7
+#define EVX_ERR_WORKSPACE    8
+#define EVX_ERR_UNSUPPORTED  9  /* reference: NotImplementedError (evoxels/problem_definition.py:151-155) */
+
+/* ---- boundary conditions (evoxels/boundary_conditions.py:9-59) --------- */
+#define EVX_BC_PERIODIC   0
+#define EVX_BC_NEUMANN    1   /* ghost = first/last interior value */
+#define EVX_BC_DIRICHLET  2   /* ghost = 2*v - first/last interior value */
+
+typedef struct evx_bc {
+    int32_t kind[3];      /* x, y, z */
+    float   two_v_lo[3];  /* float32(2.0*v_left)  of Dirichlet axes (0 otherwise) */
+    float   two_v_hi[3];  /* float32(2.0*v_right) of Dirichlet axes (0 otherwise) */
+} evx_bc;
+
+/* Grid geometry: shape, the spacing as the reference's python doubles
+ * (VoxelFields.spacing, evoxels/voxelfields.py:84-86; used for the k-grid),
+ * and the float32 div_dx / div_dx2 factors (evoxels/voxelgrid.py:29-30) with
+ * float32 sum(div_dx2) (evoxels/fd_stencils.py:74) used by the stencils. */
+typedef struct evx_grid {
+    int32_t nx, ny, nz, reserved;
+    double  h[3];
+    float   inv_h[3];
+    float   inv_h2[3];
+    float   inv_h2_sum;
+} evx_grid;
+
+/* Cahn-Hilliard parameters (evoxels/problem_definition.py:290-305), each the
+ * float32 rounding of the python-double expression the reference evaluates:
+ *   D        = D
+ *   kappa    = 2*eps                      (gradient coefficient, mu = mu_hom - kappa*lap)
+ *   w        = 18/eps by default          (mu_hom = w*c*(1-c)*(1-2c))
+ *   A        = A (0.25)
+ *   sym_coef = -2*eps*D*A                 (fourier_symbol = sym_coef*(k^2)^2)
+ *   dt       = dt                         (prefac = dt/(1 - dt*symbol), evoxels/timesteppers.py:77) */
+typedef struct evx_ch_params {
+    float D, kappa, w, A, sym_coef, dt;
+} evx_ch_params;
+
+/* ---- library info -------------------------------------------------------- */
+const char* evx_last_error(void);
+int evx_version(void);
+
+/* Host-only: per-axis k^2 tables exactly as VoxelGrid.rfft_k_squared builds
+ * them in float32 (evoxels/voxelgrid.py:84-90,110-114): kx2[nx], ky2[ny],
+ * kz2[nz/2+1]; k^2(i,j,k) = (kx2[i] + ky2[j]) + kz2[k].  Needs no GPU. */
+int evx_k2_tables_host(int nx, int ny, int nz, double hx, double hy, double hz,
+                       float* kx2, float* ky2, float* kz2);
+
+/* ---- finite-difference stencil path ------------------------------------- */
+
+/* ReactionDiffusion.rhs with f = 0: r = D*laplace(pad_bc(u))
+ * (evoxels/problem_definition.py:226-229, evoxels/fd_stencils.py:62-75). */
+int evx_rd_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc,
+               float D, void* stream);
+
+/* nsteps ForwardEuler steps of ReactionDiffusion (f = 0):
+ * u <- u + dt*(D*laplace(pad_bc(u)) + 0)   (evoxels/timesteppers.py:42-43).
+ * u_in is read only; the result lands in u_out.  scratch: one field
+ * (Nx*Ny*Nz floats) used as the ping-pong buffer when nsteps > 1 (may be
+ * NULL when nsteps == 1).  steps_per_pass in {1,2,4} selects temporal
+ * blocking (results are bit-identical for every choice). */
+int evx_fd_forward(const float* u_in, float* u_out, float* scratch,
+                   const evx_grid* g, const evx_bc* bc, float D, float dt,
+                   int nsteps, int steps_per_pass, void* stream);
+
+/* Adjoint of evx_fd_forward with respect to u_in: lam_out = (dU_n/dU_0)^T lam_in.
+ * The transposed stencil uses homogeneous ghosts (a Dirichlet ghost 2v-u0
+ * contributes -1*u0, a Neumann ghost +1*u0).  scratch as above. */
+int evx_fd_adjoint(const float* lam_in, float* lam_out, float* scratch,
+                   const evx_grid* g, const evx_bc* bc, float D, float dt,
+                   int nsteps, void* stream);
+
+/* ForwardEuler update out = u + dt*r (evoxels/timesteppers.py:43) for a
+ * precomputed right-hand side, n elements. */
+int evx_fe_update(const float* u, const float* r, float dt, float* out, size_t n, void* stream);
+
+/* ---- Cahn-Hilliard path ---------------------------------------------------- */
+
+/* CahnHilliard.rhs (evoxels/problem_definition.py:328-371) for any BC. */
+int evx_ch_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc,
+               const evx_ch_params* p, void* stream);
+
+typedef struct evx_ch_plan evx_ch_plan;
+
+/* Plan for the periodic pseudo-spectral IMEX step (evoxels/timesteppers.py:64-89)
+ * on an (nx, ny, nz) grid: cuFFT R2C/C2R plans without auto-allocated work
+ * areas, and the k^2 tables.  flags: bit 0 = also build the batch-2 C2R plan
+ * used by parameter gradients. */
+int evx_ch_plan_create(evx_ch_plan** plan, const evx_grid* g, int flags);
+int evx_ch_plan_destroy(evx_ch_plan* plan);
+
+/* Bytes of device workspace (256-byte aligned start) the plan's calls need. */
+size_t evx_ch_workspace_bytes(const evx_ch_plan* plan);
+
+/* One PseudoSpectralIMEX step of CahnHilliard (evoxels/timesteppers.py:85-89):
+ * u_out = u_in + irfftn(prefac * rfftn(rhs(u_in))).  u_in is read only. */
+int evx_ch_step(evx_ch_plan* plan, const float* u_in, float* u_out,
+                const evx_ch_params* p, void* workspace, void* stream);
+
+/* nsteps IMEX steps, the update of each step fused into the next step's rhs
+ * pass.  traj (optional, NULL for none) receives states u_1..u_n as nsteps
+ * consecutive fields; u_out receives u_n.  nonfinite (optional device int)
+ * is set to 1 if the final state holds a NaN or Inf. */
+int evx_ch_forward(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps,
+                   float* traj, const evx_ch_params* p, int* nonfinite,
+                   void* workspace, void* stream);
+
+/* Adjoint of nsteps IMEX steps.  states: nsteps+1 consecutive fields u_0..u_n
+ * of the forward trajectory; lam_in = dL/du_n; lam_out = dL/du_0.
+ * grads (optional device double[3]) accumulates dL/dD, dL/dkappa, dL/dw
+ * (kappa, w as in evx_ch_params; needs a plan made with flags bit 0).
+ * lam_in is read only. */
+int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps,
+                   const float* lam_in, float* lam_out, const evx_ch_params* p,
+                   double* grads, void* workspace, void* stream);
+
+/* ---- inversion loss ---------------------------------------------------------- */
+
+/* loss = mean((u - target)^2) (device double) and, if lam != NULL, its gradient
+ * lam = 2*(u - target)/n: the seed of the adjoint for the parameter-estimation
+ * workflow (evoxels/inversion.py:105-124 fits simulated to observed fields).
+ * scratch: evx_mse_scratch_bytes(n) bytes of device memory for partial sums. */
+size_t evx_mse_scratch_bytes(size_t n);
+int evx_mse_grad(const float* u, const float* target, size_t n, float* lam, double* loss,
+                 void* scratch, size_t scratch_bytes, void* stream);
+
+/* ---- instrumentation ------------------------------------------------------ */
+
+/* Per-kernel timing: when enabled, every kernel launch and cuFFT execution of
+ * the library is bracketed by CUDA events on its stream.  collect() waits for
+ * them and accumulates milliseconds per named slot; query() walks the slots
+ * (returns -1 past the last).  Off by default. */
+void evx_prof_enable(int on);
+int evx_prof_collect(void);
+void evx_prof_reset(void);
+int evx_prof_query(int index, char* name, int name_cap, double* total_ms, long long* count);
+
+/* Number of this library's own kernel launches since load (cuFFT's excluded). */
+unsigned long long evx_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EVX_H */

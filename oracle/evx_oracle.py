@@ -1,0 +1,367 @@
+"""Operation-by-operation CPU restatement of the reference's hot path.
+
+TEST INFRASTRUCTURE ONLY: the oracle the CUDA path is checked against.  Every
+function names the reference file:line whose arithmetic it follows (paths are
+relative to the evoxels project root).  Floating-point operations are written
+in the same order and association as the reference so that, in fp32, the
+finite-difference parts reproduce the reference's rounding exactly.
+
+Fields are torch CPU tensors of shape ``(C, Nx, Ny, Nz)`` (z fastest), the
+layout ``VoxelGridTorch.init_scalar_field`` produces (evoxels/voxelgrid.py:126-130).
+
+Boundary conditions use the reference's normalised form
+``((kind, values), (kind, values), (kind, values))`` for the x, y, z axes,
+``kind`` in {'periodic', 'neumann', 'dirichlet'}
+(evoxels/problem_definition.py:60-115).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+__all__ = [
+    "normalize_bc",
+    "pad_periodic",
+    "pad_bc",
+    "grid_factors",
+    "laplace",
+    "to_face",
+    "grad_face",
+    "ch_rhs",
+    "rd_rhs",
+    "rfft_k_squared",
+    "imex_prefac",
+    "imex_step",
+    "fe_step",
+    "ch_imex_run",
+    "rd_fe_run",
+    "ch_imex_vjp",
+    "ch_imex_loss_grads",
+    "seeded_ch_field",
+    "seeded_unit_field",
+    "rel_to_max",
+]
+
+_SLAB = slice(1, -1)
+
+
+# ----------------------------------------------------------------------------
+# Boundary conditions
+# ----------------------------------------------------------------------------
+
+def normalize_bc(bc):
+    """Normalise a BC spec the way evoxels/problem_definition.py:60-103 does.
+
+    ``None`` or ``'fully_periodic'`` -> periodic on all axes
+    (evoxels/problem_definition.py:62-65).  Raises ``ValueError`` with the
+    reference's messages for malformed specs.
+    """
+    if bc is None or bc == "fully_periodic":
+        return (("periodic", None),) * 3
+    if len(bc) != 3:
+        raise ValueError("bc must contain exactly three axis entries ordered as (x, y, z).")
+    out = []
+    for axis_bc in bc:
+        if isinstance(axis_bc, str):
+            if axis_bc == "dirichlet":
+                raise ValueError("Dirichlet BCs require explicit values ('dirichlet', (left, right)).")
+            if axis_bc not in {"periodic", "neumann"}:
+                raise ValueError(f"Unsupported BC type: {axis_bc}")
+            out.append((axis_bc, None))
+            continue
+        if len(axis_bc) != 2:
+            raise ValueError(
+                "Each axis boundary specification must be either a string or "
+                "a tuple like ('dirichlet', (left, right))."
+            )
+        kind, values = axis_bc
+        if kind not in {"periodic", "dirichlet", "neumann"}:
+            raise ValueError(f"Unsupported BC type: {kind}")
+        if kind == "dirichlet":
+            if values is None or len(values) != 2:
+                raise ValueError("Dirichlet BCs require two boundary values.")
+            out.append((kind, tuple(values)))
+        else:
+            if values is not None:
+                raise ValueError(f"{kind} BCs do not accept boundary values.")
+            out.append((kind, None))
+    return tuple(out)
+
+
+def pad_periodic(field):
+    """Circular ghost layer of width 1 (evoxels/voxelgrid.py:194-195)."""
+    return torch.nn.functional.pad(field, (1, 1, 1, 1, 1, 1), mode="circular")
+
+
+def pad_bc(field, bc):
+    """Generic cell-centred ghost padding (evoxels/boundary_conditions.py:33-59).
+
+    Periodic pad first, then per axis in x, y, z order: Neumann copies the
+    first/last interior slab into the ghost slab, Dirichlet writes
+    ``2*v - interior``.  The specialised forms
+    (evoxels/boundary_conditions.py:16-31) give identical values.
+    """
+    bc = normalize_bc(bc)
+    padded = pad_periodic(field)
+    for axis, (kind, values) in enumerate(bc):
+        if kind == "periodic":
+            continue
+        dim = axis + 1
+
+        def sl(i):
+            idx = [slice(None)] * 4
+            idx[dim] = i
+            return tuple(idx)
+
+        if kind == "neumann":
+            padded[sl(0)] = padded[sl(1)]
+            padded[sl(-1)] = padded[sl(-2)]
+        elif kind == "dirichlet":
+            padded[sl(0)] = 2.0 * values[0] - padded[sl(1)]
+            padded[sl(-1)] = 2.0 * values[1] - padded[sl(-2)]
+        else:  # pragma: no cover - normalize_bc rejects it
+            raise ValueError(f"Unsupported BC type: {kind}")
+    return padded
+
+
+# ----------------------------------------------------------------------------
+# Stencils (evoxels/fd_stencils.py)
+# ----------------------------------------------------------------------------
+
+def grid_factors(spacing, dtype):
+    """``div_dx``, ``div_dx2`` as the reference builds them (evoxels/voxelgrid.py:29-30)."""
+    sp = torch.tensor(np.array(spacing), dtype=dtype)
+    return 1 / sp, 1 / sp ** 2
+
+
+def laplace(padded, div_dx2):
+    """Compact 7-point Laplacian on a padded field (evoxels/fd_stencils.py:62-75)."""
+    c = padded[:, 1:-1, 1:-1, 1:-1]
+    left, right = padded[:, :-2, 1:-1, 1:-1], padded[:, 2:, 1:-1, 1:-1]
+    bottom, top = padded[:, 1:-1, :-2, 1:-1], padded[:, 1:-1, 2:, 1:-1]
+    back, front = padded[:, 1:-1, 1:-1, :-2], padded[:, 1:-1, 1:-1, 2:]
+    return (right + left) * div_dx2[0] + \
+           (top + bottom) * div_dx2[1] + \
+           (front + back) * div_dx2[2] - \
+           2 * c * torch.sum(div_dx2)
+
+
+def to_face(field, axis):
+    """Face average ``0.5*(f[i+1] + f[i])`` along ``axis`` (evoxels/fd_stencils.py:20-30)."""
+    d = axis + 1
+    n = field.shape[d]
+    return 0.5 * (field.narrow(d, 1, n - 1) + field.narrow(d, 0, n - 1))
+
+
+def grad_face(field, axis, div_dx):
+    """Face gradient ``(f[i+1] - f[i]) * 1/h`` along ``axis`` (evoxels/fd_stencils.py:32-42)."""
+    d = axis + 1
+    n = field.shape[d]
+    return (field.narrow(d, 1, n - 1) - field.narrow(d, 0, n - 1)) * div_dx[axis]
+
+
+# ----------------------------------------------------------------------------
+# Right-hand sides (evoxels/problem_definition.py)
+# ----------------------------------------------------------------------------
+
+def _default_mu_hom(eps):
+    # evoxels/problem_definition.py:304-305
+    return lambda c, lib=None: 18 / eps * c * (1 - c) * (1 - 2 * c)
+
+
+def ch_rhs(u, eps=3.0, D=1.0, bc=None, spacing=(1.0, 1.0, 1.0), mu_hom=None):
+    """``CahnHilliard.rhs`` (evoxels/problem_definition.py:328-371).
+
+    ``c = clip(u,0,1)``; ``mu = mu_hom(c) - 2*eps*laplace(pad_bc(c))``;
+    ``rhs = D * sum_axes grad_face( to_face(c)*(1-to_face(c)) * grad_face(pad_bc(mu)) )``.
+    ``eps`` and ``D`` may be python floats or 0-d tensors (autograd use).
+    """
+    bc = normalize_bc(bc)
+    div_dx, div_dx2 = grid_factors(spacing, u.dtype)
+    if mu_hom is None:
+        mu_hom = _default_mu_hom(eps)
+    c = torch.clip(u, 0, 1)
+    c_bc = pad_bc(c, bc)
+    lap = laplace(c_bc, div_dx2)
+    try:
+        mh = mu_hom(c, torch)
+    except TypeError:
+        mh = mu_hom(c)
+    mu = mh - 2 * eps * lap
+    mu = pad_bc(mu, bc)
+
+    inner = [(slice(None), slice(None), slice(1, -1), slice(1, -1)),
+             (slice(None), slice(1, -1), slice(None), slice(1, -1)),
+             (slice(None), slice(1, -1), slice(1, -1), slice(None))]
+    divergence = None
+    for axis in range(3):
+        cf = to_face(c_bc, axis)
+        flux = cf * (1 - to_face(c_bc, axis)) * grad_face(mu, axis, div_dx)
+        term = grad_face(flux, axis, div_dx)[inner[axis]]
+        divergence = term if divergence is None else divergence + term
+    return D * divergence
+
+
+def rd_rhs(u, D=1.0, bc=None, spacing=(1.0, 1.0, 1.0), f=None, t=0.0):
+    """``ReactionDiffusion.rhs`` (evoxels/problem_definition.py:226-229).
+
+    ``D*laplace(pad_bc(u)) + f(t, u)``; the default source is the python int 0
+    (evoxels/problem_definition.py:202-203).
+    """
+    bc = normalize_bc(bc)
+    _, div_dx2 = grid_factors(spacing, u.dtype)
+    lap = laplace(pad_bc(u, bc), div_dx2)
+    if f is None:
+        src = 0
+    else:
+        try:
+            src = f(t, u, torch)
+        except TypeError:
+            src = f(t, u)
+    return D * lap + src
+
+
+# ----------------------------------------------------------------------------
+# Spectral machinery (evoxels/voxelgrid.py:84-114, evoxels/timesteppers.py:64-89)
+# ----------------------------------------------------------------------------
+
+def rfft_k_squared(shape, spacing=(1.0, 1.0, 1.0), dtype=torch.float32):
+    """``VoxelGrid.rfft_k_squared`` (evoxels/voxelgrid.py:84-90,110-114).
+
+    ``k_i = 2*pi*fftfreq(n_i, h_i)`` on x and y, ``2*pi*rfftfreq`` on z, summed
+    as ``kx**2 + ky**2 + kz**2`` on an ``ij`` mesh, in ``dtype`` (the reference
+    uses torch's default dtype here).
+    """
+    ax = [2 * torch.pi * torch.fft.fftfreq(n, d, dtype=dtype) for n, d in zip(shape, spacing)]
+    az = 2 * torch.pi * torch.fft.rfftfreq(shape[2], spacing[2], dtype=dtype)
+    kx, ky, kz = torch.meshgrid(ax[0], ax[1], az, indexing="ij")
+    return kx ** 2 + ky ** 2 + kz ** 2
+
+
+def imex_prefac(shape, dt, eps=3.0, D=1.0, A=0.25, spacing=(1.0, 1.0, 1.0), dtype=torch.float32):
+    """``PseudoSpectralIMEX._fft_prefac`` for ``CahnHilliard``.
+
+    ``symbol = -2*eps*D*A*(k^2)^2`` (evoxels/problem_definition.py:303) and
+    ``prefac = dt / (1 - dt*symbol)`` (evoxels/timesteppers.py:77).
+    """
+    k2 = rfft_k_squared(shape, spacing, dtype)
+    symbol = -2 * eps * D * A * k2 ** 2
+    return dt / (1 - dt * symbol)
+
+
+def imex_step(u, prefac, rhs_fn):
+    """``PseudoSpectralIMEX.step`` for a periodic problem (evoxels/timesteppers.py:85-89).
+
+    The FFT pad is the identity for periodic x (evoxels/boundary_conditions.py:61-63);
+    the transform runs over the full 4-D shape including the channel axis.
+    """
+    dc = rhs_fn(u)
+    dc_fft = prefac * torch.fft.rfftn(dc, s=dc.shape)
+    update = torch.fft.irfftn(dc_fft, s=dc.shape)[:, :u.shape[1]]
+    return u + update
+
+
+def fe_step(u, dt, rhs_fn):
+    """``ForwardEuler.step`` (evoxels/timesteppers.py:42-43): ``u + dt*rhs``."""
+    return u + dt * rhs_fn(u)
+
+
+def ch_imex_run(u0, nsteps, dt=0.1, eps=3.0, D=1.0, A=0.25, spacing=(1.0, 1.0, 1.0),
+                mu_hom=None, k_dtype=None, keep=None):
+    """``nsteps`` Cahn-Hilliard IMEX steps from ``u0``; returns the final state.
+
+    ``keep`` (optional list) receives every intermediate state, ``u0`` first.
+    """
+    shape = tuple(u0.shape[1:])
+    prefac = imex_prefac(shape, dt, eps, D, A, spacing, k_dtype or u0.dtype)
+    u = u0
+    if keep is not None:
+        keep.append(u)
+    for _ in range(nsteps):
+        u = imex_step(u, prefac, lambda v: ch_rhs(v, eps, D, None, spacing, mu_hom))
+        if keep is not None:
+            keep.append(u)
+    return u
+
+
+def rd_fe_run(u0, nsteps, dt, D=1.0, bc=None, spacing=(1.0, 1.0, 1.0)):
+    """``nsteps`` ``ForwardEuler`` steps of ``ReactionDiffusion`` with ``f = 0``."""
+    u = u0
+    for _ in range(nsteps):
+        u = fe_step(u, dt, lambda v: rd_rhs(v, D, bc, spacing))
+    return u
+
+
+# ----------------------------------------------------------------------------
+# Adjoint oracle: torch autograd through the restated step
+# ----------------------------------------------------------------------------
+
+def ch_imex_vjp(u, lam, dt=0.1, eps=3.0, D=1.0, A=0.25, spacing=(1.0, 1.0, 1.0), mu_hom=None):
+    """Vector-Jacobian product of one IMEX step: returns ``(J^T lam, dD, deps)``.
+
+    ``dD``/``deps`` are the contributions of this step to the parameter
+    gradients when ``D`` and ``eps`` enter both the rhs and the spectral
+    prefactor (``eps`` also sets the default bulk term ``18/eps`` unless
+    ``mu_hom`` pins it).
+    """
+    u = u.detach().clone().requires_grad_(True)
+    Dt = torch.tensor(float(D), dtype=u.dtype, requires_grad=True)
+    et = torch.tensor(float(eps), dtype=u.dtype, requires_grad=True)
+    shape = tuple(u.shape[1:])
+    k2 = rfft_k_squared(shape, spacing, u.dtype)
+    prefac = dt / (1 - dt * (-2 * et * Dt * A * k2 ** 2))
+    mh = mu_hom if mu_hom is not None else (lambda c, lib=None: 18 / et * c * (1 - c) * (1 - 2 * c))
+    out = imex_step(u, prefac, lambda v: ch_rhs(v, et, Dt, None, spacing, mh))
+    gu, gD, ge = torch.autograd.grad(out, (u, Dt, et), grad_outputs=lam)
+    return gu.detach(), float(gD), float(ge)
+
+
+def ch_imex_loss_grads(c0, target, nsteps, dt=0.1, eps=3.0, D=1.0, A=0.25,
+                       spacing=(1.0, 1.0, 1.0), mu_hom=None):
+    """Loss ``mean((u_T - target)^2)`` and its gradients w.r.t. ``c0``, ``D``, ``eps``.
+
+    Torch autograd through ``nsteps`` restated IMEX steps (the reference has no
+    torch gradient path of its own; this is the autograd-through-the-reference
+    construction, evoxels/problem_definition.py:290-371 with tensor ``D``/``eps``).
+    """
+    c0 = c0.detach().clone().requires_grad_(True)
+    Dt = torch.tensor(float(D), dtype=c0.dtype, requires_grad=True)
+    et = torch.tensor(float(eps), dtype=c0.dtype, requires_grad=True)
+    shape = tuple(c0.shape[1:])
+    k2 = rfft_k_squared(shape, spacing, c0.dtype)
+    prefac = dt / (1 - dt * (-2 * et * Dt * A * k2 ** 2))
+    mh = mu_hom if mu_hom is not None else (lambda c, lib=None: 18 / et * c * (1 - c) * (1 - 2 * c))
+    u = c0
+    for _ in range(nsteps):
+        u = imex_step(u, prefac, lambda v: ch_rhs(v, et, Dt, None, spacing, mh))
+    loss = torch.mean((u - target) ** 2)
+    g0, gD, ge = torch.autograd.grad(loss, (c0, Dt, et))
+    return float(loss.detach()), g0.detach(), float(gD), float(ge)
+
+
+# ----------------------------------------------------------------------------
+# Seeded inputs and error metric
+# ----------------------------------------------------------------------------
+
+def seeded_ch_field(shape, seed):
+    """``0.5 + 0.1*U[0,1)`` from ``np.random.default_rng(seed)`` (float64, ``(Nx,Ny,Nz)``)."""
+    rng = np.random.default_rng(seed)
+    return 0.5 + 0.1 * rng.random(tuple(shape))
+
+
+def seeded_unit_field(shape, seed):
+    """``U[0,1)`` from ``np.random.default_rng(seed)`` (float64, ``(Nx,Ny,Nz)``)."""
+    rng = np.random.default_rng(seed)
+    return rng.random(tuple(shape))
+
+
+def rel_to_max(a, ref):
+    """``max|a - ref| / max|ref|`` in float64."""
+    a = np.asarray(a, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    den = float(np.max(np.abs(ref)))
+    if den == 0.0:
+        return float(np.max(np.abs(a - ref)))
+    return float(np.max(np.abs(a - ref)) / den)
+

@@ -1,0 +1,187 @@
+"""Generate the golden fixtures in this folder by running the evoxels reference.
+
+Run in a container that has the reference checked out (path in ``EVOXELS_REF``,
+default ``/root/reference``) and torch on CPU::
+
+    python tests/golden/make_golden.py
+
+The reference package is imported with a small shim: ``matplotlib`` is absent
+here, so stub modules stand in for it (only plotting uses it), and the package
+``__init__`` is bypassed because it imports the JAX-only inversion module.
+Everything that produces numbers below is the reference's own code:
+``CahnHilliard.rhs``, ``ReactionDiffusion.rhs``, ``PseudoSpectralIMEX``,
+``ForwardEuler``, ``CellCenteredBCs.pad_bc`` and ``run_cahn_hilliard_solver``,
+all on ``device='cpu'``, ``jit=False``.
+
+Each fixture is a small ``.npz`` (fields of at most 16^3 voxels).  Inputs are
+the seeded float64 arrays the product and the oracle both consume.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import types
+import warnings
+
+import numpy as np
+import torch
+
+REF = os.environ.get("EVOXELS_REF", "/root/reference")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def import_reference():
+    """Import the reference's torch-path modules without matplotlib/JAX."""
+    for name in ("matplotlib", "matplotlib.pyplot", "matplotlib.widgets", "matplotlib.patches"):
+        if name not in sys.modules:
+            mod = types.ModuleType(name)
+            sys.modules[name] = mod
+    sys.modules["matplotlib.widgets"].Slider = object
+    sys.modules["matplotlib.patches"].Patch = object
+    sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+    if "evoxels" not in sys.modules:
+        pkg = types.ModuleType("evoxels")
+        pkg.__path__ = [os.path.join(REF, "evoxels")]
+        sys.modules["evoxels"] = pkg
+    import importlib
+    mods = {}
+    for m in ("voxelfields", "voxelgrid", "problem_definition", "timesteppers",
+              "solvers", "precompiled_solvers.cahn_hilliard"):
+        mods[m] = importlib.import_module("evoxels." + m)
+    return mods
+
+
+def ch_field(shape, seed):
+    rng = np.random.default_rng(seed)
+    return 0.5 + 0.1 * rng.random(shape)
+
+
+def unit_field(shape, seed):
+    rng = np.random.default_rng(seed)
+    return rng.random(shape)
+
+
+def make_vg(R, shape, precision="float32", domain=None):
+    vf = R["voxelfields"].VoxelFields(shape, domain_size=domain or shape)
+    vf.precision = precision
+    return vf, R["voxelgrid"].VoxelGridTorch(vf.grid_info(), precision=precision, device="cpu")
+
+
+def main():
+    R = import_reference()
+    PD, TS = R["problem_definition"], R["timesteppers"]
+    warnings.simplefilter("ignore")
+    torch.set_default_dtype(torch.float32)
+    out = {}
+
+    # 1) the reference test's exact mixed-BC ghost golden (tests/test_solvers.py:105-126)
+    _, vg = make_vg(R, (2, 2, 2), domain=(1, 1, 1))
+    prob = PD.ReactionDiffusion(vg, D=1.0, bc=(("dirichlet", (10.0, 20.0)), "neumann", "periodic"))
+    field = vg.init_scalar_field(np.arange(1, 9, dtype=np.float32).reshape(2, 2, 2))
+    out["pad_mixed"] = dict(u=field.numpy(), padded=prob.pad_bc(field).numpy())
+
+    # 2) CahnHilliard.rhs, fp32, periodic and non-periodic, odd shapes, clip exercised
+    cases = [((8, 8, 8), 11, None, (1.0, 1.0, 1.0)),
+             ((5, 7, 9), 12, None, (1.0, 1.0, 1.0)),
+             ((12, 10, 6), 13, None, (0.5, 0.75, 1.25)),
+             ((9, 8, 7), 14, (("dirichlet", (0.2, 0.7)), "neumann", "periodic"), (1.0, 1.0, 1.0)),
+             ((6, 9, 8), 15, ("neumann", ("dirichlet", (0.0, 1.0)), "neumann"), (1.0, 1.0, 1.0))]
+    for i, (shape, seed, bc, spacing) in enumerate(cases):
+        domain = tuple(n * h for n, h in zip(shape, spacing))
+        _, vg = make_vg(R, shape, domain=domain)
+        u0 = ch_field(shape, seed)
+        if i == 1:  # push some voxels outside [0, 1] so clip matters
+            u0 = u0 + 0.8 * (unit_field(shape, 99) - 0.5)
+        kw = dict(eps=3.0, D=1.0)
+        if bc is not None:
+            kw["bc"] = bc
+        prob = PD.CahnHilliard(vg, **kw)
+        u = vg.init_scalar_field(u0)
+        r = prob.rhs(0.0, u)
+        out[f"ch_rhs_{i}"] = dict(u0=u0, rhs=r.numpy(), shape=np.array(shape),
+                                  spacing=np.array(spacing), bc=np.array(repr(bc)))
+
+    # 3) PseudoSpectralIMEX on CahnHilliard: 1 step and 10 steps, fp32, plus eps/D variants
+    for i, (shape, seed, eps, D, dt, n) in enumerate([((16, 16, 16), 21, 3.0, 1.0, 0.1, 1),
+                                                       ((16, 16, 16), 21, 3.0, 1.0, 0.1, 10),
+                                                       ((12, 10, 14), 22, 1.0, 0.7, 0.1, 10),
+                                                       ((10, 12, 9), 23, 2.5, 1.6, 0.05, 5)]):
+        _, vg = make_vg(R, shape)
+        prob = PD.CahnHilliard(vg, eps=eps, D=D)
+        st = TS.PseudoSpectralIMEX(prob, dt)
+        u0 = ch_field(shape, seed)
+        u = vg.init_scalar_field(u0)
+        for _ in range(n):
+            u = st.step(0.0, u)
+        out[f"ch_imex_{i}"] = dict(u0=u0, u=u.numpy(), shape=np.array(shape), eps=eps, D=D, dt=dt, n=n)
+
+    # 4) true FP64 CH IMEX (default dtype float64 so the k-grid is fp64 too)
+    torch.set_default_dtype(torch.float64)
+    shape = (16, 16, 16)
+    _, vg = make_vg(R, shape, precision="float64")
+    prob = PD.CahnHilliard(vg)
+    st = TS.PseudoSpectralIMEX(prob, 0.1)
+    u0 = ch_field(shape, 21)
+    u = vg.init_scalar_field(u0)
+    for _ in range(10):
+        u = st.step(0.0, u)
+    out["ch_imex_fp64"] = dict(u0=u0, u=u.numpy(), n=10)
+    torch.set_default_dtype(torch.float32)
+
+    # 5) ReactionDiffusion + ForwardEuler (the explicit FD path), generic and specialised pads
+    fd_cases = [((9, 8, 7), 31, (("dirichlet", (0, 0)), "neumann", "neumann"), 1.0 / 60, 10),
+                ((8, 8, 8), 32, None, 1.0 / 60, 10),
+                ((7, 9, 10), 33, (("dirichlet", (10.0, 20.0)), "neumann", "periodic"), 1.0 / 60, 5),
+                ((10, 6, 8), 34, ("neumann", "periodic", "periodic"), 1.0 / 60, 5),
+                ((6, 8, 12), 35, (("dirichlet", (1.0, -1.0)), "periodic", "periodic"), 1.0 / 60, 5)]
+    for i, (shape, seed, bc, dt, n) in enumerate(fd_cases):
+        _, vg = make_vg(R, shape)
+        kw = dict(D=1.0)
+        if bc is not None:
+            kw["bc"] = bc
+        prob = PD.ReactionDiffusion(vg, **kw)
+        st = TS.ForwardEuler(prob, dt)
+        u0 = unit_field(shape, seed)
+        u = vg.init_scalar_field(u0)
+        for _ in range(n):
+            u = st.step(0.0, u)
+        out[f"fd_fe_{i}"] = dict(u0=u0, u=u.numpy(), shape=np.array(shape), bc=np.array(repr(bc)),
+                                 dt=dt, n=n)
+
+    # 6) torch autograd through the reference: dL/dc0, dL/dD, dL/deps, fp64
+    torch.set_default_dtype(torch.float64)
+    shape = (8, 8, 8)
+    _, vg = make_vg(R, shape, precision="float64")
+    u0 = ch_field(shape, 41)
+    tgt = ch_field(shape, 42)
+    Dt = torch.tensor(1.3, requires_grad=True)
+    et = torch.tensor(2.0, requires_grad=True)
+    prob = PD.CahnHilliard(vg, eps=et, D=Dt)
+    st = TS.PseudoSpectralIMEX(prob, 0.1)
+    c0 = vg.init_scalar_field(u0).requires_grad_(True)
+    u = c0
+    for _ in range(5):
+        u = st.step(0.0, u)
+    loss = torch.mean((u - vg.init_scalar_field(tgt)) ** 2)
+    loss.backward()
+    out["ch_grad"] = dict(u0=u0, target=tgt, n=5, D=1.3, eps=2.0, dt=0.1, loss=float(loss),
+                          g_c0=c0.grad.numpy(), g_D=float(Dt.grad), g_eps=float(et.grad))
+    torch.set_default_dtype(torch.float32)
+
+    # 7) the drop-in driver end to end: run_cahn_hilliard_solver on CPU, fp32
+    vf = R["voxelfields"].VoxelFields((16, 16, 16), domain_size=(16, 16, 16))
+    u0 = ch_field((16, 16, 16), 51)
+    vf.add_field("c", u0.copy())
+    R["precompiled_solvers.cahn_hilliard"].run_cahn_hilliard_solver(
+        vf, "c", "torch", jit=False, device="cpu", time_increment=0.1, frames=2, max_iters=20,
+        verbose=False)
+    out["driver_ch"] = dict(u0=u0, c=vf.fields["c"], n=20)
+
+    for name, arrays in out.items():
+        np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrays)
+    print("wrote", len(out), "fixtures to", OUT)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,318 @@
+"""GPU parity of the CUDA path against the oracle and the reference's golden outputs.
+
+Bars (stated per test):
+* stencil right-hand sides and forward-Euler steps: bit-exact (same IEEE float32
+  operations in the reference's order);
+* one IMEX step: max|d|/max|ref| <= 1e-5 against the FP64 oracle; 1000 steps <= 1e-4;
+* adjoint: against torch autograd through the FP64 oracle, relative 1e-4 for
+  dL/dc0 and 1e-3 for parameter gradients; against central differences 1e-3.
+"""
+
+import warnings
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import load_golden, parse_bc
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda"
+
+
+def vg_for(shape, spacing=(1.0, 1.0, 1.0)):
+    from evoxels_gb300.voxelfields import VoxelFields
+    from evoxels_gb300.voxelgrid import VoxelGridGB300
+    vf = VoxelFields(shape, domain_size=tuple(n * h for n, h in zip(shape, spacing)))
+    return VoxelGridGB300(vf.grid_info(), device=DEV)
+
+
+def gpu(a):
+    return torch.tensor(np.asarray(a), dtype=torch.float32, device=DEV).unsqueeze(0)
+
+
+def cpu32(a):
+    return torch.tensor(np.asarray(a), dtype=torch.float32).unsqueeze(0)
+
+
+def cpu64(a):
+    return torch.tensor(np.asarray(a), dtype=torch.float64).unsqueeze(0)
+
+
+# ---------------------------------------------------------------------------
+# stencils: bit-exact
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("i", range(5))
+def test_ch_rhs_bitexact_vs_reference_golden(cuda_lib, i):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    g = load_golden(f"ch_rhs_{i}")
+    shape = tuple(int(x) for x in g["shape"])
+    spacing = tuple(float(x) for x in g["spacing"])
+    bc = parse_bc(g["bc"])
+    vg = vg_for(shape, spacing)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        prob = CahnHilliard(vg, eps=3.0, D=1.0, **({"bc": bc} if bc is not None else {}))
+    r = prob.rhs(0.0, gpu(g["u0"])).cpu().numpy()
+    np.testing.assert_array_equal(r, g["rhs"])
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (3, 1, 2), (33, 17, 9), (40, 36, 70), (64, 64, 64)])
+@pytest.mark.parametrize("bc", [None, (("dirichlet", (0.1, 0.9)), "neumann", "periodic"),
+                                ("neumann", "neumann", ("dirichlet", (0.0, 1.0)))])
+def test_ch_rhs_bitexact_vs_oracle(cuda_lib, shape, bc):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    u0 = oracle.seeded_ch_field(shape, 7) + 0.6 * (oracle.seeded_unit_field(shape, 8) - 0.5)
+    vg = vg_for(shape)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        prob = CahnHilliard(vg, eps=2.5, D=1.3, **({"bc": bc} if bc else {}))
+    r = prob.rhs(0.0, gpu(u0)).cpu().numpy()
+    ref = oracle.ch_rhs(cpu32(u0), 2.5, 1.3, bc).numpy()
+    np.testing.assert_array_equal(r, ref)
+
+
+@pytest.mark.parametrize("i", range(5))
+@pytest.mark.parametrize("spp", [1, 2, 4])
+def test_fd_forward_euler_bitexact_vs_reference_golden(cuda_lib, i, spp):
+    from evoxels_gb300.problem_definition import ReactionDiffusion
+    from evoxels_gb300.timesteppers import ForwardEuler
+    g = load_golden(f"fd_fe_{i}")
+    shape = tuple(int(x) for x in g["shape"])
+    bc = parse_bc(g["bc"])
+    vg = vg_for(shape)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        prob = ReactionDiffusion(vg, D=1.0, **({"bc": bc} if bc is not None else {}))
+    st = ForwardEuler(prob, float(g["dt"]), steps_per_pass=spp)
+    u = st.advance(gpu(g["u0"]), int(g["n"])).cpu().numpy()
+    np.testing.assert_array_equal(u, g["u"])
+
+
+@pytest.mark.parametrize("shape", [(2, 3, 5), (17, 9, 33), (48, 40, 64), (70, 33, 35)])
+@pytest.mark.parametrize("bc", [None, (("dirichlet", (0.0, 0.0)), "neumann", "neumann"),
+                                ("neumann", ("dirichlet", (1.0, -2.0)), "periodic"),
+                                ("periodic", "periodic", ("dirichlet", (0.5, 0.25)))])
+def test_fd_steps_bitexact_all_blockings(cuda_lib, shape, bc):
+    from evoxels_gb300.problem_definition import ReactionDiffusion
+    from evoxels_gb300.timesteppers import ForwardEuler
+    u0 = oracle.seeded_unit_field(shape, 5)
+    dt = 1.0 / 60
+    ref = oracle.rd_fe_run(cpu32(u0), 9, dt, 1.0, bc).numpy()
+    vg = vg_for(shape)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        prob = ReactionDiffusion(vg, D=1.0, **({"bc": bc} if bc else {}))
+    for spp in (1, 2, 4):
+        u = ForwardEuler(prob, dt, steps_per_pass=spp).advance(gpu(u0), 9).cpu().numpy()
+        np.testing.assert_array_equal(u, ref, err_msg=f"steps_per_pass={spp}")
+    r = prob.rhs(0.0, gpu(u0)).cpu().numpy()
+    np.testing.assert_array_equal(r, oracle.rd_rhs(cpu32(u0), 1.0, bc).numpy())
+
+
+# ---------------------------------------------------------------------------
+# spectral step: tolerance against the FP64 oracle
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("i", range(4))
+def test_ch_imex_vs_reference_golden(cuda_lib, i):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    g = load_golden(f"ch_imex_{i}")
+    shape = tuple(int(x) for x in g["shape"])
+    prob = CahnHilliard(vg_for(shape), eps=float(g["eps"]), D=float(g["D"]))
+    st = PseudoSpectralIMEX(prob, float(g["dt"]))
+    u = gpu(g["u0"])
+    for _ in range(int(g["n"])):
+        u = st.step(0.0, u)
+    # reference fp32 (pocketfft) vs ours (cuFFT): agreement to float32 FFT rounding
+    assert oracle.rel_to_max(u.cpu().numpy(), g["u"]) < 2e-6
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 16), (5, 7, 9), (24, 20, 18), (100, 100, 100)])
+def test_ch_one_step_error_vs_fp64_oracle(cuda_lib, shape):
+    """Spec bar: <= 1e-5 relative (to max) per step against FP64."""
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    u0 = oracle.seeded_ch_field(shape, 1)
+    st = PseudoSpectralIMEX(CahnHilliard(vg_for(shape)), 0.1)
+    u = st.step(0.0, gpu(u0)).cpu().numpy()
+    ref = oracle.ch_imex_run(cpu64(u0), 1, 0.1).numpy()
+    err = oracle.rel_to_max(u, ref)
+    assert err <= 1e-5, err
+
+
+def test_ch_forward_fused_equals_stepwise(cuda_lib):
+    """The fused multi-step pass performs the same float operations as single steps."""
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    shape = (24, 20, 36)
+    u0 = gpu(oracle.seeded_ch_field(shape, 3))
+    st = PseudoSpectralIMEX(CahnHilliard(vg_for(shape), eps=2.0, D=0.8), 0.1)
+    u = u0
+    for _ in range(7):
+        u = st.step(0.0, u)
+    traj = torch.empty((7,) + shape, dtype=torch.float32, device=DEV)
+    v = st.advance(u0, 7, traj=traj)
+    torch.testing.assert_close(v, u, rtol=0, atol=0)
+    torch.testing.assert_close(traj[-1:], u, rtol=0, atol=0)
+    w = u0
+    for s in range(7):
+        w = st.step(0.0, w)
+        torch.testing.assert_close(traj[s:s + 1], w, rtol=0, atol=0)
+
+
+def test_ch_1000_steps_vs_fp64_oracle(cuda_lib):
+    """Spec bar: <= 1e-4 relative (to max) after 1000 steps (32^3 keeps the FP64 run short)."""
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    shape = (32, 32, 32)
+    u0 = oracle.seeded_ch_field(shape, 1)
+    st = PseudoSpectralIMEX(CahnHilliard(vg_for(shape)), 0.1)
+    u = st.advance(gpu(u0), 1000).cpu().numpy()
+    ref = oracle.ch_imex_run(cpu64(u0), 1000, 0.1).numpy()
+    err = oracle.rel_to_max(u, ref)
+    assert err <= 1e-4, err
+
+
+def test_driver_matches_reference_golden(cuda_lib):
+    import evoxels_gb300 as evo
+    g = load_golden("driver_ch")
+    vf = evo.VoxelFields((16, 16, 16), domain_size=(16, 16, 16))
+    vf.add_field("c", g["u0"].copy())
+    evo.run_cahn_hilliard_solver(vf, "c", "torch", jit=False, time_increment=0.1, frames=2,
+                                 max_iters=int(g["n"]), verbose=False)
+    assert oracle.rel_to_max(vf.fields["c"], g["c"]) < 2e-6
+
+
+def test_nonfinite_flag(cuda_lib):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    shape = (8, 8, 8)
+    u0 = oracle.seeded_ch_field(shape, 2)
+    st = PseudoSpectralIMEX(CahnHilliard(vg_for(shape)), 0.1)
+    flag = torch.zeros(1, dtype=torch.int32, device=DEV)
+    st.advance(gpu(u0), 3, nonfinite=flag)
+    assert int(flag) == 0
+    u0[1, 2, 3] = np.nan
+    st.advance(gpu(u0), 3, nonfinite=flag)
+    assert int(flag) == 1
+
+
+def test_solver_nan_abort_exits(cuda_lib, capsys):
+    import evoxels_gb300 as evo
+    vf = evo.VoxelFields((8, 8, 8), domain_size=(8, 8, 8))
+    u0 = oracle.seeded_ch_field((8, 8, 8), 2)
+    u0[0, 0, 0] = np.nan
+    vf.add_field("c", u0)
+    with pytest.raises(SystemExit) as e:
+        evo.run_cahn_hilliard_solver(vf, "c", "torch", frames=2, max_iters=4, verbose=False)
+    assert e.value.code == 1
+    assert "NaN detected in frame 0" in capsys.readouterr().out
+
+
+def test_errors_match_reference(cuda_lib):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    vg = vg_for((4, 4, 4))
+    with pytest.raises(ValueError, match="support at most one non-periodic axis"):
+        PseudoSpectralIMEX(CahnHilliard(vg, bc=("neumann", "neumann", "periodic")), 0.1)
+    with pytest.raises(NotImplementedError, match="Axis permutation"):
+        PseudoSpectralIMEX(CahnHilliard(vg, bc=("periodic", "neumann", "periodic")), 0.1)
+    with pytest.raises(ValueError):
+        CahnHilliard(vg).rhs(0.0, torch.zeros((1, 4, 4, 5), device=DEV))
+    with pytest.raises(NotImplementedError):
+        CahnHilliard(vg, mu_hom=lambda c: c ** 2)
+    # a pinned double-well mu_hom is accepted (the inversion/batched configuration)
+    CahnHilliard(vg, eps=1.0, mu_hom=lambda c, lib=None: 18 / 3.0 * c * (1 - c) * (1 - 2 * c))
+
+
+# ---------------------------------------------------------------------------
+# adjoint
+# ---------------------------------------------------------------------------
+
+def _plan_with_grads(vg):
+    from evoxels_gb300.timesteppers import get_plan
+    return get_plan(vg, grads=True)
+
+
+def _adjoint(vg, prob, dt, states, lam, grads=False):
+    from evoxels_gb300 import _lib
+    from evoxels_gb300.voxelgrid import cuda_stream
+    plan = _plan_with_grads(vg)
+    n = states.shape[0] - 1
+    out = torch.empty_like(lam)
+    gbuf = torch.zeros(3, dtype=torch.float64, device=DEV) if grads else None
+    _lib.check(_lib.lib().evx_ch_adjoint(plan.handle, states.data_ptr(), n, lam.data_ptr(), out.data_ptr(),
+                                         prob.evx_params(dt), gbuf.data_ptr() if grads else None,
+                                         plan.workspace.data_ptr(), cuda_stream()), "evx_ch_adjoint")
+    return out, gbuf
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (6, 10, 12), (33, 20, 17)])
+def test_ch_adjoint_one_step_vs_autograd(cuda_lib, shape):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    u0 = oracle.seeded_ch_field(shape, 11) + 0.7 * (oracle.seeded_unit_field(shape, 12) - 0.5)
+    lam = oracle.seeded_unit_field(shape, 13) - 0.5
+    vg = vg_for(shape)
+    prob = CahnHilliard(vg, eps=2.0, D=1.2)
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    st = PseudoSpectralIMEX(prob, 0.1)
+    ug = gpu(u0)
+    states = torch.cat([ug, st.step(0.0, ug)], 0).contiguous()
+    out, gr = _adjoint(vg, prob, 0.1, states, gpu(lam), grads=True)
+    ref, dD, de = oracle.ch_imex_vjp(cpu64(u0), cpu64(lam), 0.1, 2.0, 1.2)
+    assert oracle.rel_to_max(out.cpu().numpy(), ref.numpy()) < 1e-4
+    gD, gK, gW = gr.cpu().tolist()
+    # eps enters as kappa = 2*eps and the default bulk w = 18/eps
+    ge = 2 * gK - 18 / 2.0 ** 2 * gW
+    assert abs(gD - dD) <= 1e-3 * abs(dD)
+    assert abs(ge - de) <= 1e-3 * abs(de)
+
+
+def test_ch_adjoint_multi_step_vs_reference_autograd_golden(cuda_lib):
+    """dL/dc0, dL/dD, dL/deps through 5 steps vs torch autograd through the reference."""
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    g = load_golden("ch_grad")
+    shape = g["u0"].shape
+    n, D, eps, dt = int(g["n"]), float(g["D"]), float(g["eps"]), float(g["dt"])
+    vg = vg_for(shape)
+    prob = CahnHilliard(vg, eps=eps, D=D)
+    st = PseudoSpectralIMEX(prob, dt)
+    traj = torch.empty((n + 1,) + shape, dtype=torch.float32, device=DEV)
+    traj[0] = gpu(g["u0"])[0]
+    st.advance(traj[0:1], n, traj=traj[1:])
+    lam = 2 * (traj[n:n + 1] - gpu(g["target"])) / float(np.prod(shape))
+    out, gr = _adjoint(vg, prob, dt, traj, lam.contiguous(), grads=True)
+    assert oracle.rel_to_max(out.cpu().numpy()[0], g["g_c0"]) < 1e-4
+    gD, gK, gW = gr.cpu().tolist()
+    ge = 2 * gK - 18 / eps ** 2 * gW
+    assert abs(gD - float(g["g_D"])) <= 1e-3 * abs(float(g["g_D"]))
+    assert abs(ge - float(g["g_eps"])) <= 1e-3 * abs(float(g["g_eps"]))
+
+
+def test_fd_adjoint_vs_autograd(cuda_lib):
+    from evoxels_gb300 import _lib
+    from evoxels_gb300.problem_definition import ReactionDiffusion
+    from evoxels_gb300.voxelgrid import cuda_stream
+    shape = (12, 9, 14)
+    bc = (("dirichlet", (0.3, 0.0)), "neumann", "periodic")
+    u0 = oracle.seeded_unit_field(shape, 3)
+    lam = oracle.seeded_unit_field(shape, 4) - 0.5
+    x = cpu64(u0).requires_grad_(True)
+    y = oracle.rd_fe_run(x, 6, 1 / 60, 1.0, bc)
+    (ref,) = torch.autograd.grad(y, x, grad_outputs=cpu64(lam))
+    vg = vg_for(shape)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        prob = ReactionDiffusion(vg, D=1.0, bc=bc)
+    lg = gpu(lam)
+    out = torch.empty_like(lg)
+    scratch = torch.empty_like(lg)
+    _lib.check(_lib.lib().evx_fd_adjoint(lg.data_ptr(), out.data_ptr(), scratch.data_ptr(), vg.evx_grid(),
+                                         prob._evx_bc, 1.0, float(np.float32(1 / 60)), 6, cuda_stream()))
+    assert oracle.rel_to_max(out.cpu().numpy(), ref.numpy()) < 1e-5

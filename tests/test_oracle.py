@@ -1,0 +1,108 @@
+"""Pin the CPU oracle against outputs of the reference itself (golden fixtures).
+
+The fixtures were produced by ``tests/golden/make_golden.py`` running the
+reference's own torch code on CPU.  The finite-difference parts must match
+bit for bit (same IEEE operations in the same order); spectral steps match to
+the FFT library's rounding.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import load_golden, parse_bc
+
+
+def t32(a):
+    return torch.tensor(np.asarray(a), dtype=torch.float32).unsqueeze(0) if np.asarray(a).ndim == 3 \
+        else torch.tensor(np.asarray(a), dtype=torch.float32)
+
+
+def test_pad_mixed_matches_reference_test_golden():
+    g = load_golden("pad_mixed")
+    u = torch.tensor(g["u"])
+    got = oracle.pad_bc(u, (("dirichlet", (10.0, 20.0)), "neumann", "periodic"))
+    np.testing.assert_array_equal(got.numpy(), g["padded"])
+    # the literal expectation of the reference's own test (tests/test_solvers.py:119-126)
+    expected = np.pad(np.arange(1, 9, dtype=np.float32).reshape(2, 2, 2), 1, mode="wrap")
+    expected[0, :, :] = 2.0 * 10.0 - expected[1, :, :]
+    expected[-1, :, :] = 2.0 * 20.0 - expected[-2, :, :]
+    expected[:, 0, :] = expected[:, 1, :]
+    expected[:, -1, :] = expected[:, -2, :]
+    np.testing.assert_array_equal(got.numpy()[0], expected)
+
+
+@pytest.mark.parametrize("i", range(5))
+def test_ch_rhs_bitexact(i):
+    g = load_golden(f"ch_rhs_{i}")
+    u = t32(g["u0"])
+    r = oracle.ch_rhs(u, 3.0, 1.0, parse_bc(g["bc"]), tuple(g["spacing"].tolist()))
+    np.testing.assert_array_equal(r.numpy(), g["rhs"])
+
+
+@pytest.mark.parametrize("i", range(5))
+def test_fd_forward_euler_bitexact(i):
+    g = load_golden(f"fd_fe_{i}")
+    u = oracle.rd_fe_run(t32(g["u0"]), int(g["n"]), float(g["dt"]), 1.0, parse_bc(g["bc"]))
+    np.testing.assert_array_equal(u.numpy(), g["u"])
+
+
+@pytest.mark.parametrize("i", range(4))
+def test_ch_imex_matches_reference(i):
+    g = load_golden(f"ch_imex_{i}")
+    u = oracle.ch_imex_run(t32(g["u0"]), int(g["n"]), float(g["dt"]), float(g["eps"]), float(g["D"]))
+    # same torch FFT backend on the same machine class: agreement to fp32 rounding
+    assert oracle.rel_to_max(u.numpy(), g["u"]) < 1e-6
+
+
+def test_ch_imex_fp64_matches_reference():
+    g = load_golden("ch_imex_fp64")
+    u0 = torch.tensor(g["u0"], dtype=torch.float64).unsqueeze(0)
+    u = oracle.ch_imex_run(u0, int(g["n"]), 0.1)
+    assert oracle.rel_to_max(u.numpy(), g["u"]) < 1e-13
+
+
+def test_ch_grad_matches_reference_autograd():
+    g = load_golden("ch_grad")
+    c0 = torch.tensor(g["u0"], dtype=torch.float64).unsqueeze(0)
+    tgt = torch.tensor(g["target"], dtype=torch.float64).unsqueeze(0)
+    loss, g0, gD, ge = oracle.ch_imex_loss_grads(c0, tgt, int(g["n"]), float(g["dt"]),
+                                                 float(g["eps"]), float(g["D"]))
+    assert abs(loss - float(g["loss"])) <= 1e-14 * abs(float(g["loss"]))
+    assert oracle.rel_to_max(g0.numpy(), g["g_c0"]) < 1e-12
+    assert abs(gD - float(g["g_D"])) <= 1e-10 * abs(float(g["g_D"]))
+    assert abs(ge - float(g["g_eps"])) <= 1e-10 * abs(float(g["g_eps"]))
+
+
+def test_driver_run_matches_reference():
+    g = load_golden("driver_ch")
+    u = oracle.ch_imex_run(t32(g["u0"]), int(g["n"]), 0.1)
+    assert oracle.rel_to_max(u.numpy()[0], g["c"]) < 1e-6
+
+
+def test_vjp_is_consistent_with_loss_gradient():
+    """One-step VJP of the oracle equals the autograd gradient of a 1-step loss."""
+    shape = (6, 5, 7)
+    u0 = torch.tensor(oracle.seeded_ch_field(shape, 3), dtype=torch.float64).unsqueeze(0)
+    tgt = torch.tensor(oracle.seeded_ch_field(shape, 4), dtype=torch.float64).unsqueeze(0)
+    loss, g0, gD, ge = oracle.ch_imex_loss_grads(u0, tgt, 1, 0.1, 2.0, 1.2)
+    u1 = oracle.ch_imex_run(u0, 1, 0.1, 2.0, 1.2)
+    lam = 2 * (u1 - tgt) / u1.numel()
+    gu, vD, ve = oracle.ch_imex_vjp(u0, lam, 0.1, 2.0, 1.2)
+    assert oracle.rel_to_max(gu.numpy(), g0.numpy()) < 1e-13
+    assert abs(vD - gD) < 1e-12 * max(1.0, abs(gD))
+    assert abs(ve - ge) < 1e-12 * max(1.0, abs(ge))
+
+
+def test_normalize_bc_errors_match_reference_messages():
+    with pytest.raises(ValueError, match="exactly three axis entries"):
+        oracle.normalize_bc(("periodic", "periodic"))
+    with pytest.raises(ValueError, match="require explicit values"):
+        oracle.normalize_bc(("dirichlet", "periodic", "periodic"))
+    with pytest.raises(ValueError, match="Unsupported BC type"):
+        oracle.normalize_bc(("robin", "periodic", "periodic"))
+    with pytest.raises(ValueError, match="two boundary values"):
+        oracle.normalize_bc((("dirichlet", (1.0,)), "periodic", "periodic"))
+    with pytest.raises(ValueError, match="do not accept boundary values"):
+        oracle.normalize_bc((("neumann", (1.0, 2.0)), "periodic", "periodic"))
