@@ -277,17 +277,17 @@ class FdForward:
         return 4 * self.n, 4 * self.n
 
 
-def make_workload(name, torch, device):
+def make_workload(name, torch, device, inner=None):
     if name == "ch256_fwd_adj":
-        return ChFwdAdj(torch, device, 256, 10, 6)
+        return ChFwdAdj(torch, device, 256, inner or 10, 6)
     if name == "ch128_inversion":
-        return ChFwdAdj(torch, device, 128, 200, 3)
+        return ChFwdAdj(torch, device, 128, inner or 200, 3)
     if name == "ch100_fwd":
-        return ChForward(torch, device, 100, 100, 1)
+        return ChForward(torch, device, 100, inner or 100, 1)
     if name == "ch512_fwd":
-        return ChForward(torch, device, 512, 20, 5)
+        return ChForward(torch, device, 512, inner or 20, 5)
     if name == "fd512":
-        return FdForward(torch, device, 512, 100, 2)
+        return FdForward(torch, device, 512, inner or 100, 2)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -354,6 +354,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ch256_fwd_adj")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--inner-steps", type=int, default=None,
+                    help="override the IMEX/FE steps per bench step (profiling runs)")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
 
@@ -377,7 +379,7 @@ def main():
 
     from evoxels_gb300 import _lib
     L = _lib.lib()
-    wl = make_workload(args.workload, torch, device)
+    wl = make_workload(args.workload, torch, device, args.inner_steps)
 
     for _ in range(warmup):
         wl.step()

@@ -24,7 +24,7 @@
 // gradients are deterministic.
 #include <algorithm>
 
-#include "evx_ch_plan.cuh"
+#include "evx_ch_fast.cuh"
 
 namespace evx {
 
@@ -239,6 +239,9 @@ int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps, const flo
     if (rc) return rc;
     if (!lam_in || !lam_out || (!states && nsteps > 0)) return fail(EVX_ERR_BAD_ARG, "NULL field pointer");
     if (lam_in == lam_out) return fail(EVX_ERR_BAD_ARG, "lam_in and lam_out must not alias");
+    // lam buffers are cuFFT R2C inputs, which must be aligned
+    if ((reinterpret_cast<uintptr_t>(lam_in) | reinterpret_cast<uintptr_t>(lam_out)) & 15)
+        return fail(EVX_ERR_BAD_ARG, "lam_in and lam_out must be 16-byte aligned");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
     cudaStream_t st = as_stream(stream);
     const size_t N = plan->n;
@@ -271,7 +274,17 @@ int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps, const flo
         if ((rc = check_launch("ch_kspace_adj_kernel"))) return rc;
         if ((rc = ch_c2r(plan, spec, gbuf, want, st))) return rc;
         const float* us = states + (size_t)s * N;
-        if (want) {
+        if (fast_ok(g, {us, gbuf, lam, hbuf, us + N, dst})) {
+            int nb = 0;
+            if ((rc = ch_pullback_fast_launch(want, us, gbuf, lam, hbuf, us + N, dst, part, plan->n_part, g, G, P, st,
+                                              &nb)))
+                return rc;
+            if (want) {
+                EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_kernel<<<1, 256, 0, st>>>(part, nb, grads, kA, DA));
+                count_launch();
+                if ((rc = check_launch("ch_grad_reduce_kernel"))) return rc;
+            }
+        } else if (want) {
             EVX_TIMED("ch_pullback_grads", st,
                       ch_pullback_kernel<true><<<sg, dim3(32, 8), 0, st>>>(us, gbuf, lam, hbuf, us + N, dst, part, G, P, lx));
             count_launch();

@@ -19,7 +19,7 @@
 #include <cmath>
 #include <vector>
 
-#include "evx_ch_plan.cuh"
+#include "evx_ch_fast.cuh"
 
 namespace evx {
 
@@ -280,8 +280,14 @@ using namespace evx;
 
 namespace {
 
+bool all_periodic(const Geo& G) {
+    return G.kind[0] == EVX_BC_PERIODIC && G.kind[1] == EVX_BC_PERIODIC && G.kind[2] == EVX_BC_PERIODIC;
+}
+
 int ch_rhs_launch(bool fused, const float* u, const float* upd, float* u_new, float* r,
                   const evx_grid* g, const Geo& G, const ChP& P, cudaStream_t st) {
+    if (all_periodic(G) && fast_ok(g, {u, upd, u_new, r}))
+        return ch_rhs_fast_launch(fused, u, upd, u_new, r, g, G, P, st);
     dim3 grid; int lx;
     ch_stencil_grid(g, &grid, &lx);
     if (fused) EVX_TIMED("ch_rhs_fused", st, ch_rhs_kernel<true><<<grid, dim3(32, 8), 0, st>>>(u, upd, u_new, r, G, P, lx));
@@ -364,7 +370,7 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
     // workspace layout
     dim3 sg; int lx;
     ch_stencil_grid(g, &sg, &lx);
-    p->n_part = (int)(sg.x * sg.y * sg.z);
+    p->n_part = std::max((int)(sg.x * sg.y * sg.z), ch_pullback_fast_blocks(g));
     size_t off = 0;
     p->off_fft = off;  off += align256(p->ws_fft);
     p->off_r = off;    off += align256(2 * p->n * sizeof(float));

@@ -143,7 +143,8 @@ int evx_ch_forward(evx_ch_plan* plan, const float* u_in, float* u_out, int nstep
  * of the forward trajectory; lam_in = dL/du_n; lam_out = dL/du_0.
  * grads (optional device double[3]) accumulates dL/dD, dL/dkappa, dL/dw
  * (kappa, w as in evx_ch_params; needs a plan made with flags bit 0).
- * lam_in is read only. */
+ * lam_in is read only; lam_in and lam_out must be 16-byte aligned (they feed
+ * cuFFT R2C). */
 int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps,
                    const float* lam_in, float* lam_out, const evx_ch_params* p,
                    double* grads, void* workspace, void* stream);

@@ -316,3 +316,74 @@ def test_fd_adjoint_vs_autograd(cuda_lib):
     _lib.check(_lib.lib().evx_fd_adjoint(lg.data_ptr(), out.data_ptr(), scratch.data_ptr(), vg.evx_grid(),
                                          prob._evx_bc, 1.0, float(np.float32(1 / 60)), 6, cuda_stream()))
     assert oracle.rel_to_max(out.cpu().numpy(), ref.numpy()) < 1e-5
+
+
+# ---------------------------------------------------------------------------
+# fast periodic kernels vs the generic kernels (a misaligned view forces the
+# generic path: the fast path needs 16-byte aligned fields and nz % 4 == 0)
+# ---------------------------------------------------------------------------
+
+def _misaligned_copy(t):
+    flat = torch.empty(t.numel() + 1, dtype=t.dtype, device=t.device)
+    v = flat[1:].view(t.shape)
+    v.copy_(t)
+    assert v.data_ptr() % 16 != 0
+    return v
+
+
+@pytest.mark.parametrize("shape", [(10, 20, 100), (7, 33, 68), (12, 17, 4), (3, 5, 8), (40, 18, 136),
+                                   (9, 16, 64), (1, 1, 4)])
+def test_ch_rhs_fast_equals_generic_and_oracle(cuda_lib, shape):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    u0 = oracle.seeded_ch_field(shape, 21) + 0.6 * (oracle.seeded_unit_field(shape, 22) - 0.5)
+    prob = CahnHilliard(vg_for(shape), eps=2.0, D=0.9)
+    ug = gpu(u0)
+    fast = prob.rhs(0.0, ug)
+    slow = prob.rhs(0.0, _misaligned_copy(ug))
+    torch.testing.assert_close(fast, slow, rtol=0, atol=0)
+    np.testing.assert_array_equal(fast.cpu().numpy(), oracle.ch_rhs(cpu32(u0), 2.0, 0.9).numpy())
+
+
+@pytest.mark.parametrize("shape", [(10, 20, 100), (12, 17, 4), (36, 40, 72)])
+def test_ch_forward_fast_matches_fp64(cuda_lib, shape):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    u0 = oracle.seeded_ch_field(shape, 4)
+    st = PseudoSpectralIMEX(CahnHilliard(vg_for(shape)), 0.1)
+    traj = torch.empty((6,) + shape, dtype=torch.float32, device=DEV)
+    st.advance(gpu(u0), 6, traj=traj)
+    keep = []
+    oracle.ch_imex_run(cpu64(u0), 6, 0.1, keep=keep)
+    for s in range(6):
+        assert oracle.rel_to_max(traj[s].cpu().numpy(), keep[s + 1].numpy()[0]) <= 1e-5 * (s + 1)
+
+
+@pytest.mark.parametrize("shape", [(10, 20, 100), (12, 17, 4), (16, 16, 16), (9, 33, 68)])
+@pytest.mark.parametrize("grads", [False, True])
+def test_ch_adjoint_fast_equals_generic(cuda_lib, shape, grads):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    u0 = oracle.seeded_ch_field(shape, 31) + 0.5 * (oracle.seeded_unit_field(shape, 32) - 0.5)
+    lam = oracle.seeded_unit_field(shape, 33) - 0.5
+    vg = vg_for(shape)
+    prob = CahnHilliard(vg, eps=1.5, D=1.1)
+    st = PseudoSpectralIMEX(prob, 0.1)
+    n = 3
+    traj = torch.empty((n + 1,) + shape, dtype=torch.float32, device=DEV)
+    traj[0] = gpu(u0)[0]
+    st.advance(traj[0:1], n, traj=traj[1:])
+    a, ga = _adjoint(vg, prob, 0.1, traj, gpu(lam), grads=grads)
+    b, gb = _adjoint(vg, prob, 0.1, _misaligned_copy(traj), gpu(lam), grads=grads)
+    assert oracle.rel_to_max(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
+    if grads:
+        for x, y in zip(ga.cpu().tolist(), gb.cpu().tolist()):
+            assert abs(x - y) <= 1e-5 * max(abs(y), 1e-12)
+    # and against torch autograd through the FP64 oracle
+    v = lam
+    ref = cpu64(lam)
+    keep = []
+    oracle.ch_imex_run(cpu64(u0), n, 0.1, 1.5, 1.1, keep=keep)
+    for s in range(n - 1, -1, -1):
+        ref, _, _ = oracle.ch_imex_vjp(keep[s], ref, 0.1, 1.5, 1.1)
+    del v
+    assert oracle.rel_to_max(a.cpu().numpy(), ref.numpy()) < 1e-4
