@@ -277,7 +277,7 @@ class FdForward:
         return 4 * self.n, 4 * self.n
 
 
-def make_workload(name, torch, device, inner=None):
+def make_workload(name, torch, device, inner=None, spp=4):
     if name == "ch256_fwd_adj":
         return ChFwdAdj(torch, device, 256, inner or 10, 6)
     if name == "ch128_inversion":
@@ -287,7 +287,7 @@ def make_workload(name, torch, device, inner=None):
     if name == "ch512_fwd":
         return ChForward(torch, device, 512, inner or 20, 5)
     if name == "fd512":
-        return FdForward(torch, device, 512, inner or 100, 2)
+        return FdForward(torch, device, 512, inner or 100, 2, spp=spp)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -356,6 +356,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--inner-steps", type=int, default=None,
                     help="override the IMEX/FE steps per bench step (profiling runs)")
+    ap.add_argument("--fd-steps-per-pass", type=int, default=4, choices=[1, 2, 4],
+                    help="temporal blocking of the finite-difference workload")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
 
@@ -379,7 +381,7 @@ def main():
 
     from evoxels_gb300 import _lib
     L = _lib.lib()
-    wl = make_workload(args.workload, torch, device, args.inner_steps)
+    wl = make_workload(args.workload, torch, device, args.inner_steps, args.fd_steps_per_pass)
 
     for _ in range(warmup):
         wl.step()

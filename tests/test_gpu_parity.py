@@ -92,7 +92,8 @@ def test_fd_forward_euler_bitexact_vs_reference_golden(cuda_lib, i, spp):
     np.testing.assert_array_equal(u, g["u"])
 
 
-@pytest.mark.parametrize("shape", [(2, 3, 5), (17, 9, 33), (48, 40, 64), (70, 33, 35)])
+@pytest.mark.parametrize("shape", [(2, 3, 5), (17, 9, 33), (48, 40, 64), (70, 33, 35), (5, 3, 4), (33, 17, 68),
+                                   (20, 40, 132), (9, 1, 8)])
 @pytest.mark.parametrize("bc", [None, (("dirichlet", (0.0, 0.0)), "neumann", "neumann"),
                                 ("neumann", ("dirichlet", (1.0, -2.0)), "periodic"),
                                 ("periodic", "periodic", ("dirichlet", (0.5, 0.25)))])
