@@ -51,6 +51,8 @@ _SIGS = {
     "evx_rd_rhs": (C.c_int, [_P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.c_float, _P]),
     "evx_fd_forward": (C.c_int, [_P, _P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.c_float, C.c_float,
                                  C.c_int, C.c_int, _P]),
+    "evx_fd_forward_noalloc": (C.c_int, [_P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.c_float, C.c_float,
+                                         C.c_int, C.c_int, _P]),
     "evx_fd_adjoint": (C.c_int, [_P, _P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.c_float, C.c_float,
                                  C.c_int, _P]),
     "evx_fe_update": (C.c_int, [_P, _P, C.c_float, _P, C.c_size_t, _P]),

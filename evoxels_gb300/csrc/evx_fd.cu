@@ -483,3 +483,64 @@ int evx_fd_adjoint(const float* lam_in, float* lam_out, float* scratch, const ev
 }
 
 }  // extern "C"
+
+// ---- allocation-free forward Euler --------------------------------------------
+// evx_fd_forward needs one caller-allocated scratch field for its ping-pong
+// passes.  Some callers cannot provide it: hosts whose device memory is handed
+// out only by their own pre-reserved pool (an extra cudaMalloc would fail or
+// fragment it), and bindings that pass buffers from a foreign allocator and
+// must not allocate at all.  evx_fd_forward_noalloc keeps that scratch in the
+// file-scope device array below instead.  It holds EVX_FD_NOALLOC_MAX_VOXELS
+// floats (16 MiB) on every GPU that loads this library, until the process
+// exits.  All calls share the array: calls that overlap on the GPU (on
+// different streams, or from different threads) race on it.  The array keeps
+// the last call's contents; nothing in it needs to start at zero, because
+// every element a call reads was written earlier in the same call.
+#include <mutex>
+
+static __device__ __align__(256) float g_fd_noalloc_scratch[EVX_FD_NOALLOC_MAX_VOXELS];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+float* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the scratch array on the current device.  The host-side
+// symbol is only a stand-in, so the address is looked up once per device,
+// with that device current, and cached.
+int noalloc_scratch(float** out) {
+    int dev = 0;
+    int rc = evx::check_cuda(cudaGetDevice(&dev), "evx_fd_forward_noalloc: cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return evx::fail(EVX_ERR_UNSUPPORTED, "evx_fd_forward_noalloc: device ordinal %d not supported", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        rc = evx::check_cuda(cudaGetSymbolAddress(&p, g_fd_noalloc_scratch),
+                             "evx_fd_forward_noalloc: cudaGetSymbolAddress");
+        if (rc) return rc;
+        g_noalloc_ptr[dev] = static_cast<float*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return EVX_OK;
+}
+
+}  // namespace
+
+extern "C" int evx_fd_forward_noalloc(const float* u_in, float* u_out, const evx_grid* g, const evx_bc* bc,
+                                      float D, float dt, int nsteps, int steps_per_pass, void* stream) {
+    int rc = fd_common_checks(u_in, u_out, g, bc);
+    if (rc) return rc;
+    const size_t n = field_elems(g);
+    if (n > (size_t)EVX_FD_NOALLOC_MAX_VOXELS)
+        return fail(EVX_ERR_TOO_LARGE,
+                    "evx_fd_forward_noalloc: grid of %zu voxels exceeds the %u-voxel built-in scratch; "
+                    "use evx_fd_forward with a caller-provided scratch field",
+                    n, (unsigned)EVX_FD_NOALLOC_MAX_VOXELS);
+    float* scratch = nullptr;
+    if ((rc = noalloc_scratch(&scratch))) return rc;
+    Geo G = make_geo(g, bc);
+    return fd_run(u_in, u_out, scratch, g, G, D, dt, nsteps, steps_per_pass, as_stream(stream));
+}

@@ -97,6 +97,20 @@ int evx_fd_forward(const float* u_in, float* u_out, float* scratch,
                    const evx_grid* g, const evx_bc* bc, float D, float dt,
                    int nsteps, int steps_per_pass, void* stream);
 
+/* Allocation-free variant of evx_fd_forward (no counterpart in the reference):
+ * for callers that cannot let a library allocate device memory, such as hosts
+ * whose device memory comes only from their own pre-reserved pool, or
+ * bindings passing buffers from a foreign allocator.  The ping-pong scratch
+ * lives in a static device array of EVX_FD_NOALLOC_MAX_VOXELS floats (16 MiB),
+ * held on every GPU that loads the library until the process exits; larger
+ * grids are rejected with EVX_ERR_TOO_LARGE.  The first call on a device looks
+ * up the array's device address, so make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.
+ * Calls no cudaMalloc, cudaFree or allocating library routine. */
+#define EVX_FD_NOALLOC_MAX_VOXELS (1u << 22)
+int evx_fd_forward_noalloc(const float* u_in, float* u_out, const evx_grid* g, const evx_bc* bc,
+                           float D, float dt, int nsteps, int steps_per_pass, void* stream);
+
 /* Adjoint of evx_fd_forward with respect to u_in: lam_out = (dU_n/dU_0)^T lam_in.
  * The transposed stencil uses homogeneous ghosts (a Dirichlet ghost 2v-u0
  * contributes -1*u0, a Neumann ghost +1*u0).  scratch as above. */
