@@ -58,6 +58,15 @@ def algorithmic_bytes(slot, n, nspec):
         "cufft_r2c": 4 * n + 8 * nspec,
         "cufft_c2r": 8 * nspec + 4 * n,
         "cufft_c2r_x2": 16 * nspec + 8 * n,
+        "batch_rhs_fused": 16 * n,
+        "batch_rhs": 8 * n,
+        "batch_kspace_fwd": 16 * nspec,
+        "batch_kspace_adj": 24 * nspec,
+        "batch_pullback_grads": 24 * n,
+        "batch_pullback": 16 * n,
+        "batch_axpy": 12 * n,
+        "batch_cufft_r2c": 4 * n + 8 * nspec,
+        "batch_cufft_c2r": 8 * nspec + 4 * n,
         "fd_step": 8 * n,
         "fd_tblock2": 8 * n,
         "fd_tblock4": 8 * n,
@@ -277,7 +286,101 @@ class FdForward:
         return 4 * self.n, 4 * self.n
 
 
+class Batched:
+    """64 uneven periodic CH instances (sides from {32,48,64,96,128}, seed 4), per-instance
+    mobility M ~ U[0.5,2] and kappa ~ U[0.5,3] (eps = kappa/2, bulk pinned to 18/3),
+    dt = 0.1; forward, or forward + adjoint with parameter gradients."""
+
+    def __init__(self, torch, device, steps_per=50, adjoint=False, n_inst=64, autotune=True):
+        from evoxels_gb300.batched import BatchedCahnHilliard, BatchTuning
+        self.torch = torch
+        rng = np.random.default_rng(4)
+        sides = rng.choice([32, 48, 64, 96, 128], n_inst)
+        M = rng.uniform(0.5, 2.0, n_inst)
+        kappa = rng.uniform(0.5, 3.0, n_inst)
+        self.shapes = [(int(a),) * 3 for a in sides]
+        self.M, self.eps = M, kappa / 2
+        self.pin = lambda c, lib=None: 18 / 3.0 * c * (1 - c) * (1 - 2 * c)
+        tuning = BatchTuning()
+        tuned = None
+        if autotune:
+            from evoxels_gb300 import autotune as at
+            tuning = at.tune_batched(self.shapes, M, self.eps, 0.1, mu_hom=self.pin, steps=10)
+            tuned = dict(tuning.__dict__)
+        self.b = BatchedCahnHilliard(self.shapes, M, self.eps, 0.1, mu_hom=self.pin, tuning=tuning)
+        self.fields = [0.5 + 0.1 * np.random.default_rng([4, i]).random(s) for i, s in enumerate(self.shapes)]
+        self.T = steps_per
+        self.adj = adjoint
+        self.n = self.b.voxels
+        self.nspec = sum(s[0] * s[1] * (s[2] // 2 + 1) for s in self.shapes)
+        self.fft_plans = len(set(self.shapes)) if tuning.fft_group_max == 0 else \
+            sum(-(-sum(1 for t in self.shapes if t == s) // tuning.fft_group_max) for s in set(self.shapes))
+        self.u0 = self.b.pack(self.fields)
+        self.u0_host = self.u0.cpu().pin_memory()
+        self.out_host = torch.empty_like(self.u0_host).pin_memory()
+        if adjoint:
+            self.states = torch.empty((self.T + 1) * self.b.total, dtype=torch.float32, device=device)
+            self.lam = torch.empty(self.b.total, dtype=torch.float32, device=device).uniform_(-1e-3, 1e-3)
+            self.grads = torch.zeros((self.b.n, 3), dtype=torch.float64, device=device)
+        self.units_per_step = self.n * self.T
+        self.config = {"workload": "batched64_fwd_adj" if adjoint else "batched64_fwd", "instances": n_inst,
+                       "sides": sorted(set(int(a) for a in sides)), "total_voxels": self.n,
+                       "steps_per_bench_step": self.T, "dt": 0.1, "M_range": [0.5, 2.0], "kappa_range": [0.5, 3.0],
+                       "bulk": "pinned 18/3", "seed": 4, "tuning": tuned or "defaults",
+                       "work_items": self.b.work_items,
+                       "l2": "inputs larger than L2 (%.2f GB per packed field)" % (4 * self.b.total / 1e9)}
+
+    def step(self):
+        if not self.adj:
+            return self.b.forward(self.u0, self.T)
+        t = self.b.total
+        self.states[:t].copy_(self.u0)
+        self.b.forward(self.states[:t], self.T, traj=self.states[t:])
+        self.grads.zero_()
+        return self.b.adjoint(self.states, self.T, self.lam, self.grads)
+
+    def step_e2e(self):
+        self.u0.copy_(self.u0_host, non_blocking=True)
+        out = self.step()
+        self.out_host.copy_(out, non_blocking=True)
+        self.torch.cuda.current_stream().synchronize()
+
+    def e2e_bytes(self):
+        return 4 * self.b.total, 4 * self.b.total
+
+    def plain(self, steps):
+        """Same work through the single-grid path, one instance at a time (ms per bench step)."""
+        from evoxels_gb300.problem_definition import CahnHilliard
+        from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+        from evoxels_gb300.voxelfields import VoxelFields
+        from evoxels_gb300.voxelgrid import VoxelGridGB300
+        torch = self.torch
+        runs = []
+        for i, s in enumerate(self.shapes):
+            vg = VoxelGridGB300(VoxelFields(s, domain_size=s).grid_info(), device=self.u0.device)
+            st = PseudoSpectralIMEX(CahnHilliard(vg, eps=float(self.eps[i]), D=float(self.M[i]), mu_hom=self.pin), 0.1)
+            u = torch.tensor(self.fields[i], dtype=torch.float32, device=self.u0.device).unsqueeze(0)
+            runs.append((st, u))
+
+        def one():
+            for st, u in runs:
+                st.advance(u, self.T)
+        one()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            one()
+        b.record()
+        b.synchronize()
+        return a.elapsed_time(b) / steps
+
+
 def make_workload(name, torch, device, inner=None, spp=4):
+    if name == "batched64_fwd":
+        return Batched(torch, device, inner or 50, adjoint=False)
+    if name == "batched64_fwd_adj":
+        return Batched(torch, device, inner or 20, adjoint=True)
     if name == "ch256_fwd_adj":
         return ChFwdAdj(torch, device, 256, inner or 10, 6)
     if name == "ch128_inversion":
@@ -300,7 +403,23 @@ def cpu_sample(workload_name, torch, seconds_cap=30.0):
     import oracle
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    if workload_name in ("ch256_fwd_adj", "ch128_inversion"):
+    if workload_name.startswith("batched"):
+        rng = np.random.default_rng(4)
+        sides = rng.choice([32, 48, 64, 96, 128], 64)
+        kappa = (rng.uniform(0.5, 2.0, 64), rng.uniform(0.5, 3.0, 64))[1]
+        adj = workload_name.endswith("adj")
+        pin = lambda c, lib=None: 18 / 3.0 * c * (1 - c) * (1 - 2 * c)  # noqa: E731
+        fields = [torch.tensor(0.5 + 0.1 * np.random.default_rng([4, i]).random((int(a),) * 3),
+                               dtype=torch.float32).unsqueeze(0) for i, a in enumerate(sides)]
+
+        def one():
+            for i, u in enumerate(fields):
+                oracle.ch_imex_run(u, 1, 0.1, float(kappa[i] / 2), 1.0, mu_hom=pin)
+                if adj:
+                    oracle.ch_imex_vjp(u, u, 0.1, float(kappa[i] / 2), 1.0, mu_hom=pin)
+        units = sum(int(a) ** 3 for a in sides)
+        sample = "all 64 instances, 1 IMEX step each%s, fp32" % (" + 1 adjoint step (torch autograd)" if adj else "")
+    elif workload_name in ("ch256_fwd_adj", "ch128_inversion"):
         n = 256 if workload_name == "ch256_fwd_adj" else 128
         shape = (n, n, n)
         u0 = torch.tensor(oracle.seeded_ch_field(shape, 6), dtype=torch.float32).unsqueeze(0)
@@ -447,8 +566,11 @@ def main():
     peak, peak_kind = read_peaks()
     breakdown = {}
     total_ms = sum(v[0] for v in prof.values()) or 1.0
+    per_group = getattr(wl, "fft_plans", 1)   # batched FFT slots launch once per shape group
     for slot, (tms, cnt) in sorted(prof.items(), key=lambda kv: -kv[1][0]):
         b = algorithmic_bytes(slot, wl.n, wl.nspec)
+        if b and slot.startswith("batch_cufft"):
+            b = b / per_group
         avg = tms / max(cnt, 1)
         breakdown[slot] = {"launches": cnt // nprof, "avg_us": round(avg * 1e3, 2),
                            "share": round(tms / total_ms, 4),
@@ -466,7 +588,9 @@ def main():
                     "algorithmic_bytes_per_launch": b,
                     "traffic": (tr * wl.n) if tr is not None else None}
     step_bytes = None
-    if args.workload in ("ch256_fwd_adj", "ch128_inversion"):
+    if args.workload.startswith("batched"):
+        step_bytes = (64 if wl.adj else 32) * wl.units_per_step
+    elif args.workload in ("ch256_fwd_adj", "ch128_inversion"):
         step_bytes = 64 * wl.units_per_step    # 32 B forward + 32 B adjoint per voxel-step
     elif args.workload.startswith("ch"):
         step_bytes = 32 * wl.units_per_step
@@ -478,6 +602,12 @@ def main():
         step_roofline = {"achieved": round(gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
                          "bytes_per_voxel_step": step_bytes // wl.units_per_step}
 
+    vs_plain = None
+    if isinstance(wl, Batched) and not wl.adj:
+        plain_ms = wl.plain(max(2, min(args.steps, 5)))
+        vs_plain = {"plain_ms_per_step": round(plain_ms, 3), "plain_value": round(wl.units_per_step / (plain_ms / 1e3), 1),
+                    "speedup": round(plain_ms / (ms / args.steps), 3),
+                    "plain_path": "single-grid PseudoSpectralIMEX.advance per instance, same GPU"}
     out = {
         "metric": METRIC if args.workload == "ch256_fwd_adj" else f"voxel-steps/s {args.workload}",
         "value": round(value, 1),
@@ -497,6 +627,7 @@ def main():
         "kernel_breakdown": breakdown,
         "e2e": e2e,
         "gpu_launches": int(launches),
+        "vs_plain": vs_plain,
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -515,7 +646,25 @@ def run_reference(args, torch, warmup):
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
     wl = args.workload
-    if wl in ("ch256_fwd_adj", "ch128_inversion"):
+    if wl.startswith("batched"):
+        rng = np.random.default_rng(4)
+        sides = rng.choice([32, 48, 64, 96, 128], 64)
+        units = sum(int(a) ** 3 for a in sides)
+        kappa = (rng.uniform(0.5, 2.0, 64), rng.uniform(0.5, 3.0, 64))[1]
+        pin = lambda c, lib=None: 18 / 3.0 * c * (1 - c) * (1 - 2 * c)  # noqa: E731
+        fields = [torch.tensor(0.5 + 0.1 * np.random.default_rng([4, i]).random((int(a),) * 3),
+                               dtype=torch.float32).unsqueeze(0) for i, a in enumerate(sides)]
+        adj = wl.endswith("adj")
+
+        def one():
+            for i, u in enumerate(fields):
+                oracle.ch_imex_run(u, 1, 0.1, float(kappa[i] / 2), 1.0, mu_hom=pin)
+                if adj:
+                    oracle.ch_imex_vjp(u, u, 0.1, float(kappa[i] / 2), 1.0, mu_hom=pin)
+        shape = (int(round(units ** (1 / 3))),) * 3
+        sample = "all 64 instances, 1 IMEX step each%s per bench step, fp32" % (" + 1 adjoint step" if adj else "")
+        n = round(units ** (1 / 3))
+    elif wl in ("ch256_fwd_adj", "ch128_inversion"):
         n = 256 if wl == "ch256_fwd_adj" else 128
         shape = (n, n, n)
         u0 = torch.tensor(oracle.seeded_ch_field(shape, 6), dtype=torch.float32).unsqueeze(0)
@@ -548,7 +697,8 @@ def run_reference(args, torch, warmup):
     for _ in range(args.steps):
         one()
     el = time.perf_counter() - t0
-    value = n ** 3 * args.steps / el
+    units_ref = units if wl.startswith("batched") else n ** 3
+    value = units_ref * args.steps / el
     out = {
         "metric": METRIC if wl == "ch256_fwd_adj" else f"voxel-steps/s {wl}",
         "impl": "reference",
@@ -563,7 +713,7 @@ def run_reference(args, torch, warmup):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded U[0,1) fields, no dataset)",
-        "config": {"workload": wl, "grid": list(shape)},
+        "config": {"workload": wl, "grid": "64 uneven instances" if wl.startswith("batched") else list(shape)},
         "cpu_baseline": {"value": round(value, 1), "unit": "voxel-steps/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 1), "unit": "voxel-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

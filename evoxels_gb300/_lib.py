@@ -42,6 +42,17 @@ class EvxChParams(C.Structure):
                 ("sym_coef", C.c_float), ("dt", C.c_float)]
 
 
+class EvxBatchInstance(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("reserved", C.c_int32),
+                ("h", C.c_double * 3), ("inv_h", C.c_float * 3), ("inv_h2", C.c_float * 3),
+                ("inv_h2_sum", C.c_float), ("params", EvxChParams)]
+
+
+class EvxBatchTuning(C.Structure):
+    _fields_ = [("tile_variant", C.c_int32), ("x_chunk", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("fft_group_max", C.c_int32), ("graph_steps", C.c_int32)]
+
+
 # name -> (restype, argtypes); mirrors include/evx.h
 _P = C.c_void_p
 _SIGS = {
@@ -63,6 +74,16 @@ _SIGS = {
     "evx_ch_step": (C.c_int, [_P, _P, _P, C.POINTER(EvxChParams), _P, _P]),
     "evx_ch_forward": (C.c_int, [_P, _P, _P, C.c_int, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
+    "evx_set_tile_variant": (C.c_int, [C.c_int]),
+    "evx_batch_create": (C.c_int, [C.POINTER(_P), C.POINTER(EvxBatchInstance), C.c_int, C.POINTER(EvxBatchTuning),
+                                   C.c_int]),
+    "evx_batch_destroy": (C.c_int, [_P]),
+    "evx_batch_field_floats": (C.c_size_t, [_P]),
+    "evx_batch_workspace_bytes": (C.c_size_t, [_P]),
+    "evx_batch_work_items": (C.c_int, [_P]),
+    "evx_batch_offsets": (C.c_int, [_P, _P]),
+    "evx_batch_forward": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, _P, _P]),
+    "evx_batch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, _P, _P, _P]),
     "evx_mse_scratch_bytes": (C.c_size_t, [C.c_size_t]),
     "evx_mse_grad": (C.c_int, [_P, _P, C.c_size_t, _P, _P, _P, C.c_size_t, _P]),
     "evx_prof_enable": (None, [C.c_int]),

@@ -1,14 +1,15 @@
 // Tile geometry and helpers shared by the periodic fast-path stencil kernels
-// (Cahn-Hilliard rhs and its adjoint pullback).
+// (Cahn-Hilliard rhs and its adjoint pullback), single-grid and batched.
 //
-// A block of 32 x 8 threads owns a TY x TZ = 16 x 64 (y, z) tile and streams
-// along x.  Every thread owns a 2 x 2 (y, z) patch of outputs, so faces inside
-// a patch are evaluated once and the x face of a patch is carried in
-// registers from one plane to the next.  Field planes are staged in shared
-// memory with a halo of 2 rows in y and 4 columns in z (4 keeps every row
-// float4-aligned for nz % 4 == 0); chemical-potential planes cover the tile
-// grown by one cell.  Wrap-around (periodic) offsets are computed once per
-// block, so the per-plane loads are plain float4 loads.
+// A block of 256 threads owns a TY x TZ (y, z) tile and streams along x.
+// Every thread owns a 2 x 2 (y, z) patch of outputs, so faces inside a patch
+// are evaluated once and the x face of a patch is carried in registers from
+// one plane to the next.  Field planes are staged in shared memory with a halo
+// of 2 rows in y and 4 columns in z (4 keeps every row float4-aligned for
+// nz % 4 == 0); chemical-potential planes cover the tile grown by one cell.
+// Wrap-around (periodic) offsets are computed once per tile, so the per-plane
+// loads are plain float4 loads.  Two tile shapes are built: 16 x 64 (wide in
+// z) and 32 x 32 (for grids whose nz is a multiple of 32 but not of 64).
 #pragma once
 
 #include <initializer_list>
@@ -18,16 +19,29 @@
 namespace evx {
 namespace fast {
 
-constexpr int TZ = 64, TY = 16;
-constexpr int W = TZ + 8;          // shared row width: z in [k0-4, k0+68)
-constexpr int CR = TY + 4;         // field rows: y in [j0-2, j0+18)
-constexpr int MR = TY + 2;         // potential rows: y in [j0-1, j0+17); row m <-> field row m+1
-constexpr int NQ = W / 4;          // float4 per shared row
-constexpr int NLOAD = CR * NQ;     // float4 loads per field plane (360)
-constexpr int MPZ = (TZ + 4) / 2;  // 2x2 potential patches per row pair: cols 2..69
-constexpr int MPY = MR / 2;
-constexpr int NMU = MPZ * MPY;     // 306 potential patches per plane
 constexpr int THREADS = 256;
+
+template <int TZ_, int TY_>
+struct Tile {
+    static constexpr int TZ = TZ_, TY = TY_;
+    static constexpr int BX = TZ / 2, BY = TY / 2;  // thread grid over 2x2 patches
+    static constexpr int W = TZ + 8;          // shared row width: z in [k0-4, k0+TZ+4)
+    static constexpr int CR = TY + 4;         // field rows: y in [j0-2, j0+TY+2)
+    static constexpr int MR = TY + 2;         // potential rows: y in [j0-1, j0+TY+1); row m <-> field row m+1
+    static constexpr int NQ = W / 4;          // float4 per shared row
+    static constexpr int NLOAD = CR * NQ;     // float4 loads per field plane
+    static constexpr int MPZ = (TZ + 4) / 2;  // 2x2 potential patches per row pair: cols 2..TZ+5
+    static constexpr int MPY = MR / 2;
+    static constexpr int NMU = MPZ * MPY;     // potential patches per plane
+    static constexpr int FIELD = CR * W;      // floats per shared field plane
+    static constexpr int POT = MR * W;        // floats per shared potential plane
+    static_assert(BX * BY == THREADS, "tile must map to 256 threads");
+    static_assert(NLOAD <= 2 * THREADS && NMU <= 2 * THREADS, "at most two loads / patches per thread");
+};
+using TileWide = Tile<64, 16>;
+using TileSquare = Tile<32, 32>;
+constexpr int MAX_FIELD = TileWide::FIELD > TileSquare::FIELD ? TileWide::FIELD : TileSquare::FIELD;
+constexpr int MAX_POT = TileWide::POT > TileSquare::POT ? TileWide::POT : TileSquare::POT;
 
 __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
@@ -37,7 +51,7 @@ __device__ __forceinline__ float4 clip4(float4 v) {
     return make_float4(clip01(v.x), clip01(v.y), clip01(v.z), clip01(v.w));
 }
 
-// Per-thread load plan for one shared field plane (precomputed once per block).
+// Per-thread load plan for one shared field plane (precomputed once per tile).
 struct LoadPlan {
     int goff[2];    // in-plane global offset of the float4 (wrapped)
     int soff[2];    // shared offset
@@ -45,28 +59,30 @@ struct LoadPlan {
     bool own[2];    // inside the tile and the domain (written back in fused mode)
 };
 
+template <class T>
 __device__ __forceinline__ LoadPlan make_load_plan(int tid, int j0, int k0, int ny, int nz) {
     LoadPlan L;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
         const int e = tid + s * THREADS;
-        L.valid[s] = e < NLOAD;
-        const int row = L.valid[s] ? e / NQ : 0;
-        const int q = L.valid[s] ? e - row * NQ : 0;
+        L.valid[s] = e < T::NLOAD;
+        const int row = L.valid[s] ? e / T::NQ : 0;
+        const int q = L.valid[s] ? e - row * T::NQ : 0;
         const int gy = j0 + row - 2, gz = k0 + 4 * q - 4;
-        L.own[s] = L.valid[s] && row >= 2 && row < 2 + TY && q >= 1 && q < 1 + TZ / 4 && gy < ny && gz < nz;
+        L.own[s] = L.valid[s] && row >= 2 && row < 2 + T::TY && q >= 1 && q < 1 + T::TZ / 4 && gy < ny && gz < nz;
         L.goff[s] = pmod(gy, ny) * nz + pmod(gz, nz);
-        L.soff[s] = row * W + 4 * q;
+        L.soff[s] = row * T::W + 4 * q;
     }
     return L;
 }
 
-// Grid over (z tiles, y tiles, x chunks) sized to about one wave of resident blocks.
+// Grid over (z tiles, y tiles, x chunks) sized to at most one wave of resident blocks.
+template <class T>
 inline dim3 fast_grid(int nx, int ny, int nz, int blocks_per_sm, int sms, int* LX) {
-    const int tz = (nz + TZ - 1) / TZ, ty = (ny + TY - 1) / TY;
+    const int tz = (nz + T::TZ - 1) / T::TZ, ty = (ny + T::TY - 1) / T::TY;
     const long tiles = (long)tz * ty;
     const long slots = (long)blocks_per_sm * sms;
-    long chunks = slots / tiles;                         // at most one wave: no partial second wave
+    long chunks = slots / tiles;                          // no partial second wave
     if (chunks < 1) chunks = 1;
     int lx = (int)((nx + chunks - 1) / chunks);
     if (lx < 8) lx = 8;                                   // keep the x halo overhead bounded
@@ -85,11 +101,39 @@ inline bool fast_ok(const evx_grid* g, std::initializer_list<const void*> ptrs) 
     return true;
 }
 
+// Tile variant for a grid: 0 = 16 x 64, 1 = 32 x 32.  Default: the square tile
+// when nz is a multiple of 32 but not of 64, else the wide one.
+inline int default_tile_variant(int nz) { return (nz % 64 != 0 && nz % 32 == 0) ? 1 : 0; }
+int ch_tile_variant(int nz);   // honours evx_set_tile_variant
+
 int ch_rhs_fast_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
                        const Geo& G, const ChP& P, cudaStream_t st);
 int ch_pullback_fast_launch(bool grads, const float* u, const float* g, const float* lam, const float* h,
                             const float* u1, float* lam_out, double* part, int n_part_cap, const evx_grid* grid,
                             const Geo& G, const ChP& P, cudaStream_t st, int* n_part_used);
 int ch_pullback_fast_blocks(const evx_grid* g);
+
+// ---- batched (persistent) kernels ------------------------------------------------
+// One work item = one tile x one x-chunk of one instance.
+struct BatchInst {
+    int nx, ny, nz, tile;          // tile variant (0 wide, 1 square)
+    long long off;                 // field offset (floats) in the packed buffers
+    int part0;                     // first work item of this instance (partial sums)
+    int orig;                      // the caller's index of this instance
+    float ih[3], ih2[3], ih2sum;
+    ChP P;
+};
+struct BatchItem {
+    int inst;
+    int k0, j0, x0, x1;
+    int part;                      // partial-sum slot (items of one instance are consecutive slots)
+};
+int batch_rhs_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const BatchInst* insts,
+                     const BatchItem* items, int n_items, int* counter, int grid, cudaStream_t st);
+int batch_pullback_launch(bool grads, const float* u, const float* g, const float* lam, const float* h,
+                          const float* u1, float* lam_out, double* part, const BatchInst* insts,
+                          const BatchItem* items, int n_items, int* counter, int grid, cudaStream_t st);
+int batch_rhs_blocks_per_sm();
+int batch_pullback_blocks_per_sm(bool grads);
 
 }  // namespace evx

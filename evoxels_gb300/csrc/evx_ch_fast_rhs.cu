@@ -1,12 +1,16 @@
-// Periodic fast path of the Cahn-Hilliard right-hand side (see evx_ch_fast.cuh
-// for the tiling).  Same float32 operations, in the same order, as the generic
+// Periodic fast path of the Cahn-Hilliard right-hand side (tiling in
+// evx_ch_fast.cuh).  Same float32 operations, in the same order, as the generic
 // kernel and the reference (evoxels/problem_definition.py:350-371); the
 // translation unit is compiled with --fmad=false, so results are bit-identical.
 //
-// Per x-plane i a block: stores the prefetched field plane i+2 (clipped) into a
+// Per x-plane i a tile: stores the prefetched field plane i+2 (clipped) into a
 // 4-slot shared ring and issues the global loads of plane i+3; computes the
 // chemical potential of plane i+1 over the tile grown by one cell (2-slot
 // ring); then computes r on plane i.  Two barriers per plane.
+//
+// The tile body is shared by the single-grid kernel (one block per tile and
+// x-chunk) and the batched kernel (persistent blocks pulling instance x tile x
+// x-chunk work items from a global counter).
 #include "evx_ch_fast.cuh"
 
 namespace evx {
@@ -20,20 +24,15 @@ __device__ __forceinline__ float mu_at(const Geo& G, const ChP& P, float c, floa
     return __fsub_rn(mu_hom(P.w, c), __fmul_rn(P.kappa, lap7(G, c, xm, xp, ym, yp, zm, zp)));
 }
 
-template <bool FUSED>
-__global__ void __launch_bounds__(THREADS, 4)
-ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, float* __restrict__ u_new,
-                   float* __restrict__ r, Geo G, ChP P, int LX) {
-    __shared__ __align__(16) float cs[4][CR][W];
-    __shared__ __align__(16) float ms[2][MR][W];
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    const int k0 = blockIdx.x * TZ, j0 = blockIdx.y * TY;
-    const int x0 = blockIdx.z * LX;
-    const int x1 = min(x0 + LX, G.nx);
-    if (x0 >= x1) return;   // uniform across the block
+template <class T, bool FUSED>
+__device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const float* __restrict__ upd,
+                                         float* __restrict__ u_new, float* __restrict__ r, const Geo& G,
+                                         const ChP& P, int k0, int j0, int x0, int x1, float* cs, float* ms) {
+    const int tid = threadIdx.x;
+    const int tx = tid % T::BX, ty = tid / T::BX;
     const int nx = G.nx, ny = G.ny, nz = G.nz;
     const size_t plane = (size_t)ny * nz;
-    const LoadPlan LP = make_load_plan(tid, j0, k0, ny, nz);
+    const LoadPlan LP = make_load_plan<T>(tid, j0, k0, ny, nz);
 
     // potential patches owned by this thread (at most two)
     int mr[2], mc[2];
@@ -41,14 +40,14 @@ ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, f
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
         const int pidx = tid + m * THREADS;
-        mv[m] = pidx < NMU;
-        const int py = mv[m] ? pidx / MPZ : 0;
-        mr[m] = 1 + 2 * py;                       // field row of the patch's upper row
-        mc[m] = 2 + 2 * (pidx - py * MPZ);         // field column of the patch's left column
+        mv[m] = pidx < T::NMU;
+        const int py = mv[m] ? pidx / T::MPZ : 0;
+        mr[m] = 1 + 2 * py;                        // field row of the patch's upper row
+        mc[m] = 2 + 2 * (pidx - py * T::MPZ);       // field column of the patch's left column
     }
-    // output patch
-    const int ra = 2 + 2 * ty, rc = 4 + 2 * tx;   // field row / column in shared memory
-    const int gj = j0 + 2 * ty, gk = k0 + 2 * tx;  // global y / z of the patch origin
+    const int W = T::W;
+    const int ra = 2 + 2 * ty, rc = 4 + 2 * tx;    // field row / column in shared memory
+    const int gj = j0 + 2 * ty, gk = k0 + 2 * tx;   // global y / z of the patch origin
     const bool wk = gk < nz, wj0 = gj < ny && wk, wj1 = gj + 1 < ny && wk;
     const float ihx = G.ih[0], ihy = G.ih[1], ihz = G.ih[2];
 
@@ -69,16 +68,16 @@ ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, f
         }
     };
     auto stash = [&](int p) {
-        float* dst = &cs[p & 3][0][0];
+        float* dst = cs + (p & 3) * T::FIELD;
 #pragma unroll
         for (int s = 0; s < 2; ++s)
             if (LP.valid[s]) sts4(dst + LP.soff[s], clip4(pf[s]));
     };
     auto compute_mu = [&](int p) {
-        const float* cc = &cs[p & 3][0][0];
-        const float* cm = &cs[(p - 1) & 3][0][0];
-        const float* cp = &cs[(p + 1) & 3][0][0];
-        float* mo = &ms[p & 1][0][0];
+        const float* cc = cs + (p & 3) * T::FIELD;
+        const float* cm = cs + ((p - 1) & 3) * T::FIELD;
+        const float* cp = cs + ((p + 1) & 3) * T::FIELD;
+        float* mo = ms + (p & 1) * T::POT;
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
             if (!mv[m]) continue;
@@ -95,12 +94,12 @@ ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, f
         }
     };
 
-    float fxm[4];   // x flux on the face below the current plane, per patch point
+    float fxm[4] = {0.f, 0.f, 0.f, 0.f};   // x flux on the face below the current plane
     auto x_faces = [&](int plo, float out[4]) {
-        const float* c0 = &cs[plo & 3][0][0];
-        const float* c1 = &cs[(plo + 1) & 3][0][0];
-        const float* m0 = &ms[plo & 1][0][0];
-        const float* m1 = &ms[(plo + 1) & 1][0][0];
+        const float* c0 = cs + (plo & 3) * T::FIELD;
+        const float* c1 = cs + ((plo + 1) & 3) * T::FIELD;
+        const float* m0 = ms + (plo & 1) * T::POT;
+        const float* m1 = ms + ((plo + 1) & 1) * T::POT;
         const int a = ra * W + rc, b = a + W;
         const float2 cA0 = lds2(c0 + a), cB0 = lds2(c0 + b), cA1 = lds2(c1 + a), cB1 = lds2(c1 + b);
         const float2 mA0 = lds2(m0 + a - W), mB0 = lds2(m0 + b - W), mA1 = lds2(m1 + a - W), mB1 = lds2(m1 + b - W);
@@ -111,8 +110,8 @@ ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, f
     };
 
     auto compute_r = [&](int i) {
-        const float* cc = &cs[i & 3][0][0];
-        const float* mm = &ms[i & 1][0][0];
+        const float* cc = cs + (i & 3) * T::FIELD;
+        const float* mm = ms + (i & 1) * T::POT;
         const int a = ra * W + rc, b = a + W;     // field offsets; potential offsets are one row up
         float fxp[4];
         x_faces(i, fxp);
@@ -168,27 +167,128 @@ ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, f
     }
 }
 
-int g_rhs_blocks_per_sm = 0, g_sms = 0;
+template <class T, bool FUSED>
+__global__ void __launch_bounds__(THREADS, 4)
+ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, float* __restrict__ u_new,
+                   float* __restrict__ r, Geo G, ChP P, int LX) {
+    __shared__ __align__(16) float cs[4 * T::FIELD];
+    __shared__ __align__(16) float ms[2 * T::POT];
+    const int x0 = blockIdx.z * LX;
+    const int x1 = min(x0 + LX, G.nx);
+    if (x0 >= x1) return;   // uniform across the block
+    rhs_tile<T, FUSED>(u, upd, u_new, r, G, P, blockIdx.x * T::TZ, blockIdx.y * T::TY, x0, x1, cs, ms);
+}
 
-}  // namespace
-
-int ch_rhs_fast_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
-                       const Geo& G, const ChP& P, cudaStream_t st) {
-    if (!g_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rhs_blocks_per_sm, ch_rhs_fast_kernel<true>, THREADS, 0);
-        if (g_rhs_blocks_per_sm < 1) g_rhs_blocks_per_sm = 1;
+__device__ __forceinline__ Geo batch_geo(const BatchInst& B) {
+    Geo G;
+    G.nx = B.nx; G.ny = B.ny; G.nz = B.nz;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        G.kind[a] = EVX_BC_PERIODIC;
+        G.lo[a] = G.hi[a] = 0.f;
+        G.ih[a] = B.ih[a];
+        G.ih2[a] = B.ih2[a];
     }
+    G.ih2sum = B.ih2sum;
+    return G;
+}
+
+// Persistent batched rhs: blocks pull work items until the list is exhausted.
+template <bool FUSED>
+__global__ void __launch_bounds__(THREADS, 4)
+ch_rhs_batch_kernel(const float* __restrict__ u, const float* __restrict__ upd, float* __restrict__ u_new,
+                    float* __restrict__ r, const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
+                    int n_items, int* __restrict__ counter) {
+    __shared__ __align__(16) float cs[4 * MAX_FIELD];
+    __shared__ __align__(16) float ms[2 * MAX_POT];
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n_items) break;
+        const BatchItem I = items[it];
+        const BatchInst B = insts[I.inst];
+        const Geo G = batch_geo(B);
+        const size_t o = (size_t)B.off;
+        if (B.tile == 0)
+            rhs_tile<TileWide, FUSED>(u + o, FUSED ? upd + o : nullptr, FUSED ? u_new + o : nullptr, r + o, G, B.P,
+                                      I.k0, I.j0, I.x0, I.x1, cs, ms);
+        else
+            rhs_tile<TileSquare, FUSED>(u + o, FUSED ? upd + o : nullptr, FUSED ? u_new + o : nullptr, r + o, G,
+                                        B.P, I.k0, I.j0, I.x0, I.x1, cs, ms);
+        __syncthreads();   // shared memory and s_item are reused by the next item
+    }
+}
+
+int g_rhs_bps[2] = {0, 0}, g_sms = 0, g_batch_bps = 0;
+int g_tile_override = -1;
+
+void init_rhs_occupancy() {
+    if (g_sms) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rhs_bps[0], ch_rhs_fast_kernel<TileWide, true>, THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rhs_bps[1], ch_rhs_fast_kernel<TileSquare, true>, THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_batch_bps, ch_rhs_batch_kernel<true>, THREADS, 0);
+    for (int* b : {&g_rhs_bps[0], &g_rhs_bps[1], &g_batch_bps})
+        if (*b < 1) *b = 1;
+}
+
+template <class T>
+int rhs_fast_launch_t(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
+                      const Geo& G, const ChP& P, cudaStream_t st, int bps) {
     int lx;
-    const dim3 grid = fast_grid(g->nx, g->ny, g->nz, g_rhs_blocks_per_sm, g_sms, &lx);
+    const dim3 grid = fast_grid<T>(g->nx, g->ny, g->nz, bps, g_sms, &lx);
     if (fused)
-        EVX_TIMED("ch_rhs_fused", st, ch_rhs_fast_kernel<true><<<grid, dim3(32, 8), 0, st>>>(u, upd, u_new, r, G, P, lx));
+        EVX_TIMED("ch_rhs_fused", st, ch_rhs_fast_kernel<T, true><<<grid, THREADS, 0, st>>>(u, upd, u_new, r, G, P, lx));
     else
-        EVX_TIMED("ch_rhs", st, ch_rhs_fast_kernel<false><<<grid, dim3(32, 8), 0, st>>>(u, nullptr, nullptr, r, G, P, lx));
+        EVX_TIMED("ch_rhs", st, ch_rhs_fast_kernel<T, false><<<grid, THREADS, 0, st>>>(u, nullptr, nullptr, r, G, P, lx));
     count_launch();
     return check_launch("ch_rhs_fast_kernel");
 }
 
+}  // namespace
+
+int ch_tile_variant(int nz) {
+    if (g_tile_override == 0) return 0;
+    if (g_tile_override == 1) return 1;
+    return default_tile_variant(nz);
+}
+
+int ch_rhs_fast_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
+                       const Geo& G, const ChP& P, cudaStream_t st) {
+    init_rhs_occupancy();
+    if (ch_tile_variant(g->nz) == 1)
+        return rhs_fast_launch_t<TileSquare>(fused, u, upd, u_new, r, g, G, P, st, g_rhs_bps[1]);
+    return rhs_fast_launch_t<TileWide>(fused, u, upd, u_new, r, g, G, P, st, g_rhs_bps[0]);
+}
+
+int batch_rhs_blocks_per_sm() {
+    init_rhs_occupancy();
+    return g_batch_bps;
+}
+
+int batch_rhs_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const BatchInst* insts,
+                     const BatchItem* items, int n_items, int* counter, int grid, cudaStream_t st) {
+    int rc = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), st), "batch rhs counter reset");
+    if (rc) return rc;
+    if (fused)
+        EVX_TIMED("batch_rhs_fused", st,
+                  ch_rhs_batch_kernel<true><<<grid, THREADS, 0, st>>>(u, upd, u_new, r, insts, items, n_items, counter));
+    else
+        EVX_TIMED("batch_rhs", st,
+                  ch_rhs_batch_kernel<false><<<grid, THREADS, 0, st>>>(u, nullptr, nullptr, r, insts, items, n_items,
+                                                                       counter));
+    count_launch();
+    return check_launch("ch_rhs_batch_kernel");
+}
+
 }  // namespace evx
+
+extern "C" int evx_set_tile_variant(int variant) {
+    if (variant < -1 || variant > 1) return evx::fail(EVX_ERR_BAD_ARG, "tile variant must be -1, 0 or 1");
+    evx::g_tile_override = variant;
+    return EVX_OK;
+}

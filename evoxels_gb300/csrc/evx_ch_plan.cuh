@@ -45,6 +45,14 @@ int ch_plan_bind(evx_ch_plan* plan, void* workspace, cudaStream_t st, bool need_
 int ch_r2c(evx_ch_plan* plan, const float* in, float2* out, cudaStream_t st);
 int ch_c2r(evx_ch_plan* plan, float2* in, float* out, bool batch2, cudaStream_t st);
 
+// IMEX prefactor dt * (1/(1 - dt*(sym_coef*k4))) with k4 = (k^2)^2, in the
+// reference's float32 operation order (evoxels/timesteppers.py:77).
+__device__ __forceinline__ float imex_prefac(float k2, float sym_coef, float dt) {
+    const float k4 = __fmul_rn(k2, k2);
+    const float den = __fsub_rn(1.f, __fmul_rn(dt, __fmul_rn(sym_coef, k4)));
+    return __fmul_rn(__frcp_rn(den), dt);
+}
+
 // Forward k-space multiply: spec *= prefac(k) then * invN (in that order).
 int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st);
 

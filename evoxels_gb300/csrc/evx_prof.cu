@@ -59,6 +59,8 @@ ProfTok prof_begin(const char* name, cudaStream_t st) {
     ProfTok t{-1, nullptr};
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_on) return t;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return t;
     t.slot = slot_of(name);
     t.ev = take_event();
     cudaEventRecord(t.ev, st);

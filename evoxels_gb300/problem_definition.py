@@ -55,6 +55,21 @@ def double_well_coefficient(mu_hom, eps):
     return w
 
 
+def ch_params(eps, D, A, dt, w=None):
+    """``EvxChParams``: float32 roundings of the python-double constants the
+    reference evaluates (evoxels/problem_definition.py:303-305,
+    evoxels/timesteppers.py:77); ``w`` defaults to ``18/eps``."""
+    f = lambda x: float(np.float32(x))  # noqa: E731
+    p = _lib.EvxChParams()
+    p.D = f(D)
+    p.kappa = f(2 * eps)
+    p.w = f(18 / eps if w is None else w)
+    p.A = f(A)
+    p.sym_coef = f(-2 * eps * D * A)
+    p.dt = f(dt)
+    return p
+
+
 class _BCMixin:
     def initialize_boundary_conditions(self):
         """(evoxels/problem_definition.py:60-115); ghosts are applied in-kernel."""
@@ -120,15 +135,7 @@ class CahnHilliard(_BCMixin):
 
     def evx_params(self, dt=0.0):
         """float32 roundings of the python-double constants the reference evaluates."""
-        p = _lib.EvxChParams()
-        f = lambda x: float(np.float32(x))  # noqa: E731
-        p.D = f(self.D)
-        p.kappa = f(2 * self.eps)
-        p.w = f(self._w)
-        p.A = f(self.A)
-        p.sym_coef = f(-2 * self.eps * self.D * self.A)
-        p.dt = f(dt)
-        return p
+        return ch_params(self.eps, self.D, self.A, dt, self._w)
 
     def rhs(self, t, u):
         """``CahnHilliard.rhs`` on the GPU (evoxels/problem_definition.py:328-371)."""

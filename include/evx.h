@@ -163,6 +163,54 @@ int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps,
                    const float* lam_in, float* lam_out, const evx_ch_params* p,
                    double* grads, void* workspace, void* stream);
 
+/* Tile shape of the periodic fast-path stencil kernels (single grids):
+ * -1 automatic (32x32 when nz is a multiple of 32 but not of 64, else 16x64),
+ * 0 = 16x64, 1 = 32x32.  Results are bit-identical for every choice. */
+int evx_set_tile_variant(int variant);
+
+/* ---- batched uneven instances ---------------------------------------------
+ * Many independent periodic Cahn-Hilliard grids of different sizes stepped
+ * together (the reference batches parameter-estimation solves with jax.vmap,
+ * evoxels/inversion.py:121, over grids of one shape).  Fields of all instances
+ * live in one packed float32 buffer of evx_batch_field_floats() floats;
+ * instance i occupies [offsets[i], offsets[i] + nx*ny*nz) (evx_batch_offsets).
+ * Each instance needs nz % 4 == 0. */
+typedef struct evx_batch evx_batch;
+
+typedef struct evx_batch_instance {
+    int32_t nx, ny, nz, reserved;
+    double  h[3];
+    float   inv_h[3], inv_h2[3], inv_h2_sum;
+    evx_ch_params params;
+} evx_batch_instance;
+
+typedef struct evx_batch_tuning {
+    int32_t tile_variant;    /* -1 automatic per instance, 0 = 16x64, 1 = 32x32 */
+    int32_t x_chunk;         /* x planes per work item (0 = automatic) */
+    int32_t blocks_per_sm;   /* persistent blocks per SM (0 = occupancy limit) */
+    int32_t fft_group_max;   /* instances per cuFFT plan (0 = whole shape group) */
+    int32_t graph_steps;     /* fused steps per captured CUDA graph (0 = no graph) */
+} evx_batch_tuning;
+
+int evx_batch_create(evx_batch** batch, const evx_batch_instance* inst, int n,
+                     const evx_batch_tuning* tuning, int flags);
+int evx_batch_destroy(evx_batch* batch);
+size_t evx_batch_field_floats(const evx_batch* batch);
+size_t evx_batch_workspace_bytes(const evx_batch* batch);
+int evx_batch_work_items(const evx_batch* batch);
+int evx_batch_offsets(const evx_batch* batch, int64_t* offsets);
+
+/* nsteps IMEX steps of every instance (as evx_ch_forward, on packed buffers). */
+int evx_batch_forward(evx_batch* batch, const float* u_in, float* u_out, int nsteps,
+                      float* traj, int* nonfinite, void* workspace, void* stream);
+
+/* Adjoint of nsteps steps of every instance (as evx_ch_adjoint); grads
+ * (optional, device double[3*n]) accumulates dL/dD, dL/dkappa, dL/dw per
+ * instance, in the caller's instance order. */
+int evx_batch_adjoint(evx_batch* batch, const float* states, int nsteps,
+                      const float* lam_in, float* lam_out, double* grads,
+                      void* workspace, void* stream);
+
 /* ---- inversion loss ---------------------------------------------------------- */
 
 /* loss = mean((u - target)^2) (device double) and, if lam != NULL, its gradient
