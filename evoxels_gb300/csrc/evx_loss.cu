@@ -19,13 +19,15 @@ __global__ void __launch_bounds__(MSE_THREADS)
 mse_grad_kernel(const float* __restrict__ u, const float* __restrict__ t, size_t n, float scale,
                 float* __restrict__ lam, double* __restrict__ part) {
     __shared__ double red[MSE_THREADS / 32];
-    double acc = 0.0;
+    // per-thread float partial sums (a few dozen terms each), double across threads
+    float accf = 0.f;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
         const float d = __ldg(u + e) - __ldg(t + e);
         if (lam) lam[e] = scale * d;
-        acc += (double)d * (double)d;
+        accf = fmaf(d, d, accf);
     }
+    double acc = accf;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
