@@ -39,10 +39,9 @@ if ROOT not in sys.path:
 METRIC = "voxel-steps/s fwd+adjoint CH 256³: batched/fused vs plain, same GPU, ≤1e-5 err"
 FALLBACK_HBM_GBS = 6800.0
 
-# DRAM bytes (read + write) per voxel of one launch, from single-launch ncu
-# captures (profiles/ch_rhs_fast_256.md, profiles/ch_pullback_fast_256.md,
-# profiles/fd_step_reg_512.md, profiles/fd_tblock2_512.md); traffic grows in
-# proportion to the voxels a launch processes.
+# DRAM bytes (read + write) per voxel of one launch, from the single-launch ncu
+# captures summarised under profiles/ (rhs and pullback at 256^3, forward Euler
+# at 512^3); traffic grows in proportion to the voxels a launch processes.
 NCU_DRAM_BYTES_PER_VOXEL = {
     "ch_rhs_fused": (153.137408e6 + 92.517888e6) / 256 ** 3,
     "ch_pullback_grads": (344.547840e6 + 54.629120e6) / 256 ** 3,
