@@ -193,3 +193,30 @@ def default_checkpoint_interval(vg, nsteps, budget_bytes=None):
         if need <= budget_bytes:
             best = K
     return best
+
+
+def fit_parameters(runner, c0, target, nsteps, D0, eps0, iters=20, lr=0.05, checkpoint_every=None):
+    """Estimate ``(D, eps)`` from an observed final field (the reference's
+    parameter-estimation role, evoxels/inversion.py:126-233, with gradients from
+    the hand-written adjoint instead of JAX forward mode).
+
+    Adam on ``log D`` and ``log eps`` (positivity, as the reference's
+    ``pos_params``).  Returns ``(D, eps, history)``, history holding
+    ``(loss, D, eps)`` per iteration.
+    """
+    x = np.log(np.array([float(D0), float(eps0)]))
+    m = np.zeros(2)
+    v = np.zeros(2)
+    b1, b2 = 0.9, 0.999
+    hist = []
+    for it in range(1, iters + 1):
+        D, eps = np.exp(x)
+        loss, _, gD, geps = runner.loss_and_grads(c0, target, nsteps, D, eps, checkpoint_every)
+        hist.append((loss, float(D), float(eps)))
+        g = np.array([gD * D, geps * eps])           # chain rule to log-space
+        m = b1 * m + (1 - b1) * g
+        v = b2 * v + (1 - b2) * g * g
+        mh, vh = m / (1 - b1 ** it), v / (1 - b2 ** it)
+        x = x - lr * mh / (np.sqrt(vh) + 1e-12)
+    D, eps = np.exp(x)
+    return float(D), float(eps), hist
