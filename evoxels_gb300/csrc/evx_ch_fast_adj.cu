@@ -226,25 +226,22 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         const float* mm = ms + (i & 1) * T::POT;
         const float* bb = bs + (i & 1) * T::POT;
         const float* bp = bs + ((i + 1) & 1) * T::POT;
-        // acc: sum of cbar-face values around each point (times 0.5 at the end);
-        // div: forward divergence (parameter gradients only)
-        float acc[4], div[4];
+        // acc: sum of cbar-face values around each point (times 0.5 at the end)
+        float acc[4];
         {
             float cfx_p[4], Fx_p[4];
             x_faces_b(i, cfx_p, Fx_p);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 acc[q] = cfx_m[q] + cfx_p[q];
-                div[q] = GRADS ? (Fx_p[q] - Fx_m[q]) * ihx : 0.f;
                 cfx_m[q] = cfx_p[q];
-                Fx_m[q] = Fx_p[q];
             }
         }
         auto face = [&](int lo, int hi, float c_lo, float c_hi, float m_lo, float m_hi, float g_lo, float g_hi,
                         float ih, float ihD) {
-            const FaceB f = face_b<GRADS>(c_lo, c_hi, m_lo, m_hi, g_lo, g_hi, ih, ihD);
-            if (lo >= 0) { acc[lo] += f.cfb; if (GRADS) div[lo] += f.F * ih; }
-            if (hi >= 0) { acc[hi] += f.cfb; if (GRADS) div[hi] -= f.F * ih; }
+            const FaceB f = face_b<false>(c_lo, c_hi, m_lo, m_hi, g_lo, g_hi, ih, ihD);
+            if (lo >= 0) acc[lo] += f.cfb;
+            if (hi >= 0) acc[hi] += f.cfb;
         };
         {   // z faces
             const float2 A = lds2(cc + pa), MA = lds2(mm + pa - W), gA = lds2(gc + pa);
@@ -283,14 +280,14 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         const float2 A = lds2(cc + pa), B = lds2(cc + pb);
         const float cpt[4] = {A.x, A.y, B.x, B.y};
         const size_t o = (size_t)i * plane + (size_t)gj * nz + gk;
-        float ur[4];
+        float ur[4], lv[4];
         {
             const float2 u0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u + o)) : make_float2(0.f, 0.f);
             const float2 u1r = wj1 ? __ldg(reinterpret_cast<const float2*>(u + o + nz)) : make_float2(0.f, 0.f);
             const float2 l0 = wj0 ? __ldg(reinterpret_cast<const float2*>(lam + o)) : make_float2(0.f, 0.f);
             const float2 l1 = wj1 ? __ldg(reinterpret_cast<const float2*>(lam + o + nz)) : make_float2(0.f, 0.f);
             ur[0] = u0.x; ur[1] = u0.y; ur[2] = u1r.x; ur[3] = u1r.y;
-            const float lv[4] = {l0.x, l0.y, l1.x, l1.y};
+            lv[0] = l0.x; lv[1] = l0.y; lv[2] = l1.x; lv[3] = l1.y;
             float out[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -309,8 +306,6 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
                 lap_f(G, A.y, c_prev[1], cxA.y, up.y, B.y, A.x, cc[pa + 2]),
                 lap_f(G, B.x, c_prev[2], cxB.x, A.x, dn.x, cc[pb - 1], B.y),
                 lap_f(G, B.y, c_prev[3], cxB.y, A.y, dn.y, B.x, cc[pb + 2])};
-            const float2 gA = lds2(gc + pa), gB = lds2(gc + pb);
-            const float gpt[4] = {gA.x, gA.y, gB.x, gB.y};
             const float2 h0 = wj0 ? __ldg(reinterpret_cast<const float2*>(hfield + o)) : make_float2(0.f, 0.f);
             const float2 h1 = wj1 ? __ldg(reinterpret_cast<const float2*>(hfield + o + nz)) : make_float2(0.f, 0.f);
             const float2 n0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u1 + o)) : make_float2(0.f, 0.f);
@@ -318,9 +313,11 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             const float hv[4] = {h0.x, h0.y, h1.x, h1.y}, nv[4] = {n0.x, n0.y, n1.x, n1.y};
             const bool okp[4] = {wj0, wj0, wj1, wj1};
 #pragma unroll
+            const float invD = 1.f / P.D;
             for (int q = 0; q < 4; ++q) {
                 if (!okp[q]) continue;
-                sD += gpt[q] * div[q];
+                // <g, r/D> = <P lam', r>/D = <lam', u' - u>/D  (P is symmetric)
+                sD += lv[q] * (nv[q] - ur[q]) * invD;
                 sK -= bpt[q] * lc[q];
                 sW += bpt[q] * phi_c(cpt[q]);
                 sH += hv[q] * (nv[q] - ur[q]);
@@ -406,7 +403,7 @@ __device__ __forceinline__ Geo batch_geo(const BatchInst& B) {
 // Persistent batched pullback; with GRADS each work item writes its partial sums
 // to part[item*4 .. item*4+3].
 template <bool GRADS>
-__global__ void __launch_bounds__(THREADS, GRADS ? 2 : 3)
+__global__ void __launch_bounds__(THREADS, 2)
 ch_pullback_batch_kernel(const float* __restrict__ u, const float* __restrict__ gfield, const float* __restrict__ lam,
                          const float* __restrict__ hfield, const float* __restrict__ u1, float* __restrict__ lam_out,
                          double* __restrict__ part, const BatchInst* __restrict__ insts,

@@ -257,45 +257,56 @@ fd_step_reg_kernel(const float* __restrict__ u, float* __restrict__ out, Geo G, 
     const bool active = q < nq && y < G.ny;
     if (x0 >= x1 || __all_sync(0xffffffffu, !active)) return;   // whole warp idle (warp-uniform exit)
     const int nx = G.nx, ny = G.ny, nz = G.nz;
-    const size_t plane = (size_t)ny * nz;
+    const int plane = ny * nz;   // fields have < 2^31 elements
     const bool px = G.kind[0] == EVX_BC_PERIODIC, py = G.kind[1] == EVX_BC_PERIODIC,
                pz = G.kind[2] == EVX_BC_PERIODIC;
     const int qc = active ? q : 0, yc = active ? y : 0;   // inactive lanes read a valid address
     const int z = 4 * qc;
-    const int row = yc * nz;
-    const int rym = (yc == 0 ? ny - 1 : yc - 1) * nz, ryp = (yc == ny - 1 ? 0 : yc + 1) * nz;
-    const bool ylo = !py && yc == 0, yhi = !py && yc == ny - 1;
+    const float* col = u + yc * nz + z;                   // this thread's column at plane 0
+    const int dym = ((yc == 0 ? ny - 1 : yc - 1) - yc) * nz, dyp = ((yc == ny - 1 ? 0 : yc + 1) - yc) * nz;
+    const bool ylo = !py && yc == 0, yhi = !py && yc == ny - 1;   // uniform per warp (one row per warp)
     const bool zlo = !pz && z == 0, zhi = !pz && z + 4 == nz;
-    const int zl_idx = z == 0 ? nz - 1 : z - 1, zr_idx = z + 4 == nz ? 0 : z + 4;
+    const int dzl = (z == 0 ? nz - 1 : z - 1) - z, dzr = (z + 4 == nz ? 0 : z + 4) - z;
     const bool left_load = lane == 0, right_load = lane == 31 || q + 1 >= nq;
-    auto ld4 = [&](size_t o) { return __ldg(reinterpret_cast<const float4*>(u + o)); };
+    auto ld4 = [](const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); };
+    auto glo4 = [&](int a, float4 c) {
+        return make_float4(ghost_lo(G, a, c.x), ghost_lo(G, a, c.y), ghost_lo(G, a, c.z), ghost_lo(G, a, c.w));
+    };
+    auto ghi4 = [&](int a, float4 c) {
+        return make_float4(ghost_hi(G, a, c.x), ghost_hi(G, a, c.y), ghost_hi(G, a, c.z), ghost_hi(G, a, c.w));
+    };
 
-    float4 c = ld4((size_t)pmod(x0, nx) * plane + row + z);
-    float4 xm = ld4((size_t)pmod(x0 - 1, nx) * plane + row + z);
-    float4 xp = ld4((size_t)pmod(x0 + 1, nx) * plane + row + z);
+    float4 c = ld4(col + x0 * plane);
+    float4 xm = ld4(col + (x0 == 0 ? nx - 1 : x0 - 1) * plane);
+    int ip = x0 + 1;
+    if (ip >= nx) ip -= nx;
+    float4 xp = ld4(col + ip * plane);
     for (int i = x0; i < x1; ++i) {
-        const size_t b = (size_t)i * plane;
-        const float4 ym = ld4(b + rym + z), yp = ld4(b + ryp + z);
-        const float el = left_load ? __ldg(u + b + row + zl_idx) : 0.f;
-        const float er = right_load ? __ldg(u + b + row + zr_idx) : 0.f;
-        const float4 nxt = ld4((size_t)pmod(i + 2, nx) * plane + row + z);   // prefetch plane i+2
+        const float* cp = col + i * plane;
+        float4 ym = ld4(cp + dym), yp = ld4(cp + dyp);
+        const float el = left_load ? __ldg(cp + dzl) : 0.f;
+        const float er = right_load ? __ldg(cp + dzr) : 0.f;
+        int in = i + 2;
+        while (in >= nx) in -= nx;
+        const float4 nxt = ld4(col + in * plane);   // prefetch plane i+2
         float zl = __shfl_up_sync(0xffffffffu, c.w, 1);
         float zr = __shfl_down_sync(0xffffffffu, c.x, 1);
         if (left_load) zl = el;
         if (right_load) zr = er;
         if (zlo) zl = ghost_lo(G, 2, c.x);
         if (zhi) zr = ghost_hi(G, 2, c.w);
-        const bool xlo = !px && i == 0, xhi = !px && i == nx - 1;
-        auto X = [&](float cv, float m) { return xlo ? ghost_lo(G, 0, cv) : m; };
-        auto XP = [&](float cv, float m) { return xhi ? ghost_hi(G, 0, cv) : m; };
-        auto Y = [&](float cv, float m) { return ylo ? ghost_lo(G, 1, cv) : m; };
-        auto YP = [&](float cv, float m) { return yhi ? ghost_hi(G, 1, cv) : m; };
+        if (ylo) ym = glo4(1, c);
+        if (yhi) yp = ghi4(1, c);
+        if (!px) {
+            if (i == 0) xm = glo4(0, c);
+            if (i == nx - 1) xp = ghi4(0, c);
+        }
         float4 v;
-        v.x = fd_point<UNIT>(G, D, dt, c.x, X(c.x, xm.x), XP(c.x, xp.x), Y(c.x, ym.x), YP(c.x, yp.x), zl, c.y);
-        v.y = fd_point<UNIT>(G, D, dt, c.y, X(c.y, xm.y), XP(c.y, xp.y), Y(c.y, ym.y), YP(c.y, yp.y), c.x, c.z);
-        v.z = fd_point<UNIT>(G, D, dt, c.z, X(c.z, xm.z), XP(c.z, xp.z), Y(c.z, ym.z), YP(c.z, yp.z), c.y, c.w);
-        v.w = fd_point<UNIT>(G, D, dt, c.w, X(c.w, xm.w), XP(c.w, xp.w), Y(c.w, ym.w), YP(c.w, yp.w), c.z, zr);
-        if (active) *reinterpret_cast<float4*>(out + b + row + z) = v;
+        v.x = fd_point<UNIT>(G, D, dt, c.x, xm.x, xp.x, ym.x, yp.x, zl, c.y);
+        v.y = fd_point<UNIT>(G, D, dt, c.y, xm.y, xp.y, ym.y, yp.y, c.x, c.z);
+        v.z = fd_point<UNIT>(G, D, dt, c.z, xm.z, xp.z, ym.z, yp.z, c.y, c.w);
+        v.w = fd_point<UNIT>(G, D, dt, c.w, xm.w, xp.w, ym.w, yp.w, c.z, zr);
+        if (active) *reinterpret_cast<float4*>(out + (cp - u)) = v;
         xm = c;
         c = xp;
         xp = nxt;
