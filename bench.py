@@ -58,6 +58,8 @@ def algorithmic_bytes(slot, n, nspec):
         "ch_axpy": 16 * n,          # read u, update; write u_out and the trajectory slot
         "ch_kspace_fwd": 16 * nspec,  # read + write the half spectrum
         "ch_kspace_adj": 24 * nspec,  # read lam_hat; write g_hat, h_hat
+        "ch_xpass_fwd": 16 * nspec,   # read + write the (y,z)-transformed spectrum
+        "ch_xpass_adj": 24 * nspec,   # read lam_hat; write g_hat and h_hat
         "ch_pullback_grads": 24 * n,  # read u_s, g, lam, h, u_{s+1}; write lam_s
         "ch_pullback": 16 * n,
         "mse_grad": 12 * n,

@@ -28,11 +28,16 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contra
               "-Xptxas", "-v", "-I", INCLUDE]
 # Forward kernels mirror the reference's float32 rounding op by op: no FMA
 # contraction.  The adjoint has no bitwise-parity requirement and contracts.
-FMAD_ON = {"evx_adjoint.cu", "evx_ch_fast_adj.cu"}
+FMAD_ON = {"evx_adjoint.cu", "evx_ch_fast_adj.cu", "evx_fftx.cu"}
 
 
 def _fmad(src):
     return ["--fmad=true"] if os.path.basename(src) in FMAD_ON else ["--fmad=false"]
+
+
+def _extra():
+    """Developer hook: extra nvcc flags (e.g. -D tuning macros) from EVX_EXTRA_NVCC_FLAGS."""
+    return os.environ.get("EVX_EXTRA_NVCC_FLAGS", "").split()
 
 
 def _nvcc():
@@ -52,7 +57,7 @@ def sources():
 
 def _fingerprint(srcs):
     h = hashlib.sha256()
-    h.update(" ".join(ARCH + NVCC_FLAGS + sorted(FMAD_ON)).encode())
+    h.update(" ".join(ARCH + NVCC_FLAGS + sorted(FMAD_ON) + _extra()).encode())
     deps = srcs + sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h")))
     deps.append(os.path.join(INCLUDE, "evx.h"))
     for p in deps:
@@ -78,7 +83,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + _fmad(src) + ["-c", src, "-o", obj]
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + _fmad(src) + _extra() + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

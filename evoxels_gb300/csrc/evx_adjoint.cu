@@ -267,11 +267,17 @@ int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps, const flo
     for (int s = nsteps - 1; s >= 0; --s) {
         float* dst = (s % 2 == 0) ? lam_out : lbuf;
         if ((rc = ch_r2c(plan, lam, spec, st))) return rc;
-        EVX_TIMED("ch_kspace_adj", st, ch_kspace_adj_kernel<<<elementwise_grid(plan->nspec), 256, 0, st>>>(
-            spec, want ? spec_h : nullptr, g->ny, plan->nzh, plan->nspec, plan->kx2, plan->ky2, plan->kz2,
-            P.sym_coef, P.dt, invN));
-        count_launch();
-        if ((rc = check_launch("ch_kspace_adj_kernel"))) return rc;
+        if (plan->xmode) {
+            if ((rc = xpass_launch(want ? 2 : 1, g->nx, spec, want ? spec_h : nullptr, g->ny * plan->nzh, plan->nzh,
+                                   plan->kx2, plan->ky2, plan->kz2, P.sym_coef, P.dt, invN, st)))
+                return rc;
+        } else {
+            EVX_TIMED("ch_kspace_adj", st, ch_kspace_adj_kernel<<<elementwise_grid(plan->nspec), 256, 0, st>>>(
+                spec, want ? spec_h : nullptr, g->ny, plan->nzh, plan->nspec, plan->kx2, plan->ky2, plan->kz2,
+                P.sym_coef, P.dt, invN));
+            count_launch();
+            if ((rc = check_launch("ch_kspace_adj_kernel"))) return rc;
+        }
         if ((rc = ch_c2r(plan, spec, gbuf, want, st))) return rc;
         const float* us = states + (size_t)s * N;
         if (fast_ok(g, {us, gbuf, lam, hbuf, us + N, dst})) {

@@ -268,6 +268,9 @@ int ch_c2r(evx_ch_plan* plan, float2* in, float* out, bool batch2, cudaStream_t 
 
 int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st) {
     const float invN = (float)(1.0 / (double)plan->n);
+    if (plan->xmode)
+        return xpass_launch(0, plan->g.nx, spec, nullptr, plan->g.ny * plan->nzh, plan->nzh, plan->kx2, plan->ky2,
+                            plan->kz2, P.sym_coef, P.dt, invN, st);
     EVX_TIMED("ch_kspace_fwd", st, ch_kspace_fwd_kernel<<<elementwise_grid(plan->nspec), 256, 0, st>>>(
         spec, plan->g.ny, plan->nzh, plan->nspec, plan->kx2, plan->ky2, plan->kz2, P.sym_coef, P.dt, invN));
     count_launch();
@@ -338,17 +341,38 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
     if ((rc = check_cufft(cufftCreate(&p->c2r), "cufftCreate"))) return cleanup(rc);
     cufftSetAutoAllocation(p->r2c, 0);
     cufftSetAutoAllocation(p->c2r, 0);
-    if ((rc = check_cufft(cufftMakePlan3d(p->r2c, g->nx, g->ny, g->nz, CUFFT_R2C, &w1), "cufftMakePlan3d R2C")))
-        return cleanup(rc);
-    if ((rc = check_cufft(cufftMakePlan3d(p->c2r, g->nx, g->ny, g->nz, CUFFT_C2R, &w2), "cufftMakePlan3d C2R")))
-        return cleanup(rc);
+    // power-of-two nx: cuFFT transforms (y, z) for every x plane and the fused x-pass does the rest
+    p->xmode = xpass_supported(g->nx) && !(flags & 2);
+    if (p->xmode) {
+        int d2[2] = {g->ny, g->nz};
+        const int pr = g->ny * g->nz, ps = g->ny * p->nzh;
+        if ((rc = check_cufft(cufftMakePlanMany(p->r2c, 2, d2, nullptr, 1, pr, nullptr, 1, ps, CUFFT_R2C, g->nx, &w1),
+                              "cufftMakePlanMany R2C (y,z)")))
+            return cleanup(rc);
+        if ((rc = check_cufft(cufftMakePlanMany(p->c2r, 2, d2, nullptr, 1, ps, nullptr, 1, pr, CUFFT_C2R, g->nx, &w2),
+                              "cufftMakePlanMany C2R (y,z)")))
+            return cleanup(rc);
+    } else {
+        if ((rc = check_cufft(cufftMakePlan3d(p->r2c, g->nx, g->ny, g->nz, CUFFT_R2C, &w1), "cufftMakePlan3d R2C")))
+            return cleanup(rc);
+        if ((rc = check_cufft(cufftMakePlan3d(p->c2r, g->nx, g->ny, g->nz, CUFFT_C2R, &w2), "cufftMakePlan3d C2R")))
+            return cleanup(rc);
+    }
     if (flags & 1) {
         if ((rc = check_cufft(cufftCreate(&p->c2r2), "cufftCreate"))) return cleanup(rc);
         cufftSetAutoAllocation(p->c2r2, 0);
-        int dims[3] = {g->nx, g->ny, g->nz};
-        if ((rc = check_cufft(cufftMakePlanMany(p->c2r2, 3, dims, nullptr, 1, (int)p->nspec, nullptr, 1,
-                                                (int)p->n, CUFFT_C2R, 2, &w3), "cufftMakePlanMany C2R x2")))
-            return cleanup(rc);
+        if (p->xmode) {
+            int d2[2] = {g->ny, g->nz};
+            const int pr = g->ny * g->nz, ps = g->ny * p->nzh;
+            if ((rc = check_cufft(cufftMakePlanMany(p->c2r2, 2, d2, nullptr, 1, ps, nullptr, 1, pr, CUFFT_C2R,
+                                                    2 * g->nx, &w3), "cufftMakePlanMany C2R (y,z) x2")))
+                return cleanup(rc);
+        } else {
+            int dims[3] = {g->nx, g->ny, g->nz};
+            if ((rc = check_cufft(cufftMakePlanMany(p->c2r2, 3, dims, nullptr, 1, (int)p->nspec, nullptr, 1,
+                                                    (int)p->n, CUFFT_C2R, 2, &w3), "cufftMakePlanMany C2R x2")))
+                return cleanup(rc);
+        }
         p->has_c2r2 = true;
     }
     p->ws_fft = std::max(w1, std::max(w2, w3));

@@ -13,6 +13,7 @@ struct evx_ch_plan {
     size_t nspec;            // nx*ny*nzh complex values
     cufftHandle r2c = 0, c2r = 0, c2r2 = 0;
     bool has_c2r2 = false;
+    bool xmode = false;      // cuFFT over (y, z) batched over x + fused x-pass (power-of-two nx)
     size_t ws_fft = 0;       // cuFFT work area (max over plans)
     float* kx2 = nullptr;    // device k^2 tables
     float* ky2 = nullptr;
@@ -55,6 +56,12 @@ __device__ __forceinline__ float imex_prefac(float k2, float sym_coef, float dt)
 
 // Forward k-space multiply: spec *= prefac(k) then * invN (in that order).
 int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st);
+
+// Fused spectral x-pass (evx_fftx.cu): mode 0 forward multiply, 1 adjoint g,
+// 2 adjoint g and h (h into spec_h).
+bool xpass_supported(int nx);
+int xpass_launch(int mode, int nx, float2* spec, float2* spec_h, int M, int nzh, const float* kx2, const float* ky2,
+                 const float* kz2, float sym, float dt, float invN, cudaStream_t st);
 
 // Tile shape shared by the rhs and pullback stencil kernels.
 constexpr int CH_TZ = 32;           // tile extent along z (= warp width)

@@ -25,14 +25,14 @@ from .voxelgrid import cuda_stream
 class ChPlan:
     """An ``evx_ch_plan`` plus its device workspace (one per grid shape/spacing/device)."""
 
-    def __init__(self, vg, grads=False):
+    def __init__(self, vg, grads=False, cufft3d=False):
         self.vg = vg
         self.grid = vg.evx_grid()
         self.grads = grads
         h = C.c_void_p()
+        flags = (1 if grads else 0) | (2 if cufft3d else 0)
         with torch.cuda.device(vg.device):
-            _lib.check(_lib.lib().evx_ch_plan_create(C.byref(h), self.grid, 1 if grads else 0),
-                       "evx_ch_plan_create")
+            _lib.check(_lib.lib().evx_ch_plan_create(C.byref(h), self.grid, flags), "evx_ch_plan_create")
         self.handle = h
         nbytes = int(_lib.lib().evx_ch_workspace_bytes(h))
         self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=vg.device)
@@ -51,12 +51,14 @@ _plan_lock = threading.Lock()
 _plans = {}
 
 
-def get_plan(vg, grads=False):
-    key = (vg.shape, vg.spacing, str(vg.device), bool(grads))
+def get_plan(vg, grads=False, cufft3d=False):
+    """Cached plan per grid; ``cufft3d`` forces cuFFT's 3-D transforms instead of the
+    (y, z) transforms plus the fused x-pass used for power-of-two ``Nx``."""
+    key = (vg.shape, vg.spacing, str(vg.device), bool(grads), bool(cufft3d))
     with _plan_lock:
         p = _plans.get(key)
         if p is None:
-            p = ChPlan(vg, grads)
+            p = ChPlan(vg, grads, cufft3d)
             _plans[key] = p
         return p
 

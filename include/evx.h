@@ -133,7 +133,9 @@ typedef struct evx_ch_plan evx_ch_plan;
 /* Plan for the periodic pseudo-spectral IMEX step (evoxels/timesteppers.py:64-89)
  * on an (nx, ny, nz) grid: cuFFT R2C/C2R plans without auto-allocated work
  * areas, and the k^2 tables.  flags: bit 0 = also build the batch-2 C2R plan
- * used by parameter gradients. */
+ * used by parameter gradients; bit 1 = always use cuFFT's 3-D transforms (by
+ * default a power-of-two nx uses cuFFT over (y, z) and a fused x-pass that
+ * does the x transforms and the k-space multiply in one read and write). */
 int evx_ch_plan_create(evx_ch_plan** plan, const evx_grid* g, int flags);
 int evx_ch_plan_destroy(evx_ch_plan* plan);
 

@@ -388,3 +388,43 @@ def test_ch_adjoint_fast_equals_generic(cuda_lib, shape, grads):
         ref, _, _ = oracle.ch_imex_vjp(keep[s], ref, 0.1, 1.5, 1.1)
     del v
     assert oracle.rel_to_max(a.cpu().numpy(), ref.numpy()) < 1e-4
+
+
+# ---------------------------------------------------------------------------
+# fused spectral x-pass (power-of-two Nx) vs cuFFT's 3-D transforms
+# ---------------------------------------------------------------------------
+
+def _forward_with(vg, prob, u0, n, cufft3d):
+    from evoxels_gb300 import _lib
+    from evoxels_gb300.timesteppers import get_plan
+    from evoxels_gb300.voxelgrid import cuda_stream
+    plan = get_plan(vg, grads=True, cufft3d=cufft3d)
+    traj = torch.empty((n + 1,) + tuple(vg.shape), dtype=torch.float32, device=DEV)
+    traj[0] = u0[0]
+    out = torch.empty_like(u0)
+    _lib.check(_lib.lib().evx_ch_forward(plan.handle, traj[0:1].data_ptr(), out.data_ptr(), n, traj[1:].data_ptr(),
+                                         prob.evx_params(0.1), None, plan.workspace.data_ptr(), cuda_stream()))
+    lam = torch.tensor(oracle.seeded_unit_field(vg.shape, 77) - 0.5, dtype=torch.float32, device=DEV).unsqueeze(0)
+    lo = torch.empty_like(lam)
+    gr = torch.zeros(3, dtype=torch.float64, device=DEV)
+    _lib.check(_lib.lib().evx_ch_adjoint(plan.handle, traj.data_ptr(), n, lam.data_ptr(), lo.data_ptr(),
+                                         prob.evx_params(0.1), gr.data_ptr(), plan.workspace.data_ptr(), cuda_stream()))
+    return out, lo, gr
+
+
+@pytest.mark.parametrize("shape", [(8, 12, 20), (16, 16, 16), (32, 20, 36), (64, 12, 24), (128, 8, 12),
+                                   (256, 6, 8), (512, 4, 8), (256, 64, 64)])
+def test_xpass_matches_cufft3d_and_fp64(cuda_lib, shape):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    u0n = oracle.seeded_ch_field(shape, 8)
+    vg = vg_for(shape)
+    prob = CahnHilliard(vg, eps=1.7, D=1.3)
+    u0 = gpu(u0n)
+    a, la, ga = _forward_with(vg, prob, u0, 3, cufft3d=False)
+    b, lb, gb = _forward_with(vg, prob, u0, 3, cufft3d=True)
+    assert oracle.rel_to_max(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
+    assert oracle.rel_to_max(la.cpu().numpy(), lb.cpu().numpy()) < 1e-5
+    for x, y in zip(ga.cpu().tolist(), gb.cpu().tolist()):
+        assert abs(x - y) <= 1e-4 * max(abs(y), 1e-9)
+    ref = oracle.ch_imex_run(cpu64(u0n), 3, 0.1, 1.7, 1.3).numpy()
+    assert oracle.rel_to_max(a.cpu().numpy(), ref) <= 3e-5
