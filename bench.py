@@ -60,7 +60,10 @@ def algorithmic_bytes(slot, n, nspec):
         "ch_kspace_adj": 24 * nspec,  # read lam_hat; write g_hat, h_hat
         "ch_xpass_fwd": 16 * nspec,   # read + write the (y,z)-transformed spectrum
         "ch_xpass_adj": 24 * nspec,   # read lam_hat; write g_hat and h_hat
+        "ch_xpass_fwd_store": 24 * nspec,  # read + write the spectrum; write the stored increment spectrum
+        "ch_xpass_adj_spec": 24 * nspec,   # read lam_hat and the stored spectrum; write g_hat
         "ch_pullback_grads": 24 * n,  # read u_s, g, lam, h, u_{s+1}; write lam_s
+        "ch_pullback_grads_spec": 16 * n,  # read u_s, g, lam; write lam_s
         "ch_pullback": 16 * n,
         "mse_grad": 12 * n,
         "cufft_r2c": 4 * n + 8 * nspec,
@@ -184,20 +187,22 @@ class ChFwdAdj:
         self.c0.copy_(self.c0_host)
         self.target = self.t_host.to(device)
         self.lam = torch.empty((1,) + self.shape, dtype=torch.float32, device=device)
+        self.spectra = self.runner.new_spectra(self.T) if grads else None
         self.g_host = torch.empty((1,) + self.shape, dtype=torch.float32).pin_memory()
         self.units_per_step = self.n * self.T
         self.config = {"workload": f"ch{n}_fwd_adj", "grid": list(self.shape), "fwd_adj_steps_per_bench_step": self.T,
                        "dt": 0.1, "eps": 3.0, "D": 1.0, "A": 0.25, "bc": "periodic", "seed_c0": seed,
                        "seed_target": seed + 100, "param_grads": grads,
+                       "stored_spectra": self.spectra is not None,
                        "l2": "inputs larger than L2: the kept trajectory is %.2f GB" % ((self.T + 1) * 4 * self.n / 1e9)}
 
     def step(self):
         """Device-resident step: forward (trajectory kept), loss gradient, adjoint."""
         r = self.runner
-        r.forward(self.traj[0:1], self.T, 1.0, 3.0, traj=self.traj[1:])
+        r.forward(self.traj[0:1], self.T, 1.0, 3.0, traj=self.traj[1:], spectra=self.spectra)
         loss = r.mse(self.traj[self.T:self.T + 1], self.target, self.lam)
         grads = self.torch.zeros(3, dtype=self.torch.float64, device=self.c0.device) if self.grads else None
-        g0 = r.adjoint(self.traj, self.T, self.lam, 1.0, 3.0, grads)
+        g0 = r.adjoint(self.traj, self.T, self.lam, 1.0, 3.0, grads, self.spectra)
         return loss, g0, grads
 
     def step_e2e(self):

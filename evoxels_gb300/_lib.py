@@ -74,6 +74,10 @@ _SIGS = {
     "evx_ch_step": (C.c_int, [_P, _P, _P, C.POINTER(EvxChParams), _P, _P]),
     "evx_ch_forward": (C.c_int, [_P, _P, _P, C.c_int, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
+    "evx_ch_spectrum_floats": (C.c_size_t, [_P]),
+    "evx_device_status": (C.c_int, [C.c_int]),
+    "evx_ch_forward_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
+    "evx_ch_adjoint_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_set_tile_variant": (C.c_int, [C.c_int]),
     "evx_batch_create": (C.c_int, [C.POINTER(_P), C.POINTER(EvxBatchInstance), C.c_int, C.POINTER(EvxBatchTuning),
                                    C.c_int]),

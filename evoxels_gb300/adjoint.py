@@ -33,14 +33,21 @@ class CahnHilliardAdjoint:
     ``pinned_w``: when given, the bulk term is ``pinned_w*c(1-c)(1-2c)``
     independent of ``eps`` (the reference's callable ``mu_hom`` pinned to a
     fixed coefficient); otherwise it is ``18/eps*c(1-c)(1-2c)``.
+
+    ``spectral``: keep each forward step's increment spectrum beside the
+    trajectory (when the grid has the x-pass, power-of-two ``Nx``) so the
+    adjoint forms the mobility gradient sums by Parseval in k-space; this
+    costs one more field-sized buffer per step and saves an inverse FFT and
+    two field reads per adjoint step.
     """
 
-    def __init__(self, vg: VoxelGridGB300, dt=0.1, A=0.25, pinned_w=None):
+    def __init__(self, vg: VoxelGridGB300, dt=0.1, A=0.25, pinned_w=None, spectral=True):
         self.vg = vg
         self.dt = float(dt)
         self.A = float(A)
         self.pinned_w = pinned_w
         self.plan = get_plan(vg, grads=True)
+        self.spec_floats = int(_lib.lib().evx_ch_spectrum_floats(self.plan.handle)) if spectral else 0
         self.n = int(np.prod(vg.shape))
         self._pcache = {}
         self._mse_scratch = torch.empty(int(_lib.lib().evx_mse_scratch_bytes(self.n)), dtype=torch.uint8,
@@ -58,22 +65,32 @@ class CahnHilliardAdjoint:
         prob = CahnHilliard(self.vg, eps=float(eps), D=float(D), mu_hom=mu, A=self.A)
         return prob.evx_params(self.dt)
 
-    def forward(self, u0, nsteps, D, eps, traj=None):
-        """``nsteps`` IMEX steps; ``traj`` (optional) receives u_1..u_n."""
+    def new_spectra(self, nsteps):
+        """Buffer for ``nsteps`` stored increment spectra, or None when not kept."""
+        if not self.spec_floats:
+            return None
+        return torch.empty(int(nsteps) * self.spec_floats, dtype=torch.float32, device=self.vg.device)
+
+    def forward(self, u0, nsteps, D, eps, traj=None, spectra=None):
+        """``nsteps`` IMEX steps; ``traj`` (optional) receives u_1..u_n, ``spectra``
+        (optional, from ``new_spectra``) the increment spectra of the steps."""
         out = torch.empty_like(u0)
         p = self.params(D, eps)
-        _lib.check(_lib.lib().evx_ch_forward(self.plan.handle, u0.data_ptr(), out.data_ptr(), int(nsteps),
-                                             traj.data_ptr() if traj is not None else None, p, None,
-                                             self.plan.workspace.data_ptr(), cuda_stream()), "evx_ch_forward")
+        _lib.check(_lib.lib().evx_ch_forward_spectra(
+            self.plan.handle, u0.data_ptr(), out.data_ptr(), int(nsteps),
+            traj.data_ptr() if traj is not None else None, spectra.data_ptr() if spectra is not None else None,
+            p, None, self.plan.workspace.data_ptr(), cuda_stream()), "evx_ch_forward_spectra")
         return out
 
-    def adjoint(self, states, nsteps, lam, D, eps, grads):
-        """Adjoint through ``states`` (``nsteps+1`` consecutive fields); accumulates into ``grads``."""
+    def adjoint(self, states, nsteps, lam, D, eps, grads, spectra=None):
+        """Adjoint through ``states`` (``nsteps+1`` consecutive fields); accumulates into ``grads``.
+        ``spectra``: the forward's stored spectra of the same steps (optional)."""
         out = torch.empty_like(lam)
         p = self.params(D, eps)
-        _lib.check(_lib.lib().evx_ch_adjoint(self.plan.handle, states.data_ptr(), int(nsteps), lam.data_ptr(),
-                                             out.data_ptr(), p, grads.data_ptr() if grads is not None else None,
-                                             self.plan.workspace.data_ptr(), cuda_stream()), "evx_ch_adjoint")
+        _lib.check(_lib.lib().evx_ch_adjoint_spectra(
+            self.plan.handle, states.data_ptr(), spectra.data_ptr() if spectra is not None else None, int(nsteps),
+            lam.data_ptr(), out.data_ptr(), p, grads.data_ptr() if grads is not None else None,
+            self.plan.workspace.data_ptr(), cuda_stream()), "evx_ch_adjoint_spectra")
         return out
 
     def mse(self, u, target, lam=None):
@@ -92,8 +109,9 @@ class CahnHilliardAdjoint:
         if K >= nsteps:
             traj = torch.empty((nsteps + 1,) + tuple(c0.shape[1:]), dtype=torch.float32, device=c0.device)
             traj[0].copy_(c0[0])
-            self.forward(traj[0:1], nsteps, D, eps, traj=traj[1:])
-            return traj[nsteps:nsteps + 1], {"traj": traj}
+            spectra = self.new_spectra(nsteps)
+            self.forward(traj[0:1], nsteps, D, eps, traj=traj[1:], spectra=spectra)
+            return traj[nsteps:nsteps + 1], {"traj": traj, "spectra": spectra}
         cps = [c0]
         u = c0
         s = 0
@@ -109,15 +127,16 @@ class CahnHilliardAdjoint:
         """Adjoint through all steps; segments are recomputed from their checkpoints."""
         grads = torch.zeros(3, dtype=torch.float64, device=lam_T.device) if want_params else None
         if "traj" in saved:
-            return self.adjoint(saved["traj"], nsteps, lam_T, D, eps, grads), grads
+            return self.adjoint(saved["traj"], nsteps, lam_T, D, eps, grads, saved.get("spectra")), grads
         cps = saved["cps"]
         seg_buf = torch.empty((K + 1,) + tuple(lam_T.shape[1:]), dtype=torch.float32, device=lam_T.device)
+        seg_spec = self.new_spectra(K) if want_params else None
         lam = lam_T
         for si in range(len(cps) - 1, -1, -1):
             m = min(K, nsteps - si * K)
             seg_buf[0].copy_(cps[si][0])
-            self.forward(seg_buf[0:1], m, D, eps, traj=seg_buf[1:m + 1])
-            lam = self.adjoint(seg_buf[:m + 1], m, lam, D, eps, grads)
+            self.forward(seg_buf[0:1], m, D, eps, traj=seg_buf[1:m + 1], spectra=seg_spec)
+            lam = self.adjoint(seg_buf[:m + 1], m, lam, D, eps, grads, seg_spec)
         return lam, grads
 
     def param_grads(self, grads, eps):
@@ -178,8 +197,9 @@ def ch_imex_trajectory(c0, D, eps, nsteps, runner, checkpoint_every=None):
     return CahnHilliardIMEXFunction.apply(c0, D, eps, runner, int(nsteps), checkpoint_every)
 
 
-def default_checkpoint_interval(vg, nsteps, budget_bytes=None):
-    """Largest K whose (K+1)-state segment buffer plus n/K checkpoints fit the budget.
+def default_checkpoint_interval(vg, nsteps, budget_bytes=None, spectrum_bytes=0):
+    """Largest K whose (K+1)-state segment buffer, K stored spectra of
+    ``spectrum_bytes`` each, and n/K checkpoints fit the budget.
 
     Default budget: half of the device's free memory.
     """
@@ -189,7 +209,7 @@ def default_checkpoint_interval(vg, nsteps, budget_bytes=None):
         budget_bytes = free // 2
     best = 1
     for K in range(1, nsteps + 1):
-        need = (K + 1) * field + math.ceil(nsteps / K) * field
+        need = (K + 1) * field + K * spectrum_bytes + math.ceil(nsteps / K) * field
         if need <= budget_bytes:
             best = K
     return best

@@ -21,7 +21,10 @@
 //   dL/dw     += <mub, phi(c)>
 // (d prefac/da = -prefac^2 k^4, and P r = u' - u).  Block partial sums are
 // written to the workspace and reduced in a fixed order by one block, so the
-// gradients are deterministic.
+// gradients are deterministic.  With the increment spectra stored by the
+// forward pass (x-pass plans), <g, div> = <lam', u'-u>/D and <K lam', u'-u>
+// are Parseval sums formed in the adjoint x-pass instead, which drops the
+// inverse transform of K lam' and the reads of u' and K lam' in the pullback.
 #include <algorithm>
 
 #include "evx_ch_fast.cuh"
@@ -135,10 +138,12 @@ ch_pullback_kernel(const float* __restrict__ u, const float* __restrict__ g, con
             lam_out[idx] = __ldg(lam + idx) + (pass ? cbar : 0.f);
             if (GRADS) {
                 const float lapc = lap7(G, c, cxm, cxp, cym, cyp, czm, czp);
-                sD += (double)gc * (double)div;
                 sK -= (double)mub * (double)lapc;
                 sW += (double)mub * (double)phi(c);
-                sH += (double)__ldg(h + idx) * ((double)__ldg(u1 + idx) - (double)ur);
+                if (h) {   // without h the mobility sums come from the spectral x-pass
+                    sD += (double)gc * (double)div;
+                    sH += (double)__ldg(h + idx) * ((double)__ldg(u1 + idx) - (double)ur);
+                }
             }
         }
     };
@@ -219,6 +224,35 @@ __global__ void ch_grad_reduce_kernel(const double* __restrict__ part, int nblk,
     }
 }
 
+// Same, with the two mobility sums from the x-pass partials (xpart: t1 =
+// <lam', u'-u>, t2 = <K lam', u'-u> per block) instead of part's slots 0 and 3.
+__global__ void ch_grad_reduce_spec_kernel(const double* __restrict__ part, int nblk, const double* __restrict__ xpart,
+                                           int nxblk, double* __restrict__ grads, double kA, double DA, double invD) {
+    __shared__ double s[4][256];
+    const int t = threadIdx.x;
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = t; b < nblk; b += 256) {
+        a[0] += part[(size_t)b * 4 + 1];
+        a[1] += part[(size_t)b * 4 + 2];
+    }
+    for (int b = t; b < nxblk; b += 256) {
+        a[2] += xpart[(size_t)b * 2];
+        a[3] += xpart[(size_t)b * 2 + 1];
+    }
+    for (int q = 0; q < 4; ++q) s[q][t] = a[q];
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o)
+            for (int q = 0; q < 4; ++q) s[q][t] += s[q][t + o];
+        __syncthreads();
+    }
+    if (t == 0) {
+        grads[0] += s[2][0] * invD - kA * s[3][0];
+        grads[1] += s[0][0] - DA * s[3][0];
+        grads[2] += s[1][0];
+    }
+}
+
 int elementwise_grid(size_t n) {
     size_t b = (n + 255) / 256;
     return (int)std::min<size_t>(b, (size_t)152 * 16);
@@ -234,6 +268,12 @@ extern "C" {
 
 int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps, const float* lam_in, float* lam_out,
                    const evx_ch_params* prm, double* grads, void* workspace, void* stream) {
+    return evx_ch_adjoint_spectra(plan, states, nullptr, nsteps, lam_in, lam_out, prm, grads, workspace, stream);
+}
+
+int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* spectra, int nsteps,
+                           const float* lam_in, float* lam_out, const evx_ch_params* prm, double* grads,
+                           void* workspace, void* stream) {
     if (!plan) return fail(EVX_ERR_BAD_ARG, "plan is NULL");
     int rc = ch_validate_params(prm);
     if (rc) return rc;
@@ -243,13 +283,18 @@ int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps, const flo
     if ((reinterpret_cast<uintptr_t>(lam_in) | reinterpret_cast<uintptr_t>(lam_out)) & 15)
         return fail(EVX_ERR_BAD_ARG, "lam_in and lam_out must be 16-byte aligned");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
+    const bool want = grads != nullptr;
+    const bool spectral = want && spectra != nullptr;
+    if (spectral) {
+        if (!plan->spec_floats) return fail(EVX_ERR_UNSUPPORTED, "stored spectra need an x-pass plan (power-of-two nx)");
+        if (reinterpret_cast<uintptr_t>(spectra) & 15) return fail(EVX_ERR_BAD_ARG, "spectra must be 16-byte aligned");
+    }
     cudaStream_t st = as_stream(stream);
     const size_t N = plan->n;
     if (nsteps == 0)
         return check_cuda(cudaMemcpyAsync(lam_out, lam_in, N * sizeof(float), cudaMemcpyDeviceToDevice, st),
                           "evx_ch_adjoint copy");
-    const bool want = grads != nullptr;
-    if ((rc = ch_plan_bind(plan, workspace, st, want))) return rc;
+    if ((rc = ch_plan_bind(plan, workspace, st, want && !spectral))) return rc;
     const evx_grid* g = &plan->g;
     const Geo G = make_geo(g, nullptr);
     const ChP P = make_chp(prm);
@@ -259,18 +304,27 @@ int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps, const flo
     float2* spec_h = spec + plan->nspec;
     float* lbuf = reinterpret_cast<float*>(ws_at(workspace, plan->off_lam));
     double* part = reinterpret_cast<double*>(ws_at(workspace, plan->off_part));
+    double* xpart = reinterpret_cast<double*>(ws_at(workspace, plan->off_xpart));
     const float invN = (float)(1.0 / (double)N);
     dim3 sg; int lx;
     ch_stencil_grid(g, &sg, &lx);
-    const double kA = (double)prm->kappa * prm->A, DA = (double)prm->D * prm->A;
+    const double kA = (double)prm->kappa * prm->A, DA = (double)prm->D * prm->A, invD = 1.0 / (double)prm->D;
+    const int gmode = spectral ? 2 : (want ? 1 : 0);
     const float* lam = lam_in;
     for (int s = nsteps - 1; s >= 0; --s) {
         float* dst = (s % 2 == 0) ? lam_out : lbuf;
+        int nxp = 0;   // x-pass partial-sum slots of this step
         if ((rc = ch_r2c(plan, lam, spec, st))) return rc;
         if (plan->xmode) {
-            if ((rc = xpass_launch(want ? 2 : 1, g->nx, spec, want ? spec_h : nullptr, g->ny * plan->nzh, plan->nzh,
-                                   plan->kx2, plan->ky2, plan->kz2, P.sym_coef, P.dt, invN, st)))
-                return rc;
+            XpassArgs a = xpass_args(plan, spectral ? 3 : (want ? 2 : 1), spec, P);
+            if (spectral) {
+                a.dspec = const_cast<float2*>(reinterpret_cast<const float2*>(spectra + (size_t)s * plan->spec_floats));
+                a.xpart = xpart;
+                a.n_xpart_out = &nxp;
+            } else if (want) {
+                a.spec_h = spec_h;
+            }
+            if ((rc = xpass_launch(a, st))) return rc;
         } else {
             EVX_TIMED("ch_kspace_adj", st, ch_kspace_adj_kernel<<<elementwise_grid(plan->nspec), 256, 0, st>>>(
                 spec, want ? spec_h : nullptr, g->ny, plan->nzh, plan->nspec, plan->kx2, plan->ky2, plan->kz2,
@@ -278,32 +332,35 @@ int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps, const flo
             count_launch();
             if ((rc = check_launch("ch_kspace_adj_kernel"))) return rc;
         }
-        if ((rc = ch_c2r(plan, spec, gbuf, want, st))) return rc;
+        if ((rc = ch_c2r(plan, spec, gbuf, want && !spectral, st))) return rc;
         const float* us = states + (size_t)s * N;
-        if (fast_ok(g, {us, gbuf, lam, hbuf, us + N, dst})) {
-            int nb = 0;
-            if ((rc = ch_pullback_fast_launch(want, us, gbuf, lam, hbuf, us + N, dst, part, plan->n_part, g, G, P, st,
-                                              &nb)))
+        const float* hb = gmode == 1 ? hbuf : nullptr;
+        const float* u1 = gmode == 1 ? us + N : nullptr;
+        int nb = (int)(sg.x * sg.y * sg.z);   // generic kernel's partial sums; the fast launcher sets its own
+        if (fast_ok(g, {us, gbuf, lam, hb, u1, dst})) {
+            if ((rc = ch_pullback_fast_launch(gmode, us, gbuf, lam, hb, u1, dst, part, plan->n_part, g, G, P, st, &nb)))
                 return rc;
-            if (want) {
-                EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_kernel<<<1, 256, 0, st>>>(part, nb, grads, kA, DA));
-                count_launch();
-                if ((rc = check_launch("ch_grad_reduce_kernel"))) return rc;
-            }
         } else if (want) {
             EVX_TIMED("ch_pullback_grads", st,
-                      ch_pullback_kernel<true><<<sg, dim3(32, 8), 0, st>>>(us, gbuf, lam, hbuf, us + N, dst, part, G, P, lx));
+                      ch_pullback_kernel<true><<<sg, dim3(32, 8), 0, st>>>(us, gbuf, lam, hb, u1, dst, part, G, P, lx));
             count_launch();
             if ((rc = check_launch("ch_pullback_kernel"))) return rc;
-            EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_kernel<<<1, 256, 0, st>>>(part, plan->n_part, grads, kA, DA));
-            count_launch();
-            if ((rc = check_launch("ch_grad_reduce_kernel"))) return rc;
         } else {
             EVX_TIMED("ch_pullback", st,
                       ch_pullback_kernel<false><<<sg, dim3(32, 8), 0, st>>>(us, gbuf, lam, nullptr, nullptr, dst, nullptr,
                                                                              G, P, lx));
             count_launch();
             if ((rc = check_launch("ch_pullback_kernel"))) return rc;
+        }
+        if (spectral) {
+            EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_spec_kernel<<<1, 256, 0, st>>>(
+                part, nb, xpart, nxp, grads, kA, DA, invD));
+            count_launch();
+            if ((rc = check_launch("ch_grad_reduce_spec_kernel"))) return rc;
+        } else if (want) {
+            EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_kernel<<<1, 256, 0, st>>>(part, nb, grads, kA, DA));
+            count_launch();
+            if ((rc = check_launch("ch_grad_reduce_kernel"))) return rc;
         }
         lam = dst;
     }

@@ -266,11 +266,14 @@ int ch_c2r(evx_ch_plan* plan, float2* in, float* out, bool batch2, cudaStream_t 
     return check_cufft(r, "cufftExecC2R");
 }
 
-int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st) {
+int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st, float2* dspec) {
     const float invN = (float)(1.0 / (double)plan->n);
-    if (plan->xmode)
-        return xpass_launch(0, plan->g.nx, spec, nullptr, plan->g.ny * plan->nzh, plan->nzh, plan->kx2, plan->ky2,
-                            plan->kz2, P.sym_coef, P.dt, invN, st);
+    if (plan->xmode) {
+        XpassArgs a = xpass_args(plan, 0, spec, P);
+        a.dspec = dspec;
+        return xpass_launch(a, st);
+    }
+    if (dspec) return fail(EVX_ERR_UNSUPPORTED, "stored spectra need an x-pass plan");
     EVX_TIMED("ch_kspace_fwd", st, ch_kspace_fwd_kernel<<<elementwise_grid(plan->nspec), 256, 0, st>>>(
         spec, plan->g.ny, plan->nzh, plan->nspec, plan->kx2, plan->ky2, plan->kz2, P.sym_coef, P.dt, invN));
     count_launch();
@@ -403,6 +406,9 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
     p->off_u = off;    off += align256(p->n * sizeof(float));
     p->off_lam = off;  off += align256(p->n * sizeof(float));
     p->off_part = off; off += align256((size_t)p->n_part * 4 * sizeof(double));
+    p->n_xpart = p->xmode ? xpass_blocks(g->nx, g->ny * p->nzh) : 0;
+    p->spec_floats = p->xmode ? xpass_spectrum_floats(g->nx, g->ny * p->nzh) : 0;
+    p->off_xpart = off; off += align256(p->n_xpart * 2 * sizeof(double));
     p->total = off;
     *out = p;
     return EVX_OK;
@@ -420,14 +426,25 @@ int evx_ch_plan_destroy(evx_ch_plan* p) {
 
 size_t evx_ch_workspace_bytes(const evx_ch_plan* p) { return p ? p->total : 0; }
 
+size_t evx_ch_spectrum_floats(const evx_ch_plan* p) { return p ? p->spec_floats : 0; }
+
 int evx_ch_forward(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps, float* traj,
                    const evx_ch_params* prm, int* nonfinite, void* workspace, void* stream) {
+    return evx_ch_forward_spectra(plan, u_in, u_out, nsteps, traj, nullptr, prm, nonfinite, workspace, stream);
+}
+
+int evx_ch_forward_spectra(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps, float* traj,
+                           float* spectra, const evx_ch_params* prm, int* nonfinite, void* workspace, void* stream) {
     if (!plan) return fail(EVX_ERR_BAD_ARG, "plan is NULL");
     int rc = ch_validate_params(prm);
     if (rc) return rc;
     if (!u_in || !u_out) return fail(EVX_ERR_BAD_ARG, "NULL field pointer");
     if (u_in == u_out) return fail(EVX_ERR_BAD_ARG, "input and output must not alias");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
+    if (spectra) {
+        if (!plan->spec_floats) return fail(EVX_ERR_UNSUPPORTED, "stored spectra need an x-pass plan (power-of-two nx)");
+        if (reinterpret_cast<uintptr_t>(spectra) & 15) return fail(EVX_ERR_BAD_ARG, "spectra must be 16-byte aligned");
+    }
     cudaStream_t st = as_stream(stream);
     const size_t N = plan->n;
     if (nsteps == 0)
@@ -452,7 +469,8 @@ int evx_ch_forward(evx_ch_plan* plan, const float* u_in, float* u_out, int nstep
         }
         if (rc) return rc;
         if ((rc = ch_r2c(plan, r, spec, st))) return rc;
-        if ((rc = ch_kspace_forward(plan, spec, P, st))) return rc;
+        float2* ds = spectra ? reinterpret_cast<float2*>(spectra + (size_t)s * plan->spec_floats) : nullptr;
+        if ((rc = ch_kspace_forward(plan, spec, P, st, ds))) return rc;
         if ((rc = ch_c2r(plan, spec, upd, false, st))) return rc;
     }
     EVX_TIMED("ch_axpy", st, ch_axpy_kernel<<<elementwise_grid(N / 4 + 1), 256, 0, st>>>(

@@ -108,7 +108,8 @@ int ch_tile_variant(int nz);   // honours evx_set_tile_variant
 
 int ch_rhs_fast_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
                        const Geo& G, const ChP& P, cudaStream_t st);
-int ch_pullback_fast_launch(bool grads, const float* u, const float* g, const float* lam, const float* h,
+// grads: 0 none, 1 all four partial sums (reads h and u1), 2 the two real-space sums only
+int ch_pullback_fast_launch(int grads, const float* u, const float* g, const float* lam, const float* h,
                             const float* u1, float* lam_out, double* part, int n_part_cap, const evx_grid* grid,
                             const Geo& G, const ChP& P, cudaStream_t st, int* n_part_used);
 int ch_pullback_fast_blocks(const evx_grid* g);

@@ -8,7 +8,9 @@
 // on plane i+1 over the tile grown by one cell (2-slot rings); then lam on
 // plane i.  x faces, the previous plane's c and mub at the patch points are
 // carried in registers.  Optional parameter-gradient partial sums are kept in
-// float per thread and reduced in double per block.
+// float per thread and reduced in double per block: GR = 1 all four sums
+// (<lam',u'-u>/D, -<mub,Lc>, <mub,phi(c)>, <h,u'-u>), GR = 2 only the two that
+// need real space (the mobility sums then come from the spectral x-pass).
 // Compiled with FMA contraction on: no bitwise-parity requirement here.
 #include <algorithm>
 #include <type_traits>
@@ -69,13 +71,14 @@ __device__ __forceinline__ void block_reduce4(float a, float b, float c, float d
     }
 }
 
-template <class T, bool GRADS>
+template <class T, int GR>
 __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const float* __restrict__ gfield,
                                               const float* __restrict__ lam, const float* __restrict__ hfield,
                                               const float* __restrict__ u1, float* __restrict__ lam_out,
                                               const Geo& G, const ChP& P, int k0, int j0, int x0, int x1,
                                               float* cs, float* gs, float* ms, float* bs,
                                               float& sD, float& sK, float& sW, float& sH) {
+    constexpr bool GRADS = GR != 0;
     const int tid = threadIdx.x;
     const int tx = tid % T::BX, ty = tid / T::BX;
     const int W = T::W;
@@ -306,21 +309,27 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
                 lap_f(G, A.y, c_prev[1], cxA.y, up.y, B.y, A.x, cc[pa + 2]),
                 lap_f(G, B.x, c_prev[2], cxB.x, A.x, dn.x, cc[pb - 1], B.y),
                 lap_f(G, B.y, c_prev[3], cxB.y, A.y, dn.y, B.x, cc[pb + 2])};
-            const float2 h0 = wj0 ? __ldg(reinterpret_cast<const float2*>(hfield + o)) : make_float2(0.f, 0.f);
-            const float2 h1 = wj1 ? __ldg(reinterpret_cast<const float2*>(hfield + o + nz)) : make_float2(0.f, 0.f);
-            const float2 n0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u1 + o)) : make_float2(0.f, 0.f);
-            const float2 n1 = wj1 ? __ldg(reinterpret_cast<const float2*>(u1 + o + nz)) : make_float2(0.f, 0.f);
-            const float hv[4] = {h0.x, h0.y, h1.x, h1.y}, nv[4] = {n0.x, n0.y, n1.x, n1.y};
             const bool okp[4] = {wj0, wj0, wj1, wj1};
+            if (GR == 1) {
+                const float2 h0 = wj0 ? __ldg(reinterpret_cast<const float2*>(hfield + o)) : make_float2(0.f, 0.f);
+                const float2 h1 = wj1 ? __ldg(reinterpret_cast<const float2*>(hfield + o + nz)) : make_float2(0.f, 0.f);
+                const float2 n0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u1 + o)) : make_float2(0.f, 0.f);
+                const float2 n1 = wj1 ? __ldg(reinterpret_cast<const float2*>(u1 + o + nz)) : make_float2(0.f, 0.f);
+                const float hv[4] = {h0.x, h0.y, h1.x, h1.y}, nv[4] = {n0.x, n0.y, n1.x, n1.y};
+                const float invD = 1.f / P.D;
 #pragma unroll
-            const float invD = 1.f / P.D;
+                for (int q = 0; q < 4; ++q) {
+                    if (!okp[q]) continue;
+                    // <g, r/D> = <P lam', r>/D = <lam', u' - u>/D  (P is symmetric)
+                    sD += lv[q] * (nv[q] - ur[q]) * invD;
+                    sH += hv[q] * (nv[q] - ur[q]);
+                }
+            }
+#pragma unroll
             for (int q = 0; q < 4; ++q) {
                 if (!okp[q]) continue;
-                // <g, r/D> = <P lam', r>/D = <lam', u' - u>/D  (P is symmetric)
-                sD += lv[q] * (nv[q] - ur[q]) * invD;
                 sK -= bpt[q] * lc[q];
                 sW += bpt[q] * phi_c(cpt[q]);
-                sH += hv[q] * (nv[q] - ur[q]);
             }
         }
 #pragma unroll
@@ -363,8 +372,8 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
 
 }
 
-template <class T, bool GRADS>
-__global__ void __launch_bounds__(THREADS, GRADS ? 2 : 3)
+template <class T, int GR>
+__global__ void __launch_bounds__(THREADS, GR ? 2 : 3)
 ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ gfield, const float* __restrict__ lam,
                         const float* __restrict__ hfield, const float* __restrict__ u1, float* __restrict__ lam_out,
                         double* __restrict__ part, Geo G, ChP P, int LX) {
@@ -378,9 +387,9 @@ ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ g
     const int x1 = min(x0 + LX, G.nx);
     float sD = 0.f, sK = 0.f, sW = 0.f, sH = 0.f;
     if (x0 < x1)
-        pullback_tile<T, GRADS>(u, gfield, lam, hfield, u1, lam_out, G, P, blockIdx.x * T::TZ, blockIdx.y * T::TY, x0,
-                                x1, cs, gs, ms, bs, sD, sK, sW, sH);
-    if (GRADS) {
+        pullback_tile<T, GR>(u, gfield, lam, hfield, u1, lam_out, G, P, blockIdx.x * T::TZ, blockIdx.y * T::TY, x0,
+                             x1, cs, gs, ms, bs, sD, sK, sW, sH);
+    if (GR) {
         const size_t blk = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
         block_reduce4(sD, sK, sW, sH, red, part + blk * 4);
     }
@@ -426,11 +435,11 @@ ch_pullback_batch_kernel(const float* __restrict__ u, const float* __restrict__ 
         const size_t o = (size_t)B.off;
         float sD = 0.f, sK = 0.f, sW = 0.f, sH = 0.f;
         if (B.tile == 0)
-            pullback_tile<TileWide, GRADS>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
+            pullback_tile<TileWide, GRADS ? 1 : 0>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
                                            GRADS ? u1 + o : nullptr, lam_out + o, G, B.P, I.k0, I.j0, I.x0, I.x1, cs,
                                            gs, ms, bs, sD, sK, sW, sH);
         else
-            pullback_tile<TileSquare, GRADS>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
+            pullback_tile<TileSquare, GRADS ? 1 : 0>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
                                              GRADS ? u1 + o : nullptr, lam_out + o, G, B.P, I.k0, I.j0, I.x0, I.x1,
                                              cs, gs, ms, bs, sD, sK, sW, sH);
         if (GRADS) block_reduce4(sD, sK, sW, sH, red, part + (size_t)I.part * 4);
@@ -438,7 +447,7 @@ ch_pullback_batch_kernel(const float* __restrict__ u, const float* __restrict__ 
     }
 }
 
-int g_bps[2][2] = {{0, 0}, {0, 0}};   // [tile variant][gradients]
+int g_bps[2][3] = {{0, 0, 0}, {0, 0, 0}};   // [tile variant][gradient mode]
 int g_batch_bps[2] = {0, 0};
 int g_sms = 0;
 
@@ -452,22 +461,24 @@ void init_occupancy() {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, THREADS, ADJ_SMEM);
         if (*out < 1) *out = 1;
     };
-    setup(ch_pullback_fast_kernel<TileWide, false>, &g_bps[0][0]);
-    setup(ch_pullback_fast_kernel<TileWide, true>, &g_bps[0][1]);
-    setup(ch_pullback_fast_kernel<TileSquare, false>, &g_bps[1][0]);
-    setup(ch_pullback_fast_kernel<TileSquare, true>, &g_bps[1][1]);
+    setup(ch_pullback_fast_kernel<TileWide, 0>, &g_bps[0][0]);
+    setup(ch_pullback_fast_kernel<TileWide, 1>, &g_bps[0][1]);
+    setup(ch_pullback_fast_kernel<TileWide, 2>, &g_bps[0][2]);
+    setup(ch_pullback_fast_kernel<TileSquare, 0>, &g_bps[1][0]);
+    setup(ch_pullback_fast_kernel<TileSquare, 1>, &g_bps[1][1]);
+    setup(ch_pullback_fast_kernel<TileSquare, 2>, &g_bps[1][2]);
     setup(ch_pullback_batch_kernel<false>, &g_batch_bps[0]);
     setup(ch_pullback_batch_kernel<true>, &g_batch_bps[1]);
 }
 
 template <class T>
-dim3 pb_grid(const evx_grid* g, bool grads, int* lx) {
+dim3 pb_grid(const evx_grid* g, int grads, int* lx) {
     const int v = std::is_same<T, TileWide>::value ? 0 : 1;
-    return fast_grid<T>(g->nx, g->ny, g->nz, g_bps[v][grads ? 1 : 0], g_sms, lx);
+    return fast_grid<T>(g->nx, g->ny, g->nz, g_bps[v][grads], g_sms, lx);
 }
 
 template <class T>
-int pb_launch_t(bool grads, const float* u, const float* g, const float* lam, const float* h, const float* u1,
+int pb_launch_t(int grads, const float* u, const float* g, const float* lam, const float* h, const float* u1,
                 float* lam_out, double* part, int n_part_cap, const evx_grid* grid_, const Geo& G, const ChP& P,
                 cudaStream_t st, int* n_part_used) {
     int lx;
@@ -475,13 +486,17 @@ int pb_launch_t(bool grads, const float* u, const float* g, const float* lam, co
     const int nb = (int)(grid.x * grid.y * grid.z);
     if (grads && nb > n_part_cap) return fail(EVX_ERR_WORKSPACE, "partial-sum buffer too small (%d > %d)", nb, n_part_cap);
     if (n_part_used) *n_part_used = nb;
-    if (grads)
+    if (grads == 1)
         EVX_TIMED("ch_pullback_grads", st,
-                  ch_pullback_fast_kernel<T, true><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, lx));
+                  ch_pullback_fast_kernel<T, 1><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, lx));
+    else if (grads == 2)
+        EVX_TIMED("ch_pullback_grads_spec", st,
+                  ch_pullback_fast_kernel<T, 2><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out, part,
+                                                                                 G, P, lx));
     else
         EVX_TIMED("ch_pullback", st,
-                  ch_pullback_fast_kernel<T, false><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
-                                                                                     nullptr, G, P, lx));
+                  ch_pullback_fast_kernel<T, 0><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
+                                                                                 nullptr, G, P, lx));
     count_launch();
     return check_launch("ch_pullback_fast_kernel");
 }
@@ -491,14 +506,14 @@ int pb_launch_t(bool grads, const float* u, const float* g, const float* lam, co
 int ch_pullback_fast_blocks(const evx_grid* g) {
     init_occupancy();
     int lx, most = 0;
-    for (bool grads : {false, true}) {
+    for (int grads : {0, 1, 2}) {
         dim3 a = pb_grid<TileWide>(g, grads, &lx), b = pb_grid<TileSquare>(g, grads, &lx);
         most = std::max(most, (int)std::max(a.x * a.y * a.z, b.x * b.y * b.z));
     }
     return most;
 }
 
-int ch_pullback_fast_launch(bool grads, const float* u, const float* g, const float* lam, const float* h,
+int ch_pullback_fast_launch(int grads, const float* u, const float* g, const float* lam, const float* h,
                             const float* u1, float* lam_out, double* part, int n_part_cap, const evx_grid* grid_,
                             const Geo& G, const ChP& P, cudaStream_t st, int* n_part_used) {
     init_occupancy();

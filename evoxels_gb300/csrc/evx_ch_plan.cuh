@@ -19,8 +19,10 @@ struct evx_ch_plan {
     float* ky2 = nullptr;
     float* kz2 = nullptr;
     // workspace layout (byte offsets)
-    size_t off_fft, off_r, off_upd, off_spec, off_u, off_lam, off_part, total;
+    size_t off_fft, off_r, off_upd, off_spec, off_u, off_lam, off_part, off_xpart, total;
     int n_part;              // capacity of the partial-sum array (blocks)
+    size_t n_xpart;          // x-pass blocks (Parseval partial sums, 2 doubles each); 0 without x-pass
+    size_t spec_floats;      // floats per stored increment spectrum; 0 without x-pass
 };
 
 namespace evx {
@@ -54,14 +56,35 @@ __device__ __forceinline__ float imex_prefac(float k2, float sym_coef, float dt)
     return __fmul_rn(__frcp_rn(den), dt);
 }
 
-// Forward k-space multiply: spec *= prefac(k) then * invN (in that order).
-int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st);
+// Forward k-space multiply: spec *= prefac(k) then * invN (in that order);
+// with dspec (x-pass plans only) the product is also stored there.
+int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st, float2* dspec = nullptr);
 
-// Fused spectral x-pass (evx_fftx.cu): mode 0 forward multiply, 1 adjoint g,
-// 2 adjoint g and h (h into spec_h).
+// Fused spectral x-pass (evx_fftx.cu): mode 0 forward multiply (and optional
+// store of the increment spectrum into dspec), 1 adjoint g, 2 adjoint g and h
+// (h into spec_h), 3 adjoint g plus Parseval sums against dspec into xpart.
+struct XpassArgs {
+    int mode, nx, M, nzh, nz;          // M = ny*nzh pencils
+    float2* spec;
+    float2* spec_h;
+    float2* dspec;
+    double* xpart;
+    const float *kx2, *ky2, *kz2;
+    float sym, dt, invN;
+    int* n_xpart_out;                  // optional: partial-sum slots written (mode 3)
+};
 bool xpass_supported(int nx);
-int xpass_launch(int mode, int nx, float2* spec, float2* spec_h, int M, int nzh, const float* kx2, const float* ky2,
-                 const float* kz2, float sym, float dt, float invN, cudaStream_t st);
+size_t xpass_blocks(int nx, int M);
+size_t xpass_spectrum_floats(int nx, int M);
+int xpass_launch(const XpassArgs& a, cudaStream_t st);
+inline XpassArgs xpass_args(const evx_ch_plan* plan, int mode, float2* spec, const ChP& P) {
+    XpassArgs a{};
+    a.mode = mode; a.nx = plan->g.nx; a.M = plan->g.ny * plan->nzh; a.nzh = plan->nzh; a.nz = plan->g.nz;
+    a.spec = spec;
+    a.kx2 = plan->kx2; a.ky2 = plan->ky2; a.kz2 = plan->kz2;
+    a.sym = P.sym_coef; a.dt = P.dt; a.invN = (float)(1.0 / (double)plan->n);
+    return a;
+}
 
 // Tile shape shared by the rhs and pullback stencil kernels.
 constexpr int CH_TZ = 32;           // tile extent along z (= warp width)

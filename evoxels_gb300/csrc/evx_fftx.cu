@@ -5,8 +5,9 @@
 //
 // Layout: spec[x][ky][kz] complex (cuFFT's 2-D R2C over (y, z), batched over
 // x), so pencil m = ky*nzh + kz is contiguous across m at fixed x and element
-// x sits at spec[x*M + m] (M = ny*nzh).  A block of 256 threads owns P = 256/N2
-// consecutive pencils; pencil p is handled by N2 threads (N = N1*N2 along x).
+// x sits at spec[x*M + m] (M = ny*nzh).  A tile of P = 256/N2 consecutive
+// pencils x all nx rows is owned by one block of 256 threads; pencil p is
+// handled by N2 threads (N = N1*N2 along x).
 //
 // Four-step FFT with N = N1*N2, n = N2*n1 + n2, k = k1 + N1*k2:
 //   forward  A[k1][n2]     = W_N^{n2 k1} * DFT_N1(x[N2 n1 + n2])[k1]     thread n2, registers
@@ -14,16 +15,42 @@
 //   inverse  B[k1][n2]     = W_N^{-n2 k1} * IDFT_N2(X[k1 + N1 .])[n2]   the thread holding X
 //            y[N2 n1 + n2] = IDFT_N1(B[.][n2])[n1]                     after a shared exchange
 // The frequency data never needs natural order, so there is no bit-reversal
-// pass, and every thread writes back exactly the elements it loaded.  Roots
-// of unity come from a table of W_512^j computed on the host in double
-// precision.  The transforms are compiled with FMA contraction (no bitwise
-// requirement; cuFFT rounds differently anyway); the forward multiplier uses
-// explicit round-to-nearest operations as the k-space kernels do.
+// pass, and every thread writes back exactly the elements it loaded.  The
+// in-register DFTs use twiddles fixed at compile time (cos/sin of 2*pi*j/L
+// evaluated by Taylor series in double, so multiplications by 1, -1 and +-i
+// vanish); the inter-stage twiddles W_N^{n2 k1} depend on the thread and come
+// from a table of W_512^j computed on the host in double precision.  The
+// transforms are compiled with FMA contraction (no bitwise requirement; cuFFT
+// rounds differently anyway); the forward multiplier uses explicit
+// round-to-nearest operations as the k-space kernels do.
 // Multipliers (same float32 expressions as the k-space kernels):
 //   forward  X * prefac(k) * invN                    (evoxels/timesteppers.py:77,87)
 //   adjoint  X * (prefac*invN), and X * (prefac*invN*k^4) into a second spectrum
+//
+// Stored increment spectra.  The forward pass can also write the multiplied
+// spectrum dU(k) = prefac*invN*R(k) (whose inverse transform is u_{s+1} - u_s)
+// in the kernel's own register order, [tile][element][thread], so that the
+// adjoint pass of the same step reads it back coalesced at the same positions.
+// With it the adjoint forms the two mobility sums by Parseval over the half
+// spectrum (weight 1 on the kz = 0 and kz = nz/2 planes, 2 elsewhere):
+//   <lam', u_{s+1} - u_s>   = sum_k wz Re(L(k) conj dU(k))
+//   <K lam', u_{s+1} - u_s> = sum_k wz prefac k^4 Re(L(k) conj dU(k))
+// with L = R2C(lam') unnormalised; per-block partial sums go out in double.
+//
+// Two kernels share this math.  The pipelined one (even M >= 256, modes 0, 1
+// and 3) is persistent: a 3-slot ring of tiles in shared memory is filled by
+// TMA tensor loads (cp.async.bulk.tensor, one thread, mbarrier completion)
+// one tile ahead of the compute, and results leave by TMA tensor stores from
+// the same slot, so the load of tile i+1 and the store of tile i-1 overlap the
+// transforms of tile i.  The per-tile kernel (any M, all modes) loads and
+// stores with plain coalesced accesses.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
+#include <type_traits>
 
 #include "evx_ch_plan.cuh"
 
@@ -31,9 +58,7 @@ namespace evx {
 namespace {
 
 __constant__ float2 c_w512[512];   // (cos, -sin)(2*pi*j/512): forward roots of unity
-
-std::once_flag g_tw_once;
-int g_tw_rc = EVX_OK;
+__device__ int g_dev_status;       // bit 0: an x-pass barrier wait gave up
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -46,6 +71,59 @@ template <bool INV>
 __device__ __forceinline__ float2 w512(int j) {
     const float2 w = c_w512[j & 511];
     return INV ? make_float2(w.x, -w.y) : w;
+}
+
+// ---- compile-time twiddles ----------------------------------------------------
+constexpr double kPi = 3.141592653589793238462643383279502884;
+// Taylor series on [-pi, pi]; 16 terms leave an error below 1e-18
+__host__ __device__ constexpr double cx_sin(double x) {
+    double t = x, s = x;
+    for (int k = 1; k < 16; ++k) {
+        t *= -x * x / ((2.0 * k) * (2.0 * k + 1.0));
+        s += t;
+    }
+    return s;
+}
+__host__ __device__ constexpr double cx_cos(double x) {
+    double t = 1.0, s = 1.0;
+    for (int k = 1; k < 16; ++k) {
+        t *= -x * x / ((2.0 * k - 1.0) * (2.0 * k));
+        s += t;
+    }
+    return s;
+}
+// 2*pi*j/L reduced to [-pi, pi]
+__host__ __device__ constexpr double cx_angle(int j, int L) {
+    j %= L;
+    if (2 * j > L) j -= L;
+    return 2.0 * kPi * (double)j / (double)L;
+}
+
+// a * W_L^J (forward, W = exp(-2*pi*i/L)) or a * conj(W_L^J) (inverse)
+template <int J, int L, bool INV>
+__device__ __forceinline__ float2 twiddle(float2 a) {
+    constexpr int j = J % L;
+    if constexpr (j == 0) {
+        return a;
+    } else if constexpr (2 * j == L) {
+        return make_float2(-a.x, -a.y);
+    } else if constexpr (4 * j == L) {        // forward -i, inverse +i
+        return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+    } else if constexpr (4 * j == 3 * L) {    // forward +i, inverse -i
+        return INV ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+    } else {
+        constexpr float c = (float)cx_cos(cx_angle(j, L));
+        constexpr float s = (float)(INV ? cx_sin(cx_angle(j, L)) : -cx_sin(cx_angle(j, L)));
+        return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+    }
+}
+
+template <int B, int E, int S = 1, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + S, E, S>(f);
+    }
 }
 
 template <int L>
@@ -72,144 +150,426 @@ __device__ __forceinline__ void dft(float2 (&v)[L]) {
             v[j] = t;
         }
     }
-#pragma unroll
-    for (int len = 2; len <= L; len <<= 1) {
-#pragma unroll
-        for (int i = 0; i < L; i += len) {
-#pragma unroll
-            for (int k = 0; k < len / 2; ++k) {
-                const float2 w = w512<INV>(k * (512 / len));
-                const float2 a = v[i + k], b = cmul(v[i + k + len / 2], w);
-                v[i + k] = cadd(a, b);
-                v[i + k + len / 2] = csub(a, b);
-            }
+    static_for<1, 6>([&](auto S) {
+        constexpr int len = 1 << decltype(S)::value;
+        if constexpr (len <= L) {
+            static_for<0, L, len>([&](auto I) {
+                static_for<0, len / 2>([&](auto K) {
+                    constexpr int i = decltype(I)::value, k = decltype(K)::value;
+                    const float2 a = v[i + k], b = twiddle<k, len, INV>(v[i + k + len / 2]);
+                    v[i + k] = cadd(a, b);
+                    v[i + k + len / 2] = csub(a, b);
+                });
+            });
         }
-    }
+    });
 }
 
 #ifndef EVX_XPASS_MIN_BLOCKS
 #define EVX_XPASS_MIN_BLOCKS 2   // resident blocks per SM the register budget is sized for
 #endif
 
-template <int N1, int N2, int MODE>   // MODE 0 forward, 1 adjoint (g), 2 adjoint (g and h)
-__global__ void __launch_bounds__(256, MODE == 2 ? 2 : EVX_XPASS_MIN_BLOCKS)
-xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, int M, int nzh,
-             const float* __restrict__ kx2, const float* __restrict__ ky2, const float* __restrict__ kz2,
-             float sym_coef, float dt, float invN) {
-    constexpr int N = N1 * N2;
-    constexpr int P = 256 / N2;          // pencils per block
-    constexpr int Q = N1 / N2;           // k1 values per thread between the exchanges
+// Per-thread context of one pencil column.
+template <int N1, int N2>
+struct Col {
+    static constexpr int N = N1 * N2, P = 256 / N2, Q = N1 / N2;
     static_assert(N1 >= N2 && N1 % N2 == 0 && 256 % N2 == 0, "unsupported split");
-    extern __shared__ float2 xs[];       // [N1][N2][P], pencil index fastest (conflict-free)
-    const int tid = threadIdx.x;
-    const int p = tid % P, n2 = tid / P;
-    const int m = blockIdx.x * P + p;
-    const bool live = m < M;
-    const int mc = live ? m : 0;
-    const int ky = mc / nzh, kz = mc - ky * nzh;
-    const float ky2v = __ldg(ky2 + ky), kz2v = __ldg(kz2 + kz);
-    auto at = [&](int k1, int j) -> float2& { return xs[(k1 * N2 + j) * P + p]; };
+    int p, n2;
+    __device__ __forceinline__ int xi(int k1, int j) const { return (k1 * N2 + j) * P + p; }   // [N1][N2][P]
+};
 
-    // ---- forward stage 1: load the thread's column, DFT over n1, twiddle
-    float2 v[N1];
-#pragma unroll
-    for (int n1 = 0; n1 < N1; ++n1)
-        v[n1] = live ? spec[(size_t)(N2 * n1 + n2) * M + m] : make_float2(0.f, 0.f);
+// Forward stage 1 on the thread's column v (x = N2*n1 + n2): DFT over n1,
+// twiddle, exchange; afterwards v[q*N2 + j] = A[n2*Q + q][j].  The exchange
+// writes only the addresses the column occupies in a [x][p] tile, so it may
+// alias the tile the column was read from.  The gathered rows are rewritten
+// only by their gathering thread (mid_stage), so no barrier follows.
+template <int N1, int N2>
+__device__ __forceinline__ void fwd_stage1(float2 (&v)[N1], float2* xs, const Col<N1, N2>& c) {
+    constexpr int N = N1 * N2, Q = N1 / N2;
     dft<N1, false>(v);
-    if (N2 > 1) {
+    if constexpr (N2 > 1) {
 #pragma unroll
-        for (int k1 = 0; k1 < N1; ++k1) at(k1, n2) = cmul(v[k1], w512<false>((n2 * k1) * (512 / N)));
+        for (int k1 = 0; k1 < N1; ++k1) xs[c.xi(k1, c.n2)] = cmul(v[k1], w512<false>((c.n2 * k1) * (512 / N)));
         __syncthreads();
 #pragma unroll
         for (int q = 0; q < Q; ++q)
 #pragma unroll
-            for (int j = 0; j < N2; ++j) v[q * N2 + j] = at(n2 * Q + q, j);   // A[k1][.] for the thread's k1
-        __syncthreads();
+            for (int j = 0; j < N2; ++j) v[q * N2 + j] = xs[c.xi(c.n2 * Q + q, j)];
     }
-    // ---- forward stage 2, multiply, inverse stage 2 (registers); stash B[k1][.]
-    float2 hv[MODE == 2 ? N1 : 1];
+}
+
+// Multiplier stage: forward DFT over k2, multiply, inverse DFT, conjugate
+// twiddle into xs[k1][j] (N2 > 1) or back into v (N2 == 1).  MODE 0 forward
+// (optional store of the product to dsp), 1 adjoint g, 2 adjoint g and h (into
+// hv), 3 adjoint g with the Parseval sums against dsp.  dsp points at the
+// tile's stored spectrum ([element][thread], thread offset included).
+template <int N1, int N2, int MODE>
+__device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 2 ? N1 : 1], float2* xs,
+                                          const Col<N1, N2>& c, float ky2v, float kz2v, float wz,
+                                          const float* __restrict__ kx2, float sym_coef, float dt, float invN,
+                                          float2* __restrict__ dsp, float& t1, float& t2) {
+    constexpr int N = N1 * N2, Q = N1 / N2;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const int k1 = N2 > 1 ? n2 * Q + q : q;
+        const int k1 = N2 > 1 ? c.n2 * Q + q : q;
         float2 a[N2], b[N2];
 #pragma unroll
         for (int j = 0; j < N2; ++j) a[j] = v[N2 > 1 ? q * N2 + j : q];
-        if (N2 > 1) dft<N2, false>(a);
+        if constexpr (N2 > 1) dft<N2, false>(a);
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) {
             const int kx = k1 + N1 * k2;
             const float k2s = __fadd_rn(__fadd_rn(__ldg(kx2 + kx), ky2v), kz2v);
-            if (MODE == 0) {
+            if constexpr (MODE == 0) {
                 const float pre = imex_prefac(k2s, sym_coef, dt);
                 a[k2] = make_float2(__fmul_rn(__fmul_rn(a[k2].x, pre), invN), __fmul_rn(__fmul_rn(a[k2].y, pre), invN));
+                if (dsp) dsp[(q * N2 + k2) * 256] = a[k2];
             } else {
                 const float k4 = k2s * k2s;
-                const float sg = (dt / (1.f - dt * (sym_coef * k4))) * invN;
-                if (MODE == 2) b[k2] = make_float2(a[k2].x * (sg * k4), a[k2].y * (sg * k4));
+                const float pre = dt / (1.f - dt * (sym_coef * k4));
+                const float sg = pre * invN;
+                if constexpr (MODE == 2) b[k2] = make_float2(a[k2].x * (sg * k4), a[k2].y * (sg * k4));
+                if constexpr (MODE == 3) {
+                    const float2 d = dsp[(q * N2 + k2) * 256];
+                    const float re = wz * (a[k2].x * d.x + a[k2].y * d.y);
+                    t1 += re;
+                    t2 += re * (pre * k4);
+                }
                 a[k2] = make_float2(a[k2].x * sg, a[k2].y * sg);
             }
         }
-        if (N2 > 1) {
+        if constexpr (N2 > 1) {
             dft<N2, true>(a);
-            if (MODE == 2) dft<N2, true>(b);
+            if constexpr (MODE == 2) dft<N2, true>(b);
 #pragma unroll
             for (int j = 0; j < N2; ++j) {
-                at(k1, j) = cmul(a[j], w512<true>((j * k1) * (512 / N)));
-                if (MODE == 2) hv[q * N2 + j] = cmul(b[j], w512<true>((j * k1) * (512 / N)));
+                xs[c.xi(k1, j)] = cmul(a[j], w512<true>((j * k1) * (512 / N)));
+                if constexpr (MODE == 2) hv[q * N2 + j] = cmul(b[j], w512<true>((j * k1) * (512 / N)));
             }
         } else {
             v[q] = a[0];
-            if (MODE == 2) hv[q] = b[0];
+            if constexpr (MODE == 2) hv[q] = b[0];
         }
     }
-    // ---- inverse stage 1: gather B[.][n2], IDFT over k1, store
-    auto finish = [&](float2* dst) {
-        if (N2 > 1) {
-            __syncthreads();
+}
+
+// Inverse stage 1: gather B[.][n2] (after a barrier), IDFT over k1; v then
+// holds the output column x = N2*n1 + n2 (same addresses as the gather).
+template <int N1, int N2>
+__device__ __forceinline__ void inv_stage1(float2 (&v)[N1], const float2* xs, const Col<N1, N2>& c) {
+    if constexpr (N2 > 1) {
+        __syncthreads();
 #pragma unroll
-            for (int k1 = 0; k1 < N1; ++k1) v[k1] = at(k1, n2);
-        }
-        dft<N1, true>(v);
+        for (int k1 = 0; k1 < N1; ++k1) v[k1] = xs[c.xi(k1, c.n2)];
+    }
+    dft<N1, true>(v);
+}
+
+__device__ __forceinline__ float kz_weight(int kz, int nz) { return (kz == 0 || 2 * kz == nz) ? 1.f : 2.f; }
+
+// Block sums of (t1, t2) in double, fixed order, into out[0..1].
+__device__ __forceinline__ void block_sum2(float t1, float t2, double* out) {
+    __shared__ double red[2][8];
+    const int tid = threadIdx.x;
+    double d1 = t1, d2 = t2;
+    for (int o = 16; o > 0; o >>= 1) {
+        d1 += __shfl_down_sync(0xffffffffu, d1, o);
+        d2 += __shfl_down_sync(0xffffffffu, d2, o);
+    }
+    if ((tid & 31) == 0) {
+        red[0][tid >> 5] = d1;
+        red[1][tid >> 5] = d2;
+    }
+    __syncthreads();
+    if (tid < 2) {
+        double x = 0.0;
+        for (int w = 0; w < 8; ++w) x += red[tid][w];
+        out[tid] = x;
+    }
+}
+
+// ---- per-tile kernel (plain loads and stores) -------------------------------------
+// MODE 0 forward (dspec: optional store of the increment spectrum), 1 adjoint (g),
+// 2 adjoint (g and h into spec_h), 3 adjoint (g and the two Parseval sums
+// against dspec into xpart[2*block .. 2*block+1])
+template <int N1, int N2, int MODE>
+__global__ void __launch_bounds__(256, MODE == 2 ? 2 : EVX_XPASS_MIN_BLOCKS)
+xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __restrict__ dspec,
+             double* __restrict__ xpart, int M, int nzh, int nz,
+             const float* __restrict__ kx2, const float* __restrict__ ky2, const float* __restrict__ kz2,
+             float sym_coef, float dt, float invN) {
+    using C = Col<N1, N2>;
+    constexpr int P = C::P, Q = C::Q;
+    extern __shared__ float2 xs[];       // [N1][N2][P], pencil index fastest (conflict-free)
+    const int tid = threadIdx.x;
+    const C c{tid % P, tid / P};
+    const int m = blockIdx.x * P + c.p;
+    const bool live = m < M;
+    const int mc = live ? m : 0;
+    const int ky = mc / nzh, kz = mc - ky * nzh;
+    const float ky2v = __ldg(ky2 + ky), kz2v = __ldg(kz2 + kz);
+    float2* dsp = dspec ? dspec + (size_t)blockIdx.x * N1 * 256 + tid : nullptr;
+    float t1 = 0.f, t2 = 0.f;
+
+    float2 v[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1)
+        v[n1] = live ? spec[(size_t)(N2 * n1 + c.n2) * M + m] : make_float2(0.f, 0.f);
+    fwd_stage1<N1, N2>(v, xs, c);
+    float2 hv[MODE == 2 ? N1 : 1];
+    mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2);
+    auto store = [&](float2* dst) {
         if (live) {
 #pragma unroll
-            for (int n1 = 0; n1 < N1; ++n1) dst[(size_t)(N2 * n1 + n2) * M + m] = v[n1];
+            for (int n1 = 0; n1 < N1; ++n1) dst[(size_t)(N2 * n1 + c.n2) * M + m] = v[n1];
         }
     };
-    finish(spec);
-    if (MODE == 2) {
-        if (N2 > 1) {
+    inv_stage1<N1, N2>(v, xs, c);
+    store(spec);
+    if constexpr (MODE == 2) {
+        if constexpr (N2 > 1) {
             __syncthreads();   // everyone has gathered the g data
 #pragma unroll
             for (int q = 0; q < Q; ++q)
 #pragma unroll
-                for (int j = 0; j < N2; ++j) at(n2 * Q + q, j) = hv[q * N2 + j];
+                for (int j = 0; j < N2; ++j) xs[c.xi(c.n2 * Q + q, j)] = hv[q * N2 + j];
         } else {
 #pragma unroll
             for (int k1 = 0; k1 < N1; ++k1) v[k1] = hv[k1];
         }
-        finish(spec_h);
+        inv_stage1<N1, N2>(v, xs, c);
+        store(spec_h);
+    }
+    if constexpr (MODE == 3) block_sum2(t1, t2, xpart + (size_t)blockIdx.x * 2);
+}
+
+// ---- pipelined persistent kernel (TMA) ----------------------------------------
+constexpr int XSTAGES = 3;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Bounded wait on a phase; false if it did not complete within 2^22 polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t a = smem_u32(bar);
+    for (int i = 0; i < (1 << 22); ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* tm, int x, int y, const void* src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
+                 ::"l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Tile t = pencils [t*P, t*P + P) x all N rows, moved as ROWS-row boxes
+// (ROWS <= 256); the tensor map describes spec as N rows of M complex values.
+template <int N1, int N2, int MODE>
+__global__ void __launch_bounds__(256, N1 >= 32 ? 1 : 2)
+xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ dspec, double* __restrict__ xpart,
+                 int M, int nzh, int nz, int ntiles, const float* __restrict__ kx2, const float* __restrict__ ky2,
+                 const float* __restrict__ kz2, float sym_coef, float dt, float invN) {
+    using C = Col<N1, N2>;
+    constexpr int P = C::P, N = C::N;
+    constexpr int TILE = N * P;                       // complex values per tile
+    constexpr int BOXES = (N + 255) / 256, ROWS = N / BOXES;
+    constexpr uint32_t TILE_BYTES = TILE * sizeof(float2);
+    extern __shared__ __align__(128) float2 ring[];   // [XSTAGES][TILE], each [x][p]
+    __shared__ __align__(8) uint64_t bar[XSTAGES];
+    const int tid = threadIdx.x;
+    const C c{tid % P, tid / P};
+
+    auto issue_load = [&](int slot, int tile) {
+        mbar_expect_tx(&bar[slot], TILE_BYTES);
+#pragma unroll
+        for (int b = 0; b < BOXES; ++b)
+            tma_load_2d(ring + (size_t)slot * TILE + b * ROWS * P, &tm, tile * P, b * ROWS, &bar[slot]);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < XSTAGES; ++s) mbar_init(&bar[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if ((int)blockIdx.x < ntiles) issue_load(0, blockIdx.x);
+    }
+    __syncthreads();
+    float t1 = 0.f, t2 = 0.f;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        const int slot = it % XSTAGES;
+        const int next = tile + gridDim.x;
+        if (tid == 0 && next < ntiles) {
+            // the next slot last held tile it-2, whose store is the older of the
+            // (at most two) bulk groups that may still be reading shared memory
+            bulk_wait_read<1>();
+            issue_load((it + 1) % XSTAGES, next);
+            if (MODE == 3) prefetch_l2(dspec + (size_t)next * N1 * 256, N1 * 256 * sizeof(float2));
+        }
+        if (!mbar_wait(&bar[slot], (uint32_t)(it / XSTAGES) & 1u)) atomicOr(&g_dev_status, 1);
+        float2* xs = ring + (size_t)slot * TILE;
+        const int m = tile * P + c.p;
+        const int mc = m < M ? m : 0;
+        const int ky = mc / nzh, kz = mc - ky * nzh;
+        const float ky2v = __ldg(ky2 + ky), kz2v = __ldg(kz2 + kz);
+        float2* dsp = dspec ? dspec + (size_t)tile * N1 * 256 + tid : nullptr;
+
+        float2 v[N1];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; ++n1) v[n1] = xs[(N2 * n1 + c.n2) * P + c.p];
+        fwd_stage1<N1, N2>(v, xs, c);
+        float2 hv[1];
+        mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2);
+        inv_stage1<N1, N2>(v, xs, c);
+#pragma unroll
+        for (int n1 = 0; n1 < N1; ++n1) xs[(N2 * n1 + c.n2) * P + c.p] = v[n1];
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+#pragma unroll
+            for (int b = 0; b < BOXES; ++b) tma_store_2d(&tm, tile * P, b * ROWS, xs + b * ROWS * P);
+            bulk_commit();
+        }
+    }
+    if (MODE == 3) block_sum2(t1, t2, xpart + (size_t)blockIdx.x * 2);
+    if (tid == 0) bulk_wait_read<0>();   // shared memory must outlive the stores' reads
+}
+
+// ---- host side -------------------------------------------------------------------
+constexpr int MAX_DEVICES = 64;
+int g_tw_rc[MAX_DEVICES];
+std::once_flag g_tw_once[MAX_DEVICES];
+bool g_tma_off = false;   // EVX_XPASS_TMA=0 selects the per-tile kernel everywhere
+
+int xpass_split_n2(int nx) {
+    switch (nx) {
+        case 8: case 16: return 1;
+        case 32: return 2;
+        case 64: return 4;
+        case 128: return 8;
+        case 256: case 512: return 16;
+        default: return 0;
     }
 }
 
-template <int N1, int N2>
-int xpass_launch_t(int mode, float2* spec, float2* spec_h, int M, int nzh, const float* kx2, const float* ky2,
-                   const float* kz2, float sym, float dt, float invN, cudaStream_t st) {
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+template <int N1, int N2, int MODE>
+int xpass_launch_tile(const XpassArgs& A, cudaStream_t st, const char* slot) {
     constexpr int P = 256 / N2;
     const size_t smem = (size_t)N1 * N2 * P * sizeof(float2);
-    static bool attr[3] = {false, false, false};
-    const dim3 grid((M + P - 1) / P);
-    if (mode == 0) {
-        if (!attr[0]) { cudaFuncSetAttribute(xpass_kernel<N1, N2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr[0] = true; }
-        EVX_TIMED("ch_xpass_fwd", st, xpass_kernel<N1, N2, 0><<<grid, 256, smem, st>>>(spec, nullptr, M, nzh, kx2, ky2, kz2, sym, dt, invN));
-    } else if (mode == 1) {
-        if (!attr[1]) { cudaFuncSetAttribute(xpass_kernel<N1, N2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr[1] = true; }
-        EVX_TIMED("ch_xpass_adj", st, xpass_kernel<N1, N2, 1><<<grid, 256, smem, st>>>(spec, nullptr, M, nzh, kx2, ky2, kz2, sym, dt, invN));
-    } else {
-        if (!attr[2]) { cudaFuncSetAttribute(xpass_kernel<N1, N2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr[2] = true; }
-        EVX_TIMED("ch_xpass_adj", st, xpass_kernel<N1, N2, 2><<<grid, 256, smem, st>>>(spec, spec_h, M, nzh, kx2, ky2, kz2, sym, dt, invN));
+    static bool attr = false;   // one flag per instantiation
+    if (!attr) {
+        const int rc = check_cuda(cudaFuncSetAttribute(xpass_kernel<N1, N2, MODE>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                                  "x-pass shared memory attribute");
+        if (rc) return rc;
+        attr = true;
     }
+    const int blocks = (A.M + P - 1) / P;
+    if (A.n_xpart_out) *A.n_xpart_out = blocks;
+    EVX_TIMED(slot, st,
+              xpass_kernel<N1, N2, MODE><<<blocks, 256, smem, st>>>(A.spec, A.spec_h, A.dspec, A.xpart, A.M, A.nzh,
+                                                                  A.nz, A.kx2, A.ky2, A.kz2, A.sym, A.dt, A.invN));
     count_launch();
     return check_launch("xpass_kernel");
+}
+
+template <int N1, int N2, int MODE>
+int xpass_launch_tma(const XpassArgs& A, cudaStream_t st, const char* slot) {
+    constexpr int P = 256 / N2, N = N1 * N2;
+    constexpr int BOXES = (N + 255) / 256, ROWS = N / BOXES;
+    const size_t smem = (size_t)XSTAGES * N * P * sizeof(float2);
+    static int grid_cap = 0;    // resident blocks on the device, per instantiation
+    if (!grid_cap) {
+        int rc = check_cuda(cudaFuncSetAttribute(xpass_tma_kernel<N1, N2, MODE>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                            "x-pass shared memory attribute");
+        if (rc) return rc;
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, xpass_tma_kernel<N1, N2, MODE>, 256, smem),
+                        "x-pass occupancy");
+        if (rc) return rc;
+        grid_cap = sms * (per > 0 ? per : 1);
+    }
+    CUtensorMap tm;
+    const cuuint64_t dims[2] = {(cuuint64_t)A.M, (cuuint64_t)N};
+    const cuuint64_t strides[1] = {(cuuint64_t)A.M * sizeof(float2)};
+    const cuuint32_t box[2] = {(cuuint32_t)P, (cuuint32_t)ROWS};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode_fn()(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, A.spec, dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(EVX_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    const int ntiles = (A.M + P - 1) / P;
+    const int blocks = ntiles < grid_cap ? ntiles : grid_cap;
+    if (A.n_xpart_out) *A.n_xpart_out = blocks;
+    EVX_TIMED(slot, st,
+              xpass_tma_kernel<N1, N2, MODE><<<blocks, 256, smem, st>>>(tm, A.dspec, A.xpart, A.M, A.nzh, A.nz, ntiles,
+                                                                      A.kx2, A.ky2, A.kz2, A.sym, A.dt, A.invN));
+    count_launch();
+    return check_launch("xpass_tma_kernel");
+}
+
+template <int N1, int N2, int MODE>
+int xpass_launch_m(const XpassArgs& A, cudaStream_t st) {
+    const char* slot = MODE == 0 ? (A.dspec ? "ch_xpass_fwd_store" : "ch_xpass_fwd")
+                                 : (MODE == 3 ? "ch_xpass_adj_spec" : "ch_xpass_adj");
+    if constexpr (MODE != 2) {
+        // TMA needs 16-byte row strides (even M) and a 16-byte aligned base; small M keeps the per-tile kernel
+        const bool tma = !g_tma_off && (A.M % 2) == 0 && A.M >= 256 &&
+                         (reinterpret_cast<uintptr_t>(A.spec) & 15) == 0 && encode_fn() != nullptr;
+        if (tma) return xpass_launch_tma<N1, N2, MODE>(A, st, slot);
+    }
+    return xpass_launch_tile<N1, N2, MODE>(A, st, slot);
+}
+
+template <int N1, int N2>
+int xpass_launch_t(const XpassArgs& A, cudaStream_t st) {
+    switch (A.mode) {
+        case 0: return xpass_launch_m<N1, N2, 0>(A, st);
+        case 1: return xpass_launch_m<N1, N2, 1>(A, st);
+        case 2: return xpass_launch_m<N1, N2, 2>(A, st);
+        default: return xpass_launch_m<N1, N2, 3>(A, st);
+    }
 }
 
 }  // namespace
@@ -219,32 +579,61 @@ bool xpass_supported(int nx) {
 }
 
 int xpass_init() {
-    std::call_once(g_tw_once, [] {
+    int dev = 0;
+    int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= MAX_DEVICES) return fail(EVX_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::call_once(g_tw_once[dev], [dev] {
         float2 h[512];
         for (int j = 0; j < 512; ++j) {
             const double a = 2.0 * M_PI * (double)j / 512.0;
             h[j] = make_float2((float)std::cos(a), (float)-std::sin(a));
         }
-        g_tw_rc = check_cuda(cudaMemcpyToSymbol(c_w512, h, sizeof(h)), "twiddle table upload");
+        g_tw_rc[dev] = check_cuda(cudaMemcpyToSymbol(c_w512, h, sizeof(h)), "twiddle table upload");
+        const char* e = std::getenv("EVX_XPASS_TMA");
+        if (e && e[0] == '0') g_tma_off = true;
     });
-    return g_tw_rc;
+    return g_tw_rc[dev];
 }
 
-// mode 0: forward multiply; 1: adjoint g; 2: adjoint g and h (spec_h)
-int xpass_launch(int mode, int nx, float2* spec, float2* spec_h, int M, int nzh, const float* kx2, const float* ky2,
-                 const float* kz2, float sym, float dt, float invN, cudaStream_t st) {
+size_t xpass_blocks(int nx, int M) {
+    const int n2 = xpass_split_n2(nx);
+    if (!n2) return 0;
+    const int P = 256 / n2;
+    return (size_t)((M + P - 1) / P);
+}
+
+size_t xpass_spectrum_floats(int nx, int M) {
+    // [tile][element < N1][thread < 256] complex values; N1 = nx / N2
+    const int n2 = xpass_split_n2(nx);
+    return n2 ? xpass_blocks(nx, M) * (size_t)(nx / n2) * 256 * 2 : 0;
+}
+
+int xpass_launch(const XpassArgs& A, cudaStream_t st) {
     int rc = xpass_init();
     if (rc) return rc;
-    switch (nx) {
-        case 8: return xpass_launch_t<8, 1>(mode, spec, spec_h, M, nzh, kx2, ky2, kz2, sym, dt, invN, st);
-        case 16: return xpass_launch_t<16, 1>(mode, spec, spec_h, M, nzh, kx2, ky2, kz2, sym, dt, invN, st);
-        case 32: return xpass_launch_t<16, 2>(mode, spec, spec_h, M, nzh, kx2, ky2, kz2, sym, dt, invN, st);
-        case 64: return xpass_launch_t<16, 4>(mode, spec, spec_h, M, nzh, kx2, ky2, kz2, sym, dt, invN, st);
-        case 128: return xpass_launch_t<16, 8>(mode, spec, spec_h, M, nzh, kx2, ky2, kz2, sym, dt, invN, st);
-        case 256: return xpass_launch_t<16, 16>(mode, spec, spec_h, M, nzh, kx2, ky2, kz2, sym, dt, invN, st);
-        case 512: return xpass_launch_t<32, 16>(mode, spec, spec_h, M, nzh, kx2, ky2, kz2, sym, dt, invN, st);
+    if ((A.mode == 3 && (!A.dspec || !A.xpart)) || (A.mode == 2 && !A.spec_h))
+        return fail(EVX_ERR_BAD_ARG, "x-pass mode %d is missing a buffer", A.mode);
+    switch (A.nx) {
+        case 8: return xpass_launch_t<8, 1>(A, st);
+        case 16: return xpass_launch_t<16, 1>(A, st);
+        case 32: return xpass_launch_t<16, 2>(A, st);
+        case 64: return xpass_launch_t<16, 4>(A, st);
+        case 128: return xpass_launch_t<16, 8>(A, st);
+        case 256: return xpass_launch_t<16, 16>(A, st);
+        case 512: return xpass_launch_t<32, 16>(A, st);
         default: return fail(EVX_ERR_UNSUPPORTED, "x-pass needs a power-of-two nx in [8, 512]");
     }
 }
 
 }  // namespace evx
+
+extern "C" int evx_device_status(int reset) {
+    int v = 0;
+    if (evx::check_cuda(cudaMemcpyFromSymbol(&v, evx::g_dev_status, sizeof(int)), "read device status")) return -1;
+    if (reset && v) {
+        const int z = 0;
+        if (evx::check_cuda(cudaMemcpyToSymbol(evx::g_dev_status, &z, sizeof(int)), "reset device status")) return -1;
+    }
+    return v;
+}

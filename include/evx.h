@@ -165,6 +165,34 @@ int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps,
                    const float* lam_in, float* lam_out, const evx_ch_params* p,
                    double* grads, void* workspace, void* stream);
 
+/* Stored increment spectra (no reference counterpart: they serve the adjoint).
+ * Floats per step of the spectrum dU = prefac/N * rfftn(rhs) whose inverse
+ * transform is u_{s+1} - u_s, in the x-pass's internal element order; 0 when
+ * the plan has no x-pass (nx not a power of two in [8, 512], or flags bit 1). */
+size_t evx_ch_spectrum_floats(const evx_ch_plan* plan);
+
+/* evx_ch_forward that also writes step s's increment spectrum to
+ * spectra + s*evx_ch_spectrum_floats(plan) (spectra: 16-byte aligned, nsteps
+ * spectra; NULL = plain evx_ch_forward).  EVX_ERR_UNSUPPORTED without x-pass. */
+int evx_ch_forward_spectra(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps,
+                           float* traj, float* spectra, const evx_ch_params* p, int* nonfinite,
+                           void* workspace, void* stream);
+
+/* evx_ch_adjoint with the spectra evx_ch_forward_spectra stored for the same
+ * states and parameters.  With grads, the two mobility sums are formed by
+ * Parseval in the adjoint x-pass, so each step needs one inverse transform
+ * (not two) and the pullback reads neither u_{s+1} nor a second field; the
+ * plan needs no flags bit 0.  states: u_0..u_{n-1} are read (u_n is not).
+ * spectra NULL or grads NULL: same as evx_ch_adjoint. */
+int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* spectra, int nsteps,
+                           const float* lam_in, float* lam_out, const evx_ch_params* p,
+                           double* grads, void* workspace, void* stream);
+
+/* Device-side status bits, synchronous read (reset != 0 clears them): bit 0 =
+ * a bounded wait of the pipelined x-pass on its tile loads gave up (the
+ * results of that call are invalid).  Returns -1 if the read itself failed. */
+int evx_device_status(int reset);
+
 /* Tile shape of the periodic fast-path stencil kernels (single grids):
  * -1 automatic (32x32 when nz is a multiple of 32 but not of 64, else 16x64),
  * 0 = 16x64, 1 = 32x32.  Results are bit-identical for every choice. */

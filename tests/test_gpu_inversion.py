@@ -14,12 +14,12 @@ pytestmark = pytest.mark.gpu
 PIN = lambda c, lib=None: 18 / 3.0 * c * (1 - c) * (1 - 2 * c)  # noqa: E731
 
 
-def runner_for(shape, pinned=None):
+def runner_for(shape, pinned=None, spectral=True):
     from evoxels_gb300.adjoint import CahnHilliardAdjoint
     from evoxels_gb300.voxelfields import VoxelFields
     from evoxels_gb300.voxelgrid import VoxelGridGB300
     vg = VoxelGridGB300(VoxelFields(shape, domain_size=shape).grid_info(), device="cuda")
-    return CahnHilliardAdjoint(vg, dt=0.1, pinned_w=pinned)
+    return CahnHilliardAdjoint(vg, dt=0.1, pinned_w=pinned, spectral=spectral)
 
 
 def test_autograd_function_checkpointed_equals_stored(cuda_lib):
@@ -44,11 +44,11 @@ def test_autograd_function_checkpointed_equals_stored(cuda_lib):
         assert out[K][3] == pytest.approx(out[None][3], rel=1e-12)
 
 
-@pytest.mark.parametrize("pinned", [None, 6.0])
-def test_parameter_gradients_vs_central_differences(cuda_lib, pinned):
+@pytest.mark.parametrize("pinned,spectral", [(None, True), (6.0, True), (None, False)])
+def test_parameter_gradients_vs_central_differences(cuda_lib, pinned, spectral):
     shape = (16, 16, 16)
     n, D, eps, h = 10, 1.1, 1.4, 1e-3
-    r = runner_for(shape, pinned)
+    r = runner_for(shape, pinned, spectral)
     c0n = oracle.seeded_ch_field(shape, 5)
     tgn = oracle.seeded_ch_field(shape, 6)
     c0 = torch.tensor(c0n, dtype=torch.float32, device="cuda").unsqueeze(0)
