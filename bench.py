@@ -47,6 +47,8 @@ NCU_DRAM_BYTES_PER_VOXEL = {
     "ch_pullback_grads": (344.547840e6 + 54.629120e6) / 256 ** 3,
     "fd_step": (552.458240e6 + 498.603264e6) / 512 ** 3,
     "fd_tblock2": (554.379264e6 + 495.615488e6) / 512 ** 3,
+    "ch_xpass_adj_spec": (135.378432e6 + 24.717824e6) / 256 ** 3,
+    "ch_xpass_fwd": (135.399168e6 + 74.517248e6) / (512 * 256 * 256),
 }
 
 
@@ -165,14 +167,14 @@ class ClockSampler:
 class ChFwdAdj:
     """CH 256^3 (or other size) forward + adjoint gradient evaluation."""
 
-    def __init__(self, torch, device, n=256, steps_per=10, seed=6, grads=True):
+    def __init__(self, torch, device, n=256, steps_per=10, seed=6, grads=True, shape=None):
         from evoxels_gb300.adjoint import CahnHilliardAdjoint
         from evoxels_gb300.voxelfields import VoxelFields
         from evoxels_gb300.voxelgrid import VoxelGridGB300
         self.torch = torch
-        self.shape = (n, n, n)
-        self.n = n ** 3
-        self.nspec = n * n * (n // 2 + 1)
+        self.shape = tuple(shape) if shape else (n, n, n)
+        self.n = int(np.prod(self.shape))
+        self.nspec = self.shape[0] * self.shape[1] * (self.shape[2] // 2 + 1)
         self.T = steps_per
         self.grads = grads
         vf = VoxelFields(self.shape, domain_size=self.shape)
@@ -221,15 +223,15 @@ class ChFwdAdj:
 class ChForward:
     """Plain CH forward steps (configs 1 and 5)."""
 
-    def __init__(self, torch, device, n=100, steps_per=100, seed=1):
+    def __init__(self, torch, device, n=100, steps_per=100, seed=1, shape=None):
         from evoxels_gb300.problem_definition import CahnHilliard
         from evoxels_gb300.timesteppers import PseudoSpectralIMEX
         from evoxels_gb300.voxelfields import VoxelFields
         from evoxels_gb300.voxelgrid import VoxelGridGB300
         self.torch = torch
-        self.shape = (n, n, n)
-        self.n = n ** 3
-        self.nspec = n * n * (n // 2 + 1)
+        self.shape = tuple(shape) if shape else (n, n, n)
+        self.n = int(np.prod(self.shape))
+        self.nspec = self.shape[0] * self.shape[1] * (self.shape[2] // 2 + 1)
         self.T = steps_per
         vf = VoxelFields(self.shape, domain_size=self.shape)
         vg = VoxelGridGB300(vf.grid_info(), device=device)
@@ -389,19 +391,19 @@ class Batched:
         return a.elapsed_time(b) / steps
 
 
-def make_workload(name, torch, device, inner=None, spp=4):
+def make_workload(name, torch, device, inner=None, spp=4, shape=None):
     if name == "batched64_fwd":
         return Batched(torch, device, inner or 50, adjoint=False)
     if name == "batched64_fwd_adj":
         return Batched(torch, device, inner or 20, adjoint=True)
     if name == "ch256_fwd_adj":
-        return ChFwdAdj(torch, device, 256, inner or 10, 6)
+        return ChFwdAdj(torch, device, 256, inner or 10, 6, shape=shape)
     if name == "ch128_inversion":
-        return ChFwdAdj(torch, device, 128, inner or 200, 3)
+        return ChFwdAdj(torch, device, 128, inner or 200, 3, shape=shape)
     if name == "ch100_fwd":
-        return ChForward(torch, device, 100, inner or 100, 1)
+        return ChForward(torch, device, 100, inner or 100, 1, shape=shape)
     if name == "ch512_fwd":
-        return ChForward(torch, device, 512, inner or 20, 5)
+        return ChForward(torch, device, 512, inner or 20, 5, shape=shape)
     if name == "fd512":
         return FdForward(torch, device, 512, inner or 100, 2, spp=spp)
     raise SystemExit(f"unknown workload {name}")
@@ -490,7 +492,13 @@ def main():
                     help="override the IMEX/FE steps per bench step (profiling runs)")
     ap.add_argument("--fd-steps-per-pass", type=int, default=4, choices=[1, 2, 4],
                     help="temporal blocking of the finite-difference workload")
+    ap.add_argument("--grid", default=None,
+                    help="NX,NY,NZ: run a Cahn-Hilliard workload on another grid (profiling runs; "
+                         "the metric then names the grid)")
     args = ap.parse_args()
+    args.shape = tuple(int(v) for v in args.grid.split(",")) if args.grid else None
+    if args.shape and (len(args.shape) != 3 or not args.workload.startswith("ch")):
+        raise SystemExit("--grid takes NX,NY,NZ and a Cahn-Hilliard workload")
     warmup = max(3, args.warmup)
 
     import torch
@@ -513,7 +521,7 @@ def main():
 
     from evoxels_gb300 import _lib
     L = _lib.lib()
-    wl = make_workload(args.workload, torch, device, args.inner_steps, args.fd_steps_per_pass)
+    wl = make_workload(args.workload, torch, device, args.inner_steps, args.fd_steps_per_pass, args.shape)
 
     for _ in range(warmup):
         wl.step()
@@ -622,7 +630,8 @@ def main():
                     "speedup": round(plain_ms / (ms / args.steps), 3),
                     "plain_path": "single-grid PseudoSpectralIMEX.advance per instance, same GPU"}
     out = {
-        "metric": METRIC if args.workload == "ch256_fwd_adj" else f"voxel-steps/s {args.workload}",
+        "metric": (METRIC if args.workload == "ch256_fwd_adj" and not args.shape
+                   else f"voxel-steps/s {args.workload}" + ("@%dx%dx%d" % args.shape if args.shape else "")),
         "value": round(value, 1),
         "unit": "voxel-steps/s",
         "n_gpus": world,
@@ -643,7 +652,7 @@ def main():
         "vs_plain": vs_plain,
         "clocks": clocks,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.shape:
         cb, _, _ = cpu_sample(args.workload, torch)
         out["cpu_baseline"] = cb
     if rank == 0:
