@@ -71,6 +71,8 @@ def algorithmic_bytes(slot, n, nspec):
         "cufft_r2c": 4 * n + 8 * nspec,
         "cufft_c2r": 8 * nspec + 4 * n,
         "cufft_c2r_x2": 16 * nspec + 8 * n,
+        "fft_yz_r2c": 4 * n + 8 * nspec,   # read the field, write the (y,z) half spectrum
+        "fft_yz_c2r": 8 * nspec + 4 * n,
         "batch_rhs_fused": 16 * n,
         "batch_rhs": 8 * n,
         "batch_kspace_fwd": 16 * nspec,

@@ -76,6 +76,8 @@ _SIGS = {
     "evx_ch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_spectrum_floats": (C.c_size_t, [_P]),
     "evx_device_status": (C.c_int, [C.c_int]),
+    "evx_fft_yz_r2c": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
+    "evx_fft_yz_c2r": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
     "evx_ch_forward_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_adjoint_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_set_tile_variant": (C.c_int, [C.c_int]),

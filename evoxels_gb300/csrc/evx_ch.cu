@@ -254,12 +254,19 @@ int ch_plan_bind(evx_ch_plan* plan, void* workspace, cudaStream_t st, bool need_
 }
 
 int ch_r2c(evx_ch_plan* plan, const float* in, float2* out, cudaStream_t st) {
+    if (plan->yzmode) return fft_yz_r2c(plan->g.nx, plan->g.ny, plan->g.nz, in, out, st);
     cufftResult r;
     EVX_TIMED("cufft_r2c", st, r = cufftExecR2C(plan->r2c, const_cast<cufftReal*>(in), reinterpret_cast<cufftComplex*>(out)));
     return check_cufft(r, "cufftExecR2C");
 }
 
 int ch_c2r(evx_ch_plan* plan, float2* in, float* out, bool batch2, cudaStream_t st) {
+    if (plan->yzmode) {
+        const evx_grid& g = plan->g;
+        int rc = fft_yz_c2r(g.nx, g.ny, g.nz, in, out, st);
+        if (!rc && batch2) rc = fft_yz_c2r(g.nx, g.ny, g.nz, in + plan->nspec, out + plan->n, st);
+        return rc;
+    }
     cufftResult r;
     EVX_TIMED(batch2 ? "cufft_c2r_x2" : "cufft_c2r", st,
               r = cufftExecC2R(batch2 ? plan->c2r2 : plan->c2r, reinterpret_cast<cufftComplex*>(in), out));
@@ -346,6 +353,7 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
     cufftSetAutoAllocation(p->c2r, 0);
     // power-of-two nx: cuFFT transforms (y, z) for every x plane and the fused x-pass does the rest
     p->xmode = xpass_supported(g->nx) && !(flags & 2);
+    p->yzmode = p->xmode && yz_supported(g->ny, g->nz) && (flags & 4);
     if (p->xmode) {
         int d2[2] = {g->ny, g->nz};
         const int pr = g->ny * g->nz, ps = g->ny * p->nzh;

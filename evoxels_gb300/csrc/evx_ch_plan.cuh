@@ -13,7 +13,8 @@ struct evx_ch_plan {
     size_t nspec;            // nx*ny*nzh complex values
     cufftHandle r2c = 0, c2r = 0, c2r2 = 0;
     bool has_c2r2 = false;
-    bool xmode = false;      // cuFFT over (y, z) batched over x + fused x-pass (power-of-two nx)
+    bool xmode = false;      // (y, z) transforms batched over x + fused x-pass (power-of-two nx)
+    bool yzmode = false;     // the (y, z) transforms by evx_fftyz.cu instead of cuFFT
     size_t ws_fft = 0;       // cuFFT work area (max over plans)
     float* kx2 = nullptr;    // device k^2 tables
     float* ky2 = nullptr;
@@ -85,6 +86,11 @@ inline XpassArgs xpass_args(const evx_ch_plan* plan, int mode, float2* spec, con
     a.sym = P.sym_coef; a.dt = P.dt; a.invN = (float)(1.0 / (double)plan->n);
     return a;
 }
+
+// Fused (y, z) R2C / C2R of all x planes (evx_fftyz.cu), cuFFT's layout and scaling.
+bool yz_supported(int ny, int nz);
+int fft_yz_r2c(int nx, int ny, int nz, const float* in, float2* out, cudaStream_t st);
+int fft_yz_c2r(int nx, int ny, int nz, const float2* in, float* out, cudaStream_t st);
 
 // Tile shape shared by the rhs and pullback stencil kernels.
 constexpr int CH_TZ = 32;           // tile extent along z (= warp width)

@@ -9,20 +9,13 @@
 // pencils x all nx rows is owned by one block of 256 threads; pencil p is
 // handled by N2 threads (N = N1*N2 along x).
 //
-// Four-step FFT with N = N1*N2, n = N2*n1 + n2, k = k1 + N1*k2:
-//   forward  A[k1][n2]     = W_N^{n2 k1} * DFT_N1(x[N2 n1 + n2])[k1]     thread n2, registers
-//            X[k1 + N1 k2] = DFT_N2(A[k1][.])[k2]                      after a shared exchange
-//   inverse  B[k1][n2]     = W_N^{-n2 k1} * IDFT_N2(X[k1 + N1 .])[n2]   the thread holding X
-//            y[N2 n1 + n2] = IDFT_N1(B[.][n2])[n1]                     after a shared exchange
-// The frequency data never needs natural order, so there is no bit-reversal
-// pass, and every thread writes back exactly the elements it loaded.  The
-// in-register DFTs use twiddles fixed at compile time (cos/sin of 2*pi*j/L
-// evaluated by Taylor series in double, so multiplications by 1, -1 and +-i
-// vanish); the inter-stage twiddles W_N^{n2 k1} depend on the thread and come
-// from a table of W_512^j computed on the host in double precision.  The
-// transforms are compiled with FMA contraction (no bitwise requirement; cuFFT
-// rounds differently anyway); the forward multiplier uses explicit
-// round-to-nearest operations as the k-space kernels do.
+// The transform along x is the four-step FFT of evx_fft.cuh (N = N1*N2,
+// compile-time twiddles in the register DFTs); the frequency data never needs
+// natural order, so there is no bit-reversal pass, and every thread writes
+// back exactly the elements it loaded.  Compiled with FMA contraction (no
+// bitwise requirement; cuFFT rounds differently anyway); the forward
+// multiplier uses explicit round-to-nearest operations as the k-space kernels
+// do.
 // Multipliers (same float32 expressions as the k-space kernels):
 //   forward  X * prefac(k) * invN                    (evoxels/timesteppers.py:77,87)
 //   adjoint  X * (prefac*invN), and X * (prefac*invN*k^4) into a second spectrum
@@ -53,150 +46,18 @@
 #include <type_traits>
 
 #include "evx_ch_plan.cuh"
+#include "evx_fft.cuh"
 
 namespace evx {
 namespace {
 
-__constant__ float2 c_w512[512];   // (cos, -sin)(2*pi*j/512): forward roots of unity
+using namespace fft;
+
 __device__ int g_dev_status;       // bit 0: an x-pass barrier wait gave up
-
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-
-// W_512^j of the forward (INV = false) or inverse (conjugate) transform
-template <bool INV>
-__device__ __forceinline__ float2 w512(int j) {
-    const float2 w = c_w512[j & 511];
-    return INV ? make_float2(w.x, -w.y) : w;
-}
-
-// ---- compile-time twiddles ----------------------------------------------------
-constexpr double kPi = 3.141592653589793238462643383279502884;
-// Taylor series on [-pi, pi]; 16 terms leave an error below 1e-18
-__host__ __device__ constexpr double cx_sin(double x) {
-    double t = x, s = x;
-    for (int k = 1; k < 16; ++k) {
-        t *= -x * x / ((2.0 * k) * (2.0 * k + 1.0));
-        s += t;
-    }
-    return s;
-}
-__host__ __device__ constexpr double cx_cos(double x) {
-    double t = 1.0, s = 1.0;
-    for (int k = 1; k < 16; ++k) {
-        t *= -x * x / ((2.0 * k - 1.0) * (2.0 * k));
-        s += t;
-    }
-    return s;
-}
-// 2*pi*j/L reduced to [-pi, pi]
-__host__ __device__ constexpr double cx_angle(int j, int L) {
-    j %= L;
-    if (2 * j > L) j -= L;
-    return 2.0 * kPi * (double)j / (double)L;
-}
-
-// a * W_L^J (forward, W = exp(-2*pi*i/L)) or a * conj(W_L^J) (inverse)
-template <int J, int L, bool INV>
-__device__ __forceinline__ float2 twiddle(float2 a) {
-    constexpr int j = J % L;
-    if constexpr (j == 0) {
-        return a;
-    } else if constexpr (2 * j == L) {
-        return make_float2(-a.x, -a.y);
-    } else if constexpr (4 * j == L) {        // forward -i, inverse +i
-        return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
-    } else if constexpr (4 * j == 3 * L) {    // forward +i, inverse -i
-        return INV ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
-    } else {
-        constexpr float c = (float)cx_cos(cx_angle(j, L));
-        constexpr float s = (float)(INV ? cx_sin(cx_angle(j, L)) : -cx_sin(cx_angle(j, L)));
-        return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
-    }
-}
-
-template <int B, int E, int S = 1, class F>
-__device__ __forceinline__ void static_for(F&& f) {
-    if constexpr (B < E) {
-        f(std::integral_constant<int, B>{});
-        static_for<B + S, E, S>(f);
-    }
-}
-
-template <int L>
-__host__ __device__ constexpr int bitrev(int i) {
-    int r = 0;
-    for (int b = 1; b < L; b <<= 1) {
-        r = (r << 1) | (i & 1);
-        i >>= 1;
-    }
-    return r;
-}
-
-// In-register DFT of length L (power of two <= 32), natural order in and out:
-// radix-2 decimation in time on the bit-reversed input (the permutation is a
-// compile-time register renaming).
-template <int L, bool INV>
-__device__ __forceinline__ void dft(float2 (&v)[L]) {
-#pragma unroll
-    for (int i = 0; i < L; ++i) {
-        const int j = bitrev<L>(i);
-        if (j > i) {
-            const float2 t = v[i];
-            v[i] = v[j];
-            v[j] = t;
-        }
-    }
-    static_for<1, 6>([&](auto S) {
-        constexpr int len = 1 << decltype(S)::value;
-        if constexpr (len <= L) {
-            static_for<0, L, len>([&](auto I) {
-                static_for<0, len / 2>([&](auto K) {
-                    constexpr int i = decltype(I)::value, k = decltype(K)::value;
-                    const float2 a = v[i + k], b = twiddle<k, len, INV>(v[i + k + len / 2]);
-                    v[i + k] = cadd(a, b);
-                    v[i + k + len / 2] = csub(a, b);
-                });
-            });
-        }
-    });
-}
 
 #ifndef EVX_XPASS_MIN_BLOCKS
 #define EVX_XPASS_MIN_BLOCKS 2   // resident blocks per SM the register budget is sized for
 #endif
-
-// Per-thread context of one pencil column.
-template <int N1, int N2>
-struct Col {
-    static constexpr int N = N1 * N2, P = 256 / N2, Q = N1 / N2;
-    static_assert(N1 >= N2 && N1 % N2 == 0 && 256 % N2 == 0, "unsupported split");
-    int p, n2;
-    __device__ __forceinline__ int xi(int k1, int j) const { return (k1 * N2 + j) * P + p; }   // [N1][N2][P]
-};
-
-// Forward stage 1 on the thread's column v (x = N2*n1 + n2): DFT over n1,
-// twiddle, exchange; afterwards v[q*N2 + j] = A[n2*Q + q][j].  The exchange
-// writes only the addresses the column occupies in a [x][p] tile, so it may
-// alias the tile the column was read from.  The gathered rows are rewritten
-// only by their gathering thread (mid_stage), so no barrier follows.
-template <int N1, int N2>
-__device__ __forceinline__ void fwd_stage1(float2 (&v)[N1], float2* xs, const Col<N1, N2>& c) {
-    constexpr int N = N1 * N2, Q = N1 / N2;
-    dft<N1, false>(v);
-    if constexpr (N2 > 1) {
-#pragma unroll
-        for (int k1 = 0; k1 < N1; ++k1) xs[c.xi(k1, c.n2)] = cmul(v[k1], w512<false>((c.n2 * k1) * (512 / N)));
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-#pragma unroll
-            for (int j = 0; j < N2; ++j) v[q * N2 + j] = xs[c.xi(c.n2 * Q + q, j)];
-    }
-}
 
 // Multiplier stage: forward DFT over k2, multiply, inverse DFT, conjugate
 // twiddle into xs[k1][j] (N2 > 1) or back into v (N2 == 1).  MODE 0 forward
@@ -253,18 +114,6 @@ __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 
     }
 }
 
-// Inverse stage 1: gather B[.][n2] (after a barrier), IDFT over k1; v then
-// holds the output column x = N2*n1 + n2 (same addresses as the gather).
-template <int N1, int N2>
-__device__ __forceinline__ void inv_stage1(float2 (&v)[N1], const float2* xs, const Col<N1, N2>& c) {
-    if constexpr (N2 > 1) {
-        __syncthreads();
-#pragma unroll
-        for (int k1 = 0; k1 < N1; ++k1) v[k1] = xs[c.xi(k1, c.n2)];
-    }
-    dft<N1, true>(v);
-}
-
 __device__ __forceinline__ float kz_weight(int kz, int nz) { return (kz == 0 || 2 * kz == nz) ? 1.f : 2.f; }
 
 // Block sums of (t1, t2) in double, fixed order, into out[0..1].
@@ -299,10 +148,10 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
              const float* __restrict__ kx2, const float* __restrict__ ky2, const float* __restrict__ kz2,
              float sym_coef, float dt, float invN) {
     using C = Col<N1, N2>;
-    constexpr int P = C::P, Q = C::Q;
+    constexpr int P = 256 / N2, Q = C::Q;
     extern __shared__ float2 xs[];       // [N1][N2][P], pencil index fastest (conflict-free)
     const int tid = threadIdx.x;
-    const C c{tid % P, tid / P};
+    const C c{tid % P, tid / P, P};
     const int m = blockIdx.x * P + c.p;
     const bool live = m < M;
     const int mc = live ? m : 0;
@@ -398,14 +247,14 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
                  int M, int nzh, int nz, int ntiles, const float* __restrict__ kx2, const float* __restrict__ ky2,
                  const float* __restrict__ kz2, float sym_coef, float dt, float invN) {
     using C = Col<N1, N2>;
-    constexpr int P = C::P, N = C::N;
+    constexpr int P = 256 / N2, N = C::N;
     constexpr int TILE = N * P;                       // complex values per tile
     constexpr int BOXES = (N + 255) / 256, ROWS = N / BOXES;
     constexpr uint32_t TILE_BYTES = TILE * sizeof(float2);
     extern __shared__ __align__(128) float2 ring[];   // [XSTAGES][TILE], each [x][p]
     __shared__ __align__(8) uint64_t bar[XSTAGES];
     const int tid = threadIdx.x;
-    const C c{tid % P, tid / P};
+    const C c{tid % P, tid / P, P};
 
     auto issue_load = [&](int slot, int tile) {
         mbar_expect_tx(&bar[slot], TILE_BYTES);
@@ -584,12 +433,7 @@ int xpass_init() {
     if (rc) return rc;
     if (dev < 0 || dev >= MAX_DEVICES) return fail(EVX_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
     std::call_once(g_tw_once[dev], [dev] {
-        float2 h[512];
-        for (int j = 0; j < 512; ++j) {
-            const double a = 2.0 * M_PI * (double)j / 512.0;
-            h[j] = make_float2((float)std::cos(a), (float)-std::sin(a));
-        }
-        g_tw_rc[dev] = check_cuda(cudaMemcpyToSymbol(c_w512, h, sizeof(h)), "twiddle table upload");
+        g_tw_rc[dev] = check_cuda(upload_w512(), "twiddle table upload");
         const char* e = std::getenv("EVX_XPASS_TMA");
         if (e && e[0] == '0') g_tma_off = true;
     });

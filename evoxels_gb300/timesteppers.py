@@ -25,12 +25,12 @@ from .voxelgrid import cuda_stream
 class ChPlan:
     """An ``evx_ch_plan`` plus its device workspace (one per grid shape/spacing/device)."""
 
-    def __init__(self, vg, grads=False, cufft3d=False):
+    def __init__(self, vg, grads=False, cufft3d=False, fused_yz=False):
         self.vg = vg
         self.grid = vg.evx_grid()
         self.grads = grads
         h = C.c_void_p()
-        flags = (1 if grads else 0) | (2 if cufft3d else 0)
+        flags = (1 if grads else 0) | (2 if cufft3d else 0) | (4 if fused_yz else 0)
         with torch.cuda.device(vg.device):
             _lib.check(_lib.lib().evx_ch_plan_create(C.byref(h), self.grid, flags), "evx_ch_plan_create")
         self.handle = h
@@ -51,14 +51,15 @@ _plan_lock = threading.Lock()
 _plans = {}
 
 
-def get_plan(vg, grads=False, cufft3d=False):
+def get_plan(vg, grads=False, cufft3d=False, fused_yz=False):
     """Cached plan per grid; ``cufft3d`` forces cuFFT's 3-D transforms instead of the
-    (y, z) transforms plus the fused x-pass used for power-of-two ``Nx``."""
-    key = (vg.shape, vg.spacing, str(vg.device), bool(grads), bool(cufft3d))
+    (y, z) transforms plus the fused x-pass used for power-of-two ``Nx``; ``fused_yz``
+    replaces cuFFT's (y, z) transforms by the fused cluster kernels (opt-in)."""
+    key = (vg.shape, vg.spacing, str(vg.device), bool(grads), bool(cufft3d), bool(fused_yz))
     with _plan_lock:
         p = _plans.get(key)
         if p is None:
-            p = ChPlan(vg, grads, cufft3d)
+            p = ChPlan(vg, grads, cufft3d, fused_yz)
             _plans[key] = p
         return p
 

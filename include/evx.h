@@ -137,6 +137,10 @@ typedef struct evx_ch_plan evx_ch_plan;
  * default a power-of-two nx uses cuFFT over (y, z) and a fused x-pass that
  * does the x transforms and the k-space multiply in one read and write). */
 int evx_ch_plan_create(evx_ch_plan** plan, const evx_grid* g, int flags);
+/* flags bit 2: with the x-pass and ny, nz in {64, 128, 256}, use the fused
+ * (y, z) kernels (evx_fft_yz_r2c/c2r) instead of cuFFT's (y, z) plans.  Off by
+ * default: on GB300 at 256^3 they take 73/68 us per transform against cuFFT's
+ * 65/62 us (latency-bound; one HBM pass instead of two does not pay yet). */
 int evx_ch_plan_destroy(evx_ch_plan* plan);
 
 /* Bytes of device workspace (256-byte aligned start) the plan's calls need. */
@@ -187,6 +191,16 @@ int evx_ch_forward_spectra(evx_ch_plan* plan, const float* u_in, float* u_out, i
 int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* spectra, int nsteps,
                            const float* lam_in, float* lam_out, const evx_ch_params* p,
                            double* grads, void* workspace, void* stream);
+
+/* Fused 2-D (y, z) real-to-complex / complex-to-real transforms of the nx
+ * planes of a float32 (nx, ny, nz) field, in cuFFT's batched 2-D layout and
+ * scaling (spec (nx, ny, nz/2+1) complex64 as interleaved floats, unnormalised);
+ * one HBM pass each (thread-block clusters exchange the transposed data in
+ * distributed shared memory).  ny, nz in {64, 128, 256}; else
+ * EVX_ERR_UNSUPPORTED.  No reference counterpart: building blocks of the
+ * spectral step exposed for tests and other hosts. */
+int evx_fft_yz_r2c(const float* in, float* spec, int nx, int ny, int nz, void* stream);
+int evx_fft_yz_c2r(const float* spec, float* out, int nx, int ny, int nz, void* stream);
 
 /* Device-side status bits, synchronous read (reset != 0 clears them): bit 0 =
  * a bounded wait of the pipelined x-pass on its tile loads gave up (the
