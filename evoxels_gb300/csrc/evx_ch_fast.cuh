@@ -51,6 +51,15 @@ __device__ __forceinline__ float4 clip4(float4 v) {
     return make_float4(clip01(v.x), clip01(v.y), clip01(v.z), clip01(v.w));
 }
 
+// Two-lane fp32 arithmetic (sm_100 FADD2 / FMUL2 / FFMA2): each lane rounds
+// exactly as the scalar __fadd_rn / __fmul_rn / __fmaf_rn.  sub2 is one
+// rounding of a - b (b*(-1) is exact), i.e. the same as __fsub_rn per lane.
+__device__ __forceinline__ float2 f2s(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2s(-1.f), a); }
+
 // Per-thread load plan for one shared field plane (precomputed once per tile).
 struct LoadPlan {
     int goff[2];    // in-plane global offset of the float4 (wrapped)

@@ -25,31 +25,38 @@ using namespace fast;
 constexpr int RING_C = 4 * MAX_FIELD, RING_M = 2 * MAX_POT;
 constexpr size_t ADJ_SMEM = (size_t)(2 * RING_C + 2 * RING_M) * sizeof(float) + 4 * 8 * sizeof(double);
 
-__device__ __forceinline__ float phi_c(float c) { return c * (1.f - c) * (1.f - 2.f * c); }
-__device__ __forceinline__ float dphi_c(float c) { return 1.f - 6.f * c + 6.f * c * c; }
-__device__ __forceinline__ float lap_f(const Geo& G, float c, float xm, float xp, float ym, float yp, float zm,
-                                       float zp) {
-    return ((xp + xm) * G.ih2[0] + (yp + ym) * G.ih2[1]) + (zp + zm) * G.ih2[2] - (2.f * c) * G.ih2sum;
+// Two points of a patch row (z-adjacent) are processed together with the
+// sm_100 two-lane fp32 instructions (FADD2 / FMUL2 / FFMA2).
+__device__ __forceinline__ float2 phi2(float2 c) {    // c(1-c)(1-2c)
+    return mul2(mul2(c, sub2(f2s(1.f), c)), fma2(c, f2s(-2.f), f2s(1.f)));
 }
-// Gbar on a face: (ih*D*(g_lo - g_hi)) * m(cf)
-__device__ __forceinline__ float gbar(float c_lo, float c_hi, float g_lo, float g_hi, float ihD) {
-    const float cf = 0.5f * (c_lo + c_hi);
-    return ihD * (g_lo - g_hi) * (cf * (1.f - cf));
+__device__ __forceinline__ float2 dphi2(float2 c) {   // 1 - 6c + 6c^2
+    return fma2(mul2(f2s(6.f), c), sub2(c, f2s(1.f)), f2s(1.f));
 }
-// cbar-face and (optionally) forward flux on a face
-struct FaceB {
-    float cfb, F;
+struct LapK {   // broadcast Laplacian weights
+    float2 x, y, z, m2sum;   // ih2 per axis, -2*sum(ih2)
 };
-template <bool GRADS>
-__device__ __forceinline__ FaceB face_b(float c_lo, float c_hi, float m_lo, float m_hi, float g_lo, float g_hi,
-                                        float ih, float ihD) {
-    const float cf = 0.5f * (c_lo + c_hi);
-    const float Gr = (m_hi - m_lo) * ih;
-    const float Fb = ihD * (g_lo - g_hi);
-    FaceB o;
-    o.cfb = (Fb * Gr) * (1.f - 2.f * cf);
-    o.F = GRADS ? (cf * (1.f - cf)) * Gr : 0.f;
-    return o;
+// ((xp+xm)*ih2x + (yp+ym)*ih2y) + (zp+zm)*ih2z - 2c*sum(ih2)
+__device__ __forceinline__ float2 lap2(const LapK& L, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
+                                       float2 zm, float2 zp) {
+    float2 t = mul2(add2(xp, xm), L.x);
+    t = fma2(add2(yp, ym), L.y, t);
+    t = fma2(add2(zp, zm), L.z, t);
+    return fma2(c, L.m2sum, t);
+}
+// Gbar on a face: (ihD*(g_lo - g_hi)) * m(cf), m(x) = x(1-x), cf = (c_lo + c_hi)/2
+__device__ __forceinline__ float2 gbar2(float2 clo, float2 chi, float2 glo, float2 ghi, float2 ihD) {
+    const float2 cf = mul2(f2s(0.5f), add2(clo, chi));
+    return mul2(mul2(ihD, sub2(glo, ghi)), mul2(cf, sub2(f2s(1.f), cf)));
+}
+// cbar on a face: (ihD*(g_lo - g_hi)) * ((mu_hi - mu_lo)*ih) * (1 - 2cf)
+__device__ __forceinline__ float2 cfb2(float2 clo, float2 chi, float2 mlo, float2 mhi, float2 glo, float2 ghi,
+                                       float2 ih, float2 ihD) {
+    const float2 cf = mul2(f2s(0.5f), add2(clo, chi));
+    return mul2(mul2(mul2(ihD, sub2(glo, ghi)), mul2(sub2(mhi, mlo), ih)), fma2(cf, f2s(-2.f), f2s(1.f)));
+}
+__device__ __forceinline__ float2 sel2(bool px, bool py, float2 v) {
+    return make_float2(px ? v.x : 0.f, py ? v.y : 0.f);
 }
 
 // Block reduction of four float partial sums into double, written by threads 0..3.
@@ -78,15 +85,15 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
                                               const Geo& G, const ChP& P, int k0, int j0, int x0, int x1,
                                               float* cs, float* gs, float* ms, float* bs,
                                               float& sD, float& sK, float& sW, float& sH) {
-    constexpr bool GRADS = GR != 0;
     const int tid = threadIdx.x;
     const int tx = tid % T::BX, ty = tid / T::BX;
     const int W = T::W;
     const int nx = G.nx, ny = G.ny, nz = G.nz;
     const size_t plane = (size_t)ny * nz;
-    const float ihx = G.ih[0], ihy = G.ih[1], ihz = G.ih[2];
-    const float ihDx = ihx * P.D, ihDy = ihy * P.D, ihDz = ihz * P.D;
-    const float w = P.w, kap = P.kappa;
+    const float2 ihx = f2s(G.ih[0]), ihy = f2s(G.ih[1]), ihz = f2s(G.ih[2]);
+    const float2 ihDx = f2s(G.ih[0] * P.D), ihDy = f2s(G.ih[1] * P.D), ihDz = f2s(G.ih[2] * P.D);
+    const float2 w2 = f2s(P.w), mk2 = f2s(-P.kappa);
+    const LapK L{f2s(G.ih2[0]), f2s(G.ih2[1]), f2s(G.ih2[2]), f2s(-2.f * G.ih2sum)};
     const LoadPlan LP = make_load_plan<T>(tid, j0, k0, ny, nz);
     int mr[2], mc[2];
     bool mv[2];
@@ -102,6 +109,7 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     const int gj = j0 + 2 * ty, gk = k0 + 2 * tx;
     const bool wk = gk < nz, wj0 = gj < ny && wk, wj1 = gj + 1 < ny && wk;
     const int pa = ra * W + rc, pb = pa + W;   // field offsets of the patch rows
+    float2 aD = f2s(0.f), aK = f2s(0.f), aW = f2s(0.f), aH = f2s(0.f);   // gradient partial sums
 
     float4 pc[2], pg[2];
     auto fetch = [&](int p) {
@@ -124,19 +132,15 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             }
     };
 
-    float gxm[2][4];   // Gbar on the x face below the current potential plane, per patch point
-    auto gx_faces = [&](int plo, int m, float out[4]) {
+    float2 gxm[2][2];   // Gbar on the x face below the current potential plane, per patch row
+    auto gx_faces = [&](int plo, int m, float2 out[2]) {
         const float* c0 = cs + (plo & 3) * T::FIELD;
         const float* c1 = cs + ((plo + 1) & 3) * T::FIELD;
         const float* g0 = gs + (plo & 3) * T::FIELD;
         const float* g1 = gs + ((plo + 1) & 3) * T::FIELD;
         const int a = mr[m] * W + mc[m], b = a + W;
-        const float2 cA0 = lds2(c0 + a), cB0 = lds2(c0 + b), cA1 = lds2(c1 + a), cB1 = lds2(c1 + b);
-        const float2 gA0 = lds2(g0 + a), gB0 = lds2(g0 + b), gA1 = lds2(g1 + a), gB1 = lds2(g1 + b);
-        out[0] = gbar(cA0.x, cA1.x, gA0.x, gA1.x, ihDx);
-        out[1] = gbar(cA0.y, cA1.y, gA0.y, gA1.y, ihDx);
-        out[2] = gbar(cB0.x, cB1.x, gB0.x, gB1.x, ihDx);
-        out[3] = gbar(cB0.y, cB1.y, gB0.y, gB1.y, ihDx);
+        out[0] = gbar2(lds2(c0 + a), lds2(c1 + a), lds2(g0 + a), lds2(g1 + a), ihDx);
+        out[1] = gbar2(lds2(c0 + b), lds2(c1 + b), lds2(g0 + b), lds2(g1 + b), ihDx);
     };
 
     auto compute_mu = [&](int p) {
@@ -150,77 +154,52 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         for (int m = 0; m < 2; ++m) {
             if (!mv[m]) continue;
             const int a = mr[m] * W + mc[m], b = a + W;
-            {   // chemical potential on the 2x2 patch
-                const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
-                const float Al = cc[a - 1], Ar = cc[a + 2], Bl = cc[b - 1], Br = cc[b + 2];
-                const float2 xmA = lds2(cm + a), xmB = lds2(cm + b), xpA = lds2(cp + a), xpB = lds2(cp + b);
-                const float m00 = w * phi_c(A.x) - kap * lap_f(G, A.x, xmA.x, xpA.x, up.x, B.x, Al, A.y);
-                const float m01 = w * phi_c(A.y) - kap * lap_f(G, A.y, xmA.y, xpA.y, up.y, B.y, A.x, Ar);
-                const float m10 = w * phi_c(B.x) - kap * lap_f(G, B.x, xmB.x, xpB.x, A.x, dn.x, Bl, B.y);
-                const float m11 = w * phi_c(B.y) - kap * lap_f(G, B.y, xmB.y, xpB.y, A.y, dn.y, B.x, Br);
-                sts2(mo + a - W, m00, m01);
-                sts2(mo + b - W, m10, m11);
+            const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
+            const float2 zmA = make_float2(cc[a - 1], A.x), zpA = make_float2(A.y, cc[a + 2]);
+            const float2 zmB = make_float2(cc[b - 1], B.x), zpB = make_float2(B.y, cc[b + 2]);
+            // chemical potential w*phi(c) - kappa*L(c) on the 2x2 patch
+            const float2 muA = fma2(w2, phi2(A), mul2(mk2, lap2(L, A, lds2(cm + a), lds2(cp + a), up, B, zmA, zpA)));
+            const float2 muB = fma2(w2, phi2(B), mul2(mk2, lap2(L, B, lds2(cm + b), lds2(cp + b), A, dn, zmB, zpB)));
+            *reinterpret_cast<float2*>(mo + a - W) = muA;
+            *reinterpret_cast<float2*>(mo + b - W) = muB;
+            // mub = sum_faces ih*(Gb_minus - Gb_plus)
+            float2 gxp[2];
+            gx_faces(p, m, gxp);
+            float2 bA = mul2(sub2(gxm[m][0], gxp[0]), ihx);
+            float2 bB = mul2(sub2(gxm[m][1], gxp[1]), ihx);
+            gxm[m][0] = gxp[0];
+            gxm[m][1] = gxp[1];
+            const float2 gup = lds2(gc + a - W), gA = lds2(gc + a), gB = lds2(gc + b), gdn = lds2(gc + b + W);
+            {   // z faces: (left, mid) and (mid, right) of each row
+                const float2 gzmA = make_float2(gc[a - 1], gA.x), gzpA = make_float2(gA.y, gc[a + 2]);
+                const float2 gzmB = make_float2(gc[b - 1], gB.x), gzpB = make_float2(gB.y, gc[b + 2]);
+                bA = fma2(sub2(gbar2(zmA, A, gzmA, gA, ihDz), gbar2(A, zpA, gA, gzpA, ihDz)), ihz, bA);
+                bB = fma2(sub2(gbar2(zmB, B, gzmB, gB, ihDz), gbar2(B, zpB, gB, gzpB, ihDz)), ihz, bB);
             }
-            // mub = sum_faces ih*(Gb_minus - Gb_plus), accumulated face by face
-            float bq[4];
-            {
-                float gxp[4];
-                gx_faces(p, m, gxp);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    bq[q] = (gxm[m][q] - gxp[q]) * ihx;
-                    gxm[m][q] = gxp[q];
-                }
+            {   // y faces above, between and below the two rows
+                const float2 y0 = gbar2(up, A, gup, gA, ihDy), y1 = gbar2(A, B, gA, gB, ihDy);
+                const float2 y2 = gbar2(B, dn, gB, gdn, ihDy);
+                bA = fma2(sub2(y0, y1), ihy, bA);
+                bB = fma2(sub2(y1, y2), ihy, bB);
             }
-            {   // z faces, row a then row b
-                const float2 A = lds2(cc + a), gA = lds2(gc + a);
-                float f = gbar(cc[a - 1], A.x, gc[a - 1], gA.x, ihDz) * ihz;
-                bq[0] += f;
-                f = gbar(A.x, A.y, gA.x, gA.y, ihDz) * ihz;
-                bq[0] -= f; bq[1] += f;
-                bq[1] -= gbar(A.y, cc[a + 2], gA.y, gc[a + 2], ihDz) * ihz;
-                const float2 B = lds2(cc + b), gB = lds2(gc + b);
-                f = gbar(cc[b - 1], B.x, gc[b - 1], gB.x, ihDz) * ihz;
-                bq[2] += f;
-                f = gbar(B.x, B.y, gB.x, gB.y, ihDz) * ihz;
-                bq[2] -= f; bq[3] += f;
-                bq[3] -= gbar(B.y, cc[b + 2], gB.y, gc[b + 2], ihDz) * ihz;
-            }
-            {   // y faces, both columns at once
-                const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
-                const float2 gup = lds2(gc + a - W), gA = lds2(gc + a), gB = lds2(gc + b), gdn = lds2(gc + b + W);
-                bq[0] += gbar(up.x, A.x, gup.x, gA.x, ihDy) * ihy;
-                bq[1] += gbar(up.y, A.y, gup.y, gA.y, ihDy) * ihy;
-                float f = gbar(A.x, B.x, gA.x, gB.x, ihDy) * ihy;
-                bq[0] -= f; bq[2] += f;
-                f = gbar(A.y, B.y, gA.y, gB.y, ihDy) * ihy;
-                bq[1] -= f; bq[3] += f;
-                bq[2] -= gbar(B.x, dn.x, gB.x, gdn.x, ihDy) * ihy;
-                bq[3] -= gbar(B.y, dn.y, gB.y, gdn.y, ihDy) * ihy;
-            }
-            sts2(bo + a - W, bq[0], bq[1]);
-            sts2(bo + b - W, bq[2], bq[3]);
+            *reinterpret_cast<float2*>(bo + a - W) = bA;
+            *reinterpret_cast<float2*>(bo + b - W) = bB;
         }
     };
 
-    // x face quantities of the output patch between planes plo and plo+1
-    float cfx_m[4], Fx_m[4], c_prev[4], b_prev[4];
-    auto x_faces_b = [&](int plo, float cfb[4], float F[4]) {
+    // x face cbar of the output patch between planes plo and plo+1
+    float2 cfx_m[2], c_prev[2], b_prev[2];
+    auto x_faces_b = [&](int plo, float2 out[2]) {
         const float* c0 = cs + (plo & 3) * T::FIELD;
         const float* c1 = cs + ((plo + 1) & 3) * T::FIELD;
         const float* g0 = gs + (plo & 3) * T::FIELD;
         const float* g1 = gs + ((plo + 1) & 3) * T::FIELD;
         const float* m0 = ms + (plo & 1) * T::POT;
         const float* m1 = ms + ((plo + 1) & 1) * T::POT;
-        const float2 cA0 = lds2(c0 + pa), cB0 = lds2(c0 + pb), cA1 = lds2(c1 + pa), cB1 = lds2(c1 + pb);
-        const float2 gA0 = lds2(g0 + pa), gB0 = lds2(g0 + pb), gA1 = lds2(g1 + pa), gB1 = lds2(g1 + pb);
-        const float2 mA0 = lds2(m0 + pa - W), mB0 = lds2(m0 + pb - W), mA1 = lds2(m1 + pa - W),
-                     mB1 = lds2(m1 + pb - W);
-        FaceB f;
-        f = face_b<GRADS>(cA0.x, cA1.x, mA0.x, mA1.x, gA0.x, gA1.x, ihx, ihDx); cfb[0] = f.cfb; F[0] = f.F;
-        f = face_b<GRADS>(cA0.y, cA1.y, mA0.y, mA1.y, gA0.y, gA1.y, ihx, ihDx); cfb[1] = f.cfb; F[1] = f.F;
-        f = face_b<GRADS>(cB0.x, cB1.x, mB0.x, mB1.x, gB0.x, gB1.x, ihx, ihDx); cfb[2] = f.cfb; F[2] = f.F;
-        f = face_b<GRADS>(cB0.y, cB1.y, mB0.y, mB1.y, gB0.y, gB1.y, ihx, ihDx); cfb[3] = f.cfb; F[3] = f.F;
+        out[0] = cfb2(lds2(c0 + pa), lds2(c1 + pa), lds2(m0 + pa - W), lds2(m1 + pa - W), lds2(g0 + pa),
+                      lds2(g1 + pa), ihx, ihDx);
+        out[1] = cfb2(lds2(c0 + pb), lds2(c1 + pb), lds2(m0 + pb - W), lds2(m1 + pb - W), lds2(g0 + pb),
+                      lds2(g1 + pb), ihx, ihDx);
     };
 
     auto compute_lam = [&](int i) {
@@ -230,113 +209,85 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         const float* bb = bs + (i & 1) * T::POT;
         const float* bp = bs + ((i + 1) & 1) * T::POT;
         // acc: sum of cbar-face values around each point (times 0.5 at the end)
-        float acc[4];
+        float2 accA, accB;
         {
-            float cfx_p[4], Fx_p[4];
-            x_faces_b(i, cfx_p, Fx_p);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                acc[q] = cfx_m[q] + cfx_p[q];
-                cfx_m[q] = cfx_p[q];
-            }
+            float2 cfx_p[2];
+            x_faces_b(i, cfx_p);
+            accA = add2(cfx_m[0], cfx_p[0]);
+            accB = add2(cfx_m[1], cfx_p[1]);
+            cfx_m[0] = cfx_p[0];
+            cfx_m[1] = cfx_p[1];
         }
-        auto face = [&](int lo, int hi, float c_lo, float c_hi, float m_lo, float m_hi, float g_lo, float g_hi,
-                        float ih, float ihD) {
-            const FaceB f = face_b<false>(c_lo, c_hi, m_lo, m_hi, g_lo, g_hi, ih, ihD);
-            if (lo >= 0) acc[lo] += f.cfb;
-            if (hi >= 0) acc[hi] += f.cfb;
-        };
+        const float2 up = lds2(cc + pa - W), A = lds2(cc + pa), B = lds2(cc + pb), dn = lds2(cc + pb + W);
+        const float2 zmA = make_float2(cc[pa - 1], A.x), zpA = make_float2(A.y, cc[pa + 2]);
+        const float2 zmB = make_float2(cc[pb - 1], B.x), zpB = make_float2(B.y, cc[pb + 2]);
+        const float2 MA = lds2(mm + pa - W), MB = lds2(mm + pb - W);
+        const float2 gA = lds2(gc + pa), gB = lds2(gc + pb);
         {   // z faces
-            const float2 A = lds2(cc + pa), MA = lds2(mm + pa - W), gA = lds2(gc + pa);
-            face(-1, 0, cc[pa - 1], A.x, mm[pa - W - 1], MA.x, gc[pa - 1], gA.x, ihz, ihDz);
-            face(0, 1, A.x, A.y, MA.x, MA.y, gA.x, gA.y, ihz, ihDz);
-            face(1, -1, A.y, cc[pa + 2], MA.y, mm[pa - W + 2], gA.y, gc[pa + 2], ihz, ihDz);
-            const float2 B = lds2(cc + pb), MB = lds2(mm + pb - W), gB = lds2(gc + pb);
-            face(-1, 2, cc[pb - 1], B.x, mm[pb - W - 1], MB.x, gc[pb - 1], gB.x, ihz, ihDz);
-            face(2, 3, B.x, B.y, MB.x, MB.y, gB.x, gB.y, ihz, ihDz);
-            face(3, -1, B.y, cc[pb + 2], MB.y, mm[pb - W + 2], gB.y, gc[pb + 2], ihz, ihDz);
+            const float2 mzmA = make_float2(mm[pa - W - 1], MA.x), mzpA = make_float2(MA.y, mm[pa - W + 2]);
+            const float2 mzmB = make_float2(mm[pb - W - 1], MB.x), mzpB = make_float2(MB.y, mm[pb - W + 2]);
+            const float2 gzmA = make_float2(gc[pa - 1], gA.x), gzpA = make_float2(gA.y, gc[pa + 2]);
+            const float2 gzmB = make_float2(gc[pb - 1], gB.x), gzpB = make_float2(gB.y, gc[pb + 2]);
+            accA = add2(accA, add2(cfb2(zmA, A, mzmA, MA, gzmA, gA, ihz, ihDz), cfb2(A, zpA, MA, mzpA, gA, gzpA, ihz, ihDz)));
+            accB = add2(accB, add2(cfb2(zmB, B, mzmB, MB, gzmB, gB, ihz, ihDz), cfb2(B, zpB, MB, mzpB, gB, gzpB, ihz, ihDz)));
         }
         {   // y faces
-            const float2 up = lds2(cc + pa - W), A = lds2(cc + pa), B = lds2(cc + pb), dn = lds2(cc + pb + W);
-            const float2 mup = lds2(mm + pa - 2 * W), MA = lds2(mm + pa - W), MB = lds2(mm + pb - W),
-                         mdn = lds2(mm + pb);
-            const float2 gup = lds2(gc + pa - W), gA = lds2(gc + pa), gB = lds2(gc + pb), gdn = lds2(gc + pb + W);
-            face(-1, 0, up.x, A.x, mup.x, MA.x, gup.x, gA.x, ihy, ihDy);
-            face(-1, 1, up.y, A.y, mup.y, MA.y, gup.y, gA.y, ihy, ihDy);
-            face(0, 2, A.x, B.x, MA.x, MB.x, gA.x, gB.x, ihy, ihDy);
-            face(1, 3, A.y, B.y, MA.y, MB.y, gA.y, gB.y, ihy, ihDy);
-            face(2, -1, B.x, dn.x, MB.x, mdn.x, gB.x, gdn.x, ihy, ihDy);
-            face(3, -1, B.y, dn.y, MB.y, mdn.y, gB.y, gdn.y, ihy, ihDy);
+            const float2 mup = lds2(mm + pa - 2 * W), mdn = lds2(mm + pb);
+            const float2 gup = lds2(gc + pa - W), gdn = lds2(gc + pb + W);
+            const float2 y0 = cfb2(up, A, mup, MA, gup, gA, ihy, ihDy), y1 = cfb2(A, B, MA, MB, gA, gB, ihy, ihDy);
+            const float2 y2 = cfb2(B, dn, MB, mdn, gB, gdn, ihy, ihDy);
+            accA = add2(accA, add2(y0, y1));
+            accB = add2(accB, add2(y1, y2));
         }
         // Laplacian of mub
-        float Lb[4], bpt[4];
-        {
-            const float2 bup = lds2(bb + pa - 2 * W), bA = lds2(bb + pa - W), bB = lds2(bb + pb - W),
-                         bdn = lds2(bb + pb);
-            const float2 bxA = lds2(bp + pa - W), bxB = lds2(bp + pb - W);
-            Lb[0] = lap_f(G, bA.x, b_prev[0], bxA.x, bup.x, bB.x, bb[pa - W - 1], bA.y);
-            Lb[1] = lap_f(G, bA.y, b_prev[1], bxA.y, bup.y, bB.y, bA.x, bb[pa - W + 2]);
-            Lb[2] = lap_f(G, bB.x, b_prev[2], bxB.x, bA.x, bdn.x, bb[pb - W - 1], bB.y);
-            Lb[3] = lap_f(G, bB.y, b_prev[3], bxB.y, bA.y, bdn.y, bB.x, bb[pb - W + 2]);
-            bpt[0] = bA.x; bpt[1] = bA.y; bpt[2] = bB.x; bpt[3] = bB.y;
-        }
-        const float2 A = lds2(cc + pa), B = lds2(cc + pb);
-        const float cpt[4] = {A.x, A.y, B.x, B.y};
+        const float2 bA = lds2(bb + pa - W), bB = lds2(bb + pb - W);
+        const float2 LbA = lap2(L, bA, b_prev[0], lds2(bp + pa - W), lds2(bb + pa - 2 * W), bB,
+                                make_float2(bb[pa - W - 1], bA.x), make_float2(bA.y, bb[pa - W + 2]));
+        const float2 LbB = lap2(L, bB, b_prev[1], lds2(bp + pb - W), bA, lds2(bb + pb),
+                                make_float2(bb[pb - W - 1], bB.x), make_float2(bB.y, bb[pb - W + 2]));
         const size_t o = (size_t)i * plane + (size_t)gj * nz + gk;
-        float ur[4], lv[4];
+        const float2 u0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u + o)) : f2s(0.f);
+        const float2 u1r = wj1 ? __ldg(reinterpret_cast<const float2*>(u + o + nz)) : f2s(0.f);
+        const float2 l0 = wj0 ? __ldg(reinterpret_cast<const float2*>(lam + o)) : f2s(0.f);
+        const float2 l1 = wj1 ? __ldg(reinterpret_cast<const float2*>(lam + o + nz)) : f2s(0.f);
         {
-            const float2 u0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u + o)) : make_float2(0.f, 0.f);
-            const float2 u1r = wj1 ? __ldg(reinterpret_cast<const float2*>(u + o + nz)) : make_float2(0.f, 0.f);
-            const float2 l0 = wj0 ? __ldg(reinterpret_cast<const float2*>(lam + o)) : make_float2(0.f, 0.f);
-            const float2 l1 = wj1 ? __ldg(reinterpret_cast<const float2*>(lam + o + nz)) : make_float2(0.f, 0.f);
-            ur[0] = u0.x; ur[1] = u0.y; ur[2] = u1r.x; ur[3] = u1r.y;
-            lv[0] = l0.x; lv[1] = l0.y; lv[2] = l1.x; lv[3] = l1.y;
-            float out[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float cbar = w * dphi_c(cpt[q]) * bpt[q] - kap * Lb[q] + 0.5f * acc[q];
-                out[q] = lv[q] + ((ur[q] >= 0.f && ur[q] <= 1.f) ? cbar : 0.f);
-            }
-            if (wj0) *reinterpret_cast<float2*>(lam_out + o) = make_float2(out[0], out[1]);
-            if (wj1) *reinterpret_cast<float2*>(lam_out + o + nz) = make_float2(out[2], out[3]);
+            // cbar = w*phi'(c)*mub - kappa*L(mub) + 0.5*acc; lam_s = lam' + [0<=u<=1]*cbar
+            const float2 cbA = fma2(mul2(w2, dphi2(A)), bA, fma2(mk2, LbA, mul2(f2s(0.5f), accA)));
+            const float2 cbB = fma2(mul2(w2, dphi2(B)), bB, fma2(mk2, LbB, mul2(f2s(0.5f), accB)));
+            const float2 oA = add2(l0, sel2(u0.x >= 0.f && u0.x <= 1.f, u0.y >= 0.f && u0.y <= 1.f, cbA));
+            const float2 oB = add2(l1, sel2(u1r.x >= 0.f && u1r.x <= 1.f, u1r.y >= 0.f && u1r.y <= 1.f, cbB));
+            if (wj0) *reinterpret_cast<float2*>(lam_out + o) = oA;
+            if (wj1) *reinterpret_cast<float2*>(lam_out + o + nz) = oB;
         }
-        if (GRADS) {
+        if (GR) {
             const float* cx = cs + ((i + 1) & 3) * T::FIELD;
-            const float2 up = lds2(cc + pa - W), dn = lds2(cc + pb + W);
-            const float2 cxA = lds2(cx + pa), cxB = lds2(cx + pb);
-            const float lc[4] = {
-                lap_f(G, A.x, c_prev[0], cxA.x, up.x, B.x, cc[pa - 1], A.y),
-                lap_f(G, A.y, c_prev[1], cxA.y, up.y, B.y, A.x, cc[pa + 2]),
-                lap_f(G, B.x, c_prev[2], cxB.x, A.x, dn.x, cc[pb - 1], B.y),
-                lap_f(G, B.y, c_prev[3], cxB.y, A.y, dn.y, B.x, cc[pb + 2])};
-            const bool okp[4] = {wj0, wj0, wj1, wj1};
+            const float2 lcA = lap2(L, A, c_prev[0], lds2(cx + pa), up, B, zmA, zpA);
+            const float2 lcB = lap2(L, B, c_prev[1], lds2(cx + pb), A, dn, zmB, zpB);
+            if (wj0) {
+                aK = fma2(mul2(f2s(-1.f), bA), lcA, aK);
+                aW = fma2(bA, phi2(A), aW);
+            }
+            if (wj1) {
+                aK = fma2(mul2(f2s(-1.f), bB), lcB, aK);
+                aW = fma2(bB, phi2(B), aW);
+            }
             if (GR == 1) {
-                const float2 h0 = wj0 ? __ldg(reinterpret_cast<const float2*>(hfield + o)) : make_float2(0.f, 0.f);
-                const float2 h1 = wj1 ? __ldg(reinterpret_cast<const float2*>(hfield + o + nz)) : make_float2(0.f, 0.f);
-                const float2 n0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u1 + o)) : make_float2(0.f, 0.f);
-                const float2 n1 = wj1 ? __ldg(reinterpret_cast<const float2*>(u1 + o + nz)) : make_float2(0.f, 0.f);
-                const float hv[4] = {h0.x, h0.y, h1.x, h1.y}, nv[4] = {n0.x, n0.y, n1.x, n1.y};
-                const float invD = 1.f / P.D;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (!okp[q]) continue;
-                    // <g, r/D> = <P lam', r>/D = <lam', u' - u>/D  (P is symmetric)
-                    sD += lv[q] * (nv[q] - ur[q]) * invD;
-                    sH += hv[q] * (nv[q] - ur[q]);
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                if (!okp[q]) continue;
-                sK -= bpt[q] * lc[q];
-                sW += bpt[q] * phi_c(cpt[q]);
+                const float2 invD = f2s(1.f / P.D);
+                const float2 h0 = wj0 ? __ldg(reinterpret_cast<const float2*>(hfield + o)) : f2s(0.f);
+                const float2 h1 = wj1 ? __ldg(reinterpret_cast<const float2*>(hfield + o + nz)) : f2s(0.f);
+                const float2 n0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u1 + o)) : f2s(0.f);
+                const float2 n1 = wj1 ? __ldg(reinterpret_cast<const float2*>(u1 + o + nz)) : f2s(0.f);
+                // <g, r/D> = <P lam', r>/D = <lam', u' - u>/D  (P is symmetric); zeros where a row is outside
+                aD = fma2(mul2(l0, sub2(n0, u0)), invD, aD);
+                aD = fma2(mul2(l1, sub2(n1, u1r)), invD, aD);
+                aH = fma2(h0, sub2(n0, u0), aH);
+                aH = fma2(h1, sub2(n1, u1r), aH);
             }
         }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            c_prev[q] = cpt[q];
-            b_prev[q] = bpt[q];
-        }
+        c_prev[0] = A;
+        c_prev[1] = B;
+        b_prev[0] = bA;
+        b_prev[1] = bB;
     };
 
     // prologue: planes x0-2 .. x0+1 staged; potentials x0-1, x0; carried x quantities
@@ -352,14 +303,14 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     compute_mu(x0 - 1);
     compute_mu(x0);
     __syncthreads();
-    x_faces_b(x0 - 1, cfx_m, Fx_m);
+    x_faces_b(x0 - 1, cfx_m);
     {
         const float* cprev = cs + ((x0 - 1) & 3) * T::FIELD;
         const float* bprev = bs + ((x0 - 1) & 1) * T::POT;
-        const float2 a = lds2(cprev + pa), b = lds2(cprev + pb);
-        const float2 ba = lds2(bprev + pa - W), bbv = lds2(bprev + pb - W);
-        c_prev[0] = a.x; c_prev[1] = a.y; c_prev[2] = b.x; c_prev[3] = b.y;
-        b_prev[0] = ba.x; b_prev[1] = ba.y; b_prev[2] = bbv.x; b_prev[3] = bbv.y;
+        c_prev[0] = lds2(cprev + pa);
+        c_prev[1] = lds2(cprev + pb);
+        b_prev[0] = lds2(bprev + pa - W);
+        b_prev[1] = lds2(bprev + pb - W);
     }
     for (int i = x0; i < x1; ++i) {
         stash(i + 2);
@@ -369,7 +320,10 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         __syncthreads();
         compute_lam(i);
     }
-
+    sD += aD.x + aD.y;
+    sK += aK.x + aK.y;
+    sW += aW.x + aW.y;
+    sH += aH.x + aH.y;
 }
 
 template <class T, int GR>

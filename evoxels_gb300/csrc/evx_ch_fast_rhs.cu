@@ -18,10 +18,32 @@ namespace {
 
 using namespace fast;
 
+// Two z-adjacent points at a time with the two-lane fp32 instructions; every
+// lane performs exactly the scalar operations of lap7 / mu_hom / face_flux
+// (evx_common.cuh) in the same order, so results stay bit-identical.
+struct RhsK {   // broadcast constants
+    float2 ih2x, ih2y, ih2z, ih2sum, w, kappa, D, ihx, ihy, ihz;
+};
+__device__ __forceinline__ float2 lap7x2(const RhsK& K, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
+                                         float2 zm, float2 zp) {
+    float2 t = mul2(add2(xp, xm), K.ih2x);
+    t = add2(t, mul2(add2(yp, ym), K.ih2y));
+    t = add2(t, mul2(add2(zp, zm), K.ih2z));
+    return sub2(t, mul2(mul2(f2s(2.f), c), K.ih2sum));
+}
 // mu = w*c*(1-c)*(1-2c) - kappa*lap(c)
-__device__ __forceinline__ float mu_at(const Geo& G, const ChP& P, float c, float xm, float xp, float ym, float yp,
-                                       float zm, float zp) {
-    return __fsub_rn(mu_hom(P.w, c), __fmul_rn(P.kappa, lap7(G, c, xm, xp, ym, yp, zm, zp)));
+__device__ __forceinline__ float2 mu_x2(const RhsK& K, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
+                                        float2 zm, float2 zp) {
+    float2 h = mul2(K.w, c);
+    h = mul2(h, sub2(f2s(1.f), c));
+    h = mul2(h, sub2(f2s(1.f), mul2(f2s(2.f), c)));
+    return sub2(h, mul2(K.kappa, lap7x2(K, c, xm, xp, ym, yp, zm, zp)));
+}
+// (cf*(1-cf)) * ((mu_hi - mu_lo)*ih), cf = 0.5*(c_hi + c_lo)
+__device__ __forceinline__ float2 flux_x2(float2 clo, float2 chi, float2 mlo, float2 mhi, float2 ih) {
+    const float2 cf = mul2(f2s(0.5f), add2(chi, clo));
+    const float2 m = mul2(cf, sub2(f2s(1.f), cf));
+    return mul2(m, mul2(sub2(mhi, mlo), ih));
 }
 
 template <class T, bool FUSED>
@@ -49,7 +71,8 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
     const int ra = 2 + 2 * ty, rc = 4 + 2 * tx;    // field row / column in shared memory
     const int gj = j0 + 2 * ty, gk = k0 + 2 * tx;   // global y / z of the patch origin
     const bool wk = gk < nz, wj0 = gj < ny && wk, wj1 = gj + 1 < ny && wk;
-    const float ihx = G.ih[0], ihy = G.ih[1], ihz = G.ih[2];
+    const RhsK K{f2s(G.ih2[0]), f2s(G.ih2[1]), f2s(G.ih2[2]), f2s(G.ih2sum), f2s(P.w), f2s(P.kappa), f2s(P.D),
+                 f2s(G.ih[0]), f2s(G.ih[1]), f2s(G.ih[2])};
 
     float4 pf[2];
     auto fetch = [&](int p) {
@@ -61,7 +84,9 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
             float4 a = ldg4(u + base + LP.goff[s]);
             if (FUSED) {
                 const float4 d = ldg4(upd + base + LP.goff[s]);
-                a = make_float4(__fadd_rn(a.x, d.x), __fadd_rn(a.y, d.y), __fadd_rn(a.z, d.z), __fadd_rn(a.w, d.w));
+                const float2 lo = add2(make_float2(a.x, a.y), make_float2(d.x, d.y));
+                const float2 hi = add2(make_float2(a.z, a.w), make_float2(d.z, d.w));
+                a = make_float4(lo.x, lo.y, hi.x, hi.y);
                 if (own_plane && LP.own[s]) *reinterpret_cast<float4*>(u_new + base + LP.goff[s]) = a;
             }
             pf[s] = a;
@@ -83,67 +108,54 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
             if (!mv[m]) continue;
             const int a = mr[m] * W + mc[m], b = a + W;
             const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
-            const float Al = cc[a - 1], Ar = cc[a + 2], Bl = cc[b - 1], Br = cc[b + 2];
-            const float2 xmA = lds2(cm + a), xmB = lds2(cm + b), xpA = lds2(cp + a), xpB = lds2(cp + b);
-            const float m00 = mu_at(G, P, A.x, xmA.x, xpA.x, up.x, B.x, Al, A.y);
-            const float m01 = mu_at(G, P, A.y, xmA.y, xpA.y, up.y, B.y, A.x, Ar);
-            const float m10 = mu_at(G, P, B.x, xmB.x, xpB.x, A.x, dn.x, Bl, B.y);
-            const float m11 = mu_at(G, P, B.y, xmB.y, xpB.y, A.y, dn.y, B.x, Br);
-            sts2(mo + a - W, m00, m01);   // potential row = field row - 1
-            sts2(mo + b - W, m10, m11);
+            const float2 zmA = make_float2(cc[a - 1], A.x), zpA = make_float2(A.y, cc[a + 2]);
+            const float2 zmB = make_float2(cc[b - 1], B.x), zpB = make_float2(B.y, cc[b + 2]);
+            // potential row = field row - 1
+            *reinterpret_cast<float2*>(mo + a - W) = mu_x2(K, A, lds2(cm + a), lds2(cp + a), up, B, zmA, zpA);
+            *reinterpret_cast<float2*>(mo + b - W) = mu_x2(K, B, lds2(cm + b), lds2(cp + b), A, dn, zmB, zpB);
         }
     };
 
-    float fxm[4] = {0.f, 0.f, 0.f, 0.f};   // x flux on the face below the current plane
-    auto x_faces = [&](int plo, float out[4]) {
+    float2 fxm[2] = {f2s(0.f), f2s(0.f)};   // x flux on the face below the current plane (rows a, b)
+    auto x_faces = [&](int plo, float2 out[2]) {
         const float* c0 = cs + (plo & 3) * T::FIELD;
         const float* c1 = cs + ((plo + 1) & 3) * T::FIELD;
         const float* m0 = ms + (plo & 1) * T::POT;
         const float* m1 = ms + ((plo + 1) & 1) * T::POT;
         const int a = ra * W + rc, b = a + W;
-        const float2 cA0 = lds2(c0 + a), cB0 = lds2(c0 + b), cA1 = lds2(c1 + a), cB1 = lds2(c1 + b);
-        const float2 mA0 = lds2(m0 + a - W), mB0 = lds2(m0 + b - W), mA1 = lds2(m1 + a - W), mB1 = lds2(m1 + b - W);
-        out[0] = face_flux(cA0.x, cA1.x, mA0.x, mA1.x, ihx);
-        out[1] = face_flux(cA0.y, cA1.y, mA0.y, mA1.y, ihx);
-        out[2] = face_flux(cB0.x, cB1.x, mB0.x, mB1.x, ihx);
-        out[3] = face_flux(cB0.y, cB1.y, mB0.y, mB1.y, ihx);
+        out[0] = flux_x2(lds2(c0 + a), lds2(c1 + a), lds2(m0 + a - W), lds2(m1 + a - W), K.ihx);
+        out[1] = flux_x2(lds2(c0 + b), lds2(c1 + b), lds2(m0 + b - W), lds2(m1 + b - W), K.ihx);
     };
 
     auto compute_r = [&](int i) {
         const float* cc = cs + (i & 3) * T::FIELD;
         const float* mm = ms + (i & 1) * T::POT;
         const int a = ra * W + rc, b = a + W;     // field offsets; potential offsets are one row up
-        float fxp[4];
+        float2 fxp[2];
         x_faces(i, fxp);
         const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
-        const float Al = cc[a - 1], Ar = cc[a + 2], Bl = cc[b - 1], Br = cc[b + 2];
         const float2 mup = lds2(mm + a - 2 * W), MA = lds2(mm + a - W), MB = lds2(mm + b - W), mdn = lds2(mm + b);
-        const float MAl = mm[a - W - 1], MAr = mm[a - W + 2], MBl = mm[b - W - 1], MBr = mm[b - W + 2];
-        // z faces
-        const float za0 = face_flux(Al, A.x, MAl, MA.x, ihz), za1 = face_flux(A.x, A.y, MA.x, MA.y, ihz);
-        const float za2 = face_flux(A.y, Ar, MA.y, MAr, ihz);
-        const float zb0 = face_flux(Bl, B.x, MBl, MB.x, ihz), zb1 = face_flux(B.x, B.y, MB.x, MB.y, ihz);
-        const float zb2 = face_flux(B.y, Br, MB.y, MBr, ihz);
-        // y faces
-        const float y0x = face_flux(up.x, A.x, mup.x, MA.x, ihy), y1x = face_flux(A.x, B.x, MA.x, MB.x, ihy);
-        const float y2x = face_flux(B.x, dn.x, MB.x, mdn.x, ihy);
-        const float y0y = face_flux(up.y, A.y, mup.y, MA.y, ihy), y1y = face_flux(A.y, B.y, MA.y, MB.y, ihy);
-        const float y2y = face_flux(B.y, dn.y, MB.y, mdn.y, ihy);
-        auto divr = [&](float fxp_, float fxm_, float fyp, float fym, float fzp, float fzm) {
-            float d = __fmul_rn(__fsub_rn(fxp_, fxm_), ihx);
-            d = __fadd_rn(d, __fmul_rn(__fsub_rn(fyp, fym), ihy));
-            d = __fadd_rn(d, __fmul_rn(__fsub_rn(fzp, fzm), ihz));
-            return __fmul_rn(P.D, d);
+        // z faces (left, mid) and (mid, right) of each row
+        const float2 zlA = flux_x2(make_float2(cc[a - 1], A.x), A, make_float2(mm[a - W - 1], MA.x), MA, K.ihz);
+        const float2 zhA = flux_x2(A, make_float2(A.y, cc[a + 2]), MA, make_float2(MA.y, mm[a - W + 2]), K.ihz);
+        const float2 zlB = flux_x2(make_float2(cc[b - 1], B.x), B, make_float2(mm[b - W - 1], MB.x), MB, K.ihz);
+        const float2 zhB = flux_x2(B, make_float2(B.y, cc[b + 2]), MB, make_float2(MB.y, mm[b - W + 2]), K.ihz);
+        // y faces above, between and below the two rows
+        const float2 y0 = flux_x2(up, A, mup, MA, K.ihy), y1 = flux_x2(A, B, MA, MB, K.ihy);
+        const float2 y2 = flux_x2(B, dn, MB, mdn, K.ihy);
+        auto divr = [&](float2 fxp_, float2 fxm_, float2 fyp, float2 fym, float2 fzp, float2 fzm) {
+            float2 d = mul2(sub2(fxp_, fxm_), K.ihx);
+            d = add2(d, mul2(sub2(fyp, fym), K.ihy));
+            d = add2(d, mul2(sub2(fzp, fzm), K.ihz));
+            return mul2(K.D, d);
         };
-        const float r00 = divr(fxp[0], fxm[0], y1x, y0x, za1, za0);
-        const float r01 = divr(fxp[1], fxm[1], y1y, y0y, za2, za1);
-        const float r10 = divr(fxp[2], fxm[2], y2x, y1x, zb1, zb0);
-        const float r11 = divr(fxp[3], fxm[3], y2y, y1y, zb2, zb1);
+        const float2 rA = divr(fxp[0], fxm[0], y1, y0, zhA, zlA);
+        const float2 rB = divr(fxp[1], fxm[1], y2, y1, zhB, zlB);
         const size_t o = (size_t)i * plane + (size_t)gj * nz + gk;
-        if (wj0) *reinterpret_cast<float2*>(r + o) = make_float2(r00, r01);
-        if (wj1) *reinterpret_cast<float2*>(r + o + nz) = make_float2(r10, r11);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) fxm[q] = fxp[q];
+        if (wj0) *reinterpret_cast<float2*>(r + o) = rA;
+        if (wj1) *reinterpret_cast<float2*>(r + o + nz) = rB;
+        fxm[0] = fxp[0];
+        fxm[1] = fxp[1];
     };
 
     // prologue: field planes x0-2 .. x0+1, potentials x0-1 and x0, first x face
