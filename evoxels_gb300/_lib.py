@@ -69,6 +69,7 @@ _SIGS = {
     "evx_fe_update": (C.c_int, [_P, _P, C.c_float, _P, C.c_size_t, _P]),
     "evx_ch_rhs": (C.c_int, [_P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.POINTER(EvxChParams), _P]),
     "evx_ch_plan_create": (C.c_int, [C.POINTER(_P), C.POINTER(EvxGrid), C.c_int]),
+    "evx_ch_plan_create_bc": (C.c_int, [C.POINTER(_P), C.POINTER(EvxGrid), C.POINTER(EvxBC), C.c_int]),
     "evx_ch_plan_destroy": (C.c_int, [_P]),
     "evx_ch_workspace_bytes": (C.c_size_t, [_P]),
     "evx_ch_step": (C.c_int, [_P, _P, _P, C.POINTER(EvxChParams), _P, _P]),

@@ -283,6 +283,7 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
     if ((reinterpret_cast<uintptr_t>(lam_in) | reinterpret_cast<uintptr_t>(lam_out)) & 15)
         return fail(EVX_ERR_BAD_ARG, "lam_in and lam_out must be 16-byte aligned");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
+    if (plan->xext) return fail(EVX_ERR_UNSUPPORTED, "the adjoint of the mirrored-x spectral step is not built");
     const bool want = grads != nullptr;
     const bool spectral = want && spectra != nullptr;
     if (spectral) {

@@ -182,6 +182,17 @@ __global__ void ch_axpy_kernel(const float* __restrict__ u, const float* __restr
     if (nonfinite && __any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(nonfinite, 1);
 }
 
+// Mirror extension along x of the rhs (evoxels/boundary_conditions.py:64-70):
+// r[nx + j] = sign * r[nx - 1 - j] for j in [0, nx), sign +1 (Neumann) or -1
+// (Dirichlet); r holds 2*nx planes of `plane` floats.
+__global__ void ch_mirror_x_kernel(float* __restrict__ r, int nx, size_t plane, float sign) {
+    const size_t half = (size_t)nx * plane, stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < half; e += stride) {
+        const size_t j = e / plane, yz = e - j * plane;
+        r[half + e] = sign * r[((size_t)nx - 1 - j) * plane + yz];
+    }
+}
+
 // spec[i,j,k] = (spec * prefac) * invN, prefac = dt * (1/(1 - dt*(sym_coef*k4)))
 // (evoxels/timesteppers.py:77,87 and torch's 1/N "backward" irfftn scaling).
 __global__ void ch_kspace_fwd_kernel(float2* __restrict__ spec, int ny, int nzh, size_t total,
@@ -274,7 +285,7 @@ int ch_c2r(evx_ch_plan* plan, float2* in, float* out, bool batch2, cudaStream_t 
 }
 
 int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st, float2* dspec) {
-    const float invN = (float)(1.0 / (double)plan->n);
+    const float invN = (float)(1.0 / ((double)plan->nxe * plan->g.ny * plan->g.nz));
     if (plan->xmode) {
         XpassArgs a = xpass_args(plan, 0, spec, P);
         a.dspec = dspec;
@@ -327,15 +338,37 @@ int evx_ch_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc, co
 }
 
 int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
+    return evx_ch_plan_create_bc(out, g, nullptr, flags);
+}
+
+int evx_ch_plan_create_bc(evx_ch_plan** out, const evx_grid* g, const evx_bc* bc, int flags) {
     if (!out) return fail(EVX_ERR_BAD_ARG, "plan pointer is NULL");
     *out = nullptr;
     int rc = validate_grid(g);
     if (rc) return rc;
+    int xext = 0;
+    if (bc) {
+        if ((rc = validate_bc(bc))) return rc;
+        const int nonper = (bc->kind[0] != EVX_BC_PERIODIC) + (bc->kind[1] != EVX_BC_PERIODIC) +
+                           (bc->kind[2] != EVX_BC_PERIODIC);
+        if (nonper > 1)
+            return fail(EVX_ERR_BAD_BC, "FFT-based timesteppers currently support at most one non-periodic axis");
+        if (nonper == 1 && bc->kind[0] == EVX_BC_PERIODIC)
+            return fail(EVX_ERR_UNSUPPORTED, "FFT-based timesteppers currently only implement the single "
+                                             "non-periodic axis case for x");
+        xext = bc->kind[0] == EVX_BC_NEUMANN ? 1 : (bc->kind[0] == EVX_BC_DIRICHLET ? 2 : 0);
+    }
     evx_ch_plan* p = new evx_ch_plan();
     p->g = *g;
+    p->xext = xext;
+    p->nxe = xext ? 2 * g->nx : g->nx;
+    if (bc) p->bc = *bc;
+    else for (int a = 0; a < 3; ++a) { p->bc.kind[a] = EVX_BC_PERIODIC; p->bc.two_v_lo[a] = p->bc.two_v_hi[a] = 0.f; }
     p->nzh = g->nz / 2 + 1;
     p->n = field_elems(g);
-    p->nspec = (size_t)g->nx * g->ny * p->nzh;
+    // the x-pass keeps nx planes of the (y, z) spectrum; cuFFT's 3-D transform all nxe
+    const bool xmode = xpass_supported(p->nxe) && !(flags & 2);
+    p->nspec = (size_t)(xmode ? g->nx : p->nxe) * g->ny * p->nzh;
     size_t w1 = 0, w2 = 0, w3 = 0;
     auto cleanup = [&](int code) {
         if (p->r2c) cufftDestroy(p->r2c);
@@ -347,12 +380,14 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
     };
     if (p->nspec > 2147483647ull || 2 * p->n > 2147483647ull)
         return cleanup(fail(EVX_ERR_TOO_LARGE, "grid too large for 32-bit cuFFT plans"));
+    if (xext && (flags & 1))
+        return cleanup(fail(EVX_ERR_UNSUPPORTED, "parameter gradients of the mirrored-x spectral step are not built"));
     if ((rc = check_cufft(cufftCreate(&p->r2c), "cufftCreate"))) return cleanup(rc);
     if ((rc = check_cufft(cufftCreate(&p->c2r), "cufftCreate"))) return cleanup(rc);
     cufftSetAutoAllocation(p->r2c, 0);
     cufftSetAutoAllocation(p->c2r, 0);
     // power-of-two nx: cuFFT transforms (y, z) for every x plane and the fused x-pass does the rest
-    p->xmode = xpass_supported(g->nx) && !(flags & 2);
+    p->xmode = xmode;
     p->yzmode = p->xmode && yz_supported(g->ny, g->nz) && (flags & 4);
     if (p->xmode) {
         int d2[2] = {g->ny, g->nz};
@@ -364,9 +399,9 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
                               "cufftMakePlanMany C2R (y,z)")))
             return cleanup(rc);
     } else {
-        if ((rc = check_cufft(cufftMakePlan3d(p->r2c, g->nx, g->ny, g->nz, CUFFT_R2C, &w1), "cufftMakePlan3d R2C")))
+        if ((rc = check_cufft(cufftMakePlan3d(p->r2c, p->nxe, g->ny, g->nz, CUFFT_R2C, &w1), "cufftMakePlan3d R2C")))
             return cleanup(rc);
-        if ((rc = check_cufft(cufftMakePlan3d(p->c2r, g->nx, g->ny, g->nz, CUFFT_C2R, &w2), "cufftMakePlan3d C2R")))
+        if ((rc = check_cufft(cufftMakePlan3d(p->c2r, p->nxe, g->ny, g->nz, CUFFT_C2R, &w2), "cufftMakePlan3d C2R")))
             return cleanup(rc);
     }
     if (flags & 1) {
@@ -387,11 +422,11 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
         p->has_c2r2 = true;
     }
     p->ws_fft = std::max(w1, std::max(w2, w3));
-    // k^2 tables, bit-identical to the reference's float32 k-grid
-    const size_t nt = (size_t)g->nx + g->ny + p->nzh;
+    // k^2 tables, bit-identical to the reference's float32 k-grid (2*nx x points when mirrored)
+    const size_t nt = (size_t)p->nxe + g->ny + p->nzh;
     float* host = new float[nt];
-    rc = evx_k2_tables_host(g->nx, g->ny, g->nz, g->h[0], g->h[1], g->h[2], host, host + g->nx,
-                            host + g->nx + g->ny);
+    rc = evx_k2_tables_host(p->nxe, g->ny, g->nz, g->h[0], g->h[1], g->h[2], host, host + p->nxe,
+                            host + p->nxe + g->ny);
     if (rc) { delete[] host; return cleanup(rc); }
     if ((rc = check_cuda(cudaMalloc(&p->kx2, nt * sizeof(float)), "cudaMalloc k2 tables"))) {
         delete[] host;
@@ -400,7 +435,7 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
     rc = check_cuda(cudaMemcpy(p->kx2, host, nt * sizeof(float), cudaMemcpyHostToDevice), "cudaMemcpy k2 tables");
     delete[] host;
     if (rc) return cleanup(rc);
-    p->ky2 = p->kx2 + g->nx;
+    p->ky2 = p->kx2 + p->nxe;
     p->kz2 = p->ky2 + g->ny;
     // workspace layout
     dim3 sg; int lx;
@@ -408,14 +443,17 @@ int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
     p->n_part = std::max((int)(sg.x * sg.y * sg.z), ch_pullback_fast_blocks(g));
     size_t off = 0;
     p->off_fft = off;  off += align256(p->ws_fft);
+    // r: 2 fields (rhs extended to 2*nx planes; g and h in the adjoint); update: the
+    // whole 2*nx-plane inverse transform on the cuFFT 3-D mirrored path
+    const size_t upd_fields = (xext && !xmode) ? 2 : 1;
     p->off_r = off;    off += align256(2 * p->n * sizeof(float));
-    p->off_upd = off;  off += align256(p->n * sizeof(float));
+    p->off_upd = off;  off += align256(upd_fields * p->n * sizeof(float));
     p->off_spec = off; off += align256(2 * p->nspec * sizeof(float2));
     p->off_u = off;    off += align256(p->n * sizeof(float));
     p->off_lam = off;  off += align256(p->n * sizeof(float));
     p->off_part = off; off += align256((size_t)p->n_part * 4 * sizeof(double));
-    p->n_xpart = p->xmode ? xpass_blocks(g->nx, g->ny * p->nzh) : 0;
-    p->spec_floats = p->xmode ? xpass_spectrum_floats(g->nx, g->ny * p->nzh) : 0;
+    p->n_xpart = p->xmode && !xext ? xpass_blocks(g->nx, g->ny * p->nzh) : 0;
+    p->spec_floats = p->xmode && !xext ? xpass_spectrum_floats(g->nx, g->ny * p->nzh) : 0;
     p->off_xpart = off; off += align256(p->n_xpart * 2 * sizeof(double));
     p->total = off;
     *out = p;
@@ -460,7 +498,7 @@ int evx_ch_forward_spectra(evx_ch_plan* plan, const float* u_in, float* u_out, i
                           "evx_ch_forward copy");
     if ((rc = ch_plan_bind(plan, workspace, st, false))) return rc;
     const evx_grid* g = &plan->g;
-    const Geo G = make_geo(g, nullptr);   // the spectral step is periodic
+    const Geo G = make_geo(g, &plan->bc);
     const ChP P = make_chp(prm);
     float* r = reinterpret_cast<float*>(ws_at(workspace, plan->off_r));
     float* upd = reinterpret_cast<float*>(ws_at(workspace, plan->off_upd));
@@ -476,6 +514,12 @@ int evx_ch_forward_spectra(evx_ch_plan* plan, const float* u_in, float* u_out, i
             src = dst;
         }
         if (rc) return rc;
+        if (plan->xext && !plan->xmode) {   // cuFFT 3-D path: extend the rhs to 2*nx planes
+            EVX_TIMED("ch_mirror_x", st, ch_mirror_x_kernel<<<elementwise_grid(N), 256, 0, st>>>(
+                r, g->nx, (size_t)g->ny * g->nz, plan->xext == 2 ? -1.f : 1.f));
+            count_launch();
+            if ((rc = check_launch("ch_mirror_x_kernel"))) return rc;
+        }
         if ((rc = ch_r2c(plan, r, spec, st))) return rc;
         float2* ds = spectra ? reinterpret_cast<float2*>(spectra + (size_t)s * plan->spec_floats) : nullptr;
         if ((rc = ch_kspace_forward(plan, spec, P, st, ds))) return rc;

@@ -8,9 +8,12 @@
 
 struct evx_ch_plan {
     evx_grid g;
+    evx_bc bc;               // the problem's BCs (y, z periodic; x periodic, Neumann or Dirichlet)
+    int xext = 0;            // x mirror extension of the spectral step: 0 none, 1 even (Neumann), 2 odd (Dirichlet)
+    int nxe;                 // transform length along x (2*nx with the extension)
     int nzh;                 // nz/2 + 1
     size_t n;                // nx*ny*nz
-    size_t nspec;            // nx*ny*nzh complex values
+    size_t nspec;            // complex values of the spectrum buffer (nxe*ny*nzh; nx*ny*nzh with the x-pass)
     cufftHandle r2c = 0, c2r = 0, c2r2 = 0;
     bool has_c2r2 = false;
     bool xmode = false;      // (y, z) transforms batched over x + fused x-pass (power-of-two nx)
@@ -73,6 +76,7 @@ struct XpassArgs {
     const float *kx2, *ky2, *kz2;
     float sym, dt, invN;
     int* n_xpart_out;                  // optional: partial-sum slots written (mode 3)
+    int ext;                           // x mirror extension (mode 0): 1 even, 2 odd; nx = transform length / 2
 };
 bool xpass_supported(int nx);
 size_t xpass_blocks(int nx, int M);
@@ -80,10 +84,12 @@ size_t xpass_spectrum_floats(int nx, int M);
 int xpass_launch(const XpassArgs& a, cudaStream_t st);
 inline XpassArgs xpass_args(const evx_ch_plan* plan, int mode, float2* spec, const ChP& P) {
     XpassArgs a{};
-    a.mode = mode; a.nx = plan->g.nx; a.M = plan->g.ny * plan->nzh; a.nzh = plan->nzh; a.nz = plan->g.nz;
+    a.mode = mode; a.nx = plan->nxe; a.M = plan->g.ny * plan->nzh; a.nzh = plan->nzh; a.nz = plan->g.nz;
     a.spec = spec;
     a.kx2 = plan->kx2; a.ky2 = plan->ky2; a.kz2 = plan->kz2;
-    a.sym = P.sym_coef; a.dt = P.dt; a.invN = (float)(1.0 / (double)plan->n);
+    a.sym = P.sym_coef; a.dt = P.dt;
+    a.invN = (float)(1.0 / ((double)plan->nxe * plan->g.ny * plan->g.nz));
+    a.ext = plan->xext;
     return a;
 }
 

@@ -140,8 +140,11 @@ __device__ __forceinline__ void block_sum2(float t1, float t2, double* out) {
 // ---- per-tile kernel (plain loads and stores) -------------------------------------
 // MODE 0 forward (dspec: optional store of the increment spectrum), 1 adjoint (g),
 // 2 adjoint (g and h into spec_h), 3 adjoint (g and the two Parseval sums
-// against dspec into xpart[2*block .. 2*block+1])
-template <int N1, int N2, int MODE>
+// against dspec into xpart[2*block .. 2*block+1]).  EXT 1 / 2: the spectrum
+// holds N/2 x rows and the transformed sequence is its even / odd mirror
+// extension, x' = N-1-x for x >= N/2 (the mirrored-x step of a Neumann /
+// Dirichlet x axis); only the first N/2 rows are written back.
+template <int N1, int N2, int MODE, int EXT = 0>
 __global__ void __launch_bounds__(256, MODE == 2 ? 2 : EVX_XPASS_MIN_BLOCKS)
 xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __restrict__ dspec,
              double* __restrict__ xpart, int M, int nzh, int nz,
@@ -160,17 +163,28 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
     float2* dsp = dspec ? dspec + (size_t)blockIdx.x * N1 * 256 + tid : nullptr;
     float t1 = 0.f, t2 = 0.f;
 
+    constexpr int NH = (N1 * N2) / 2;   // physical rows with EXT
     float2 v[N1];
 #pragma unroll
-    for (int n1 = 0; n1 < N1; ++n1)
-        v[n1] = live ? spec[(size_t)(N2 * n1 + c.n2) * M + m] : make_float2(0.f, 0.f);
+    for (int n1 = 0; n1 < N1; ++n1) {
+        const int x = N2 * n1 + c.n2;
+        if (EXT && x >= NH) {
+            const float2 w = live ? spec[(size_t)(2 * NH - 1 - x) * M + m] : make_float2(0.f, 0.f);
+            v[n1] = EXT == 2 ? make_float2(-w.x, -w.y) : w;
+        } else {
+            v[n1] = live ? spec[(size_t)x * M + m] : make_float2(0.f, 0.f);
+        }
+    }
     fwd_stage1<N1, N2>(v, xs, c);
     float2 hv[MODE == 2 ? N1 : 1];
     mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2);
     auto store = [&](float2* dst) {
         if (live) {
 #pragma unroll
-            for (int n1 = 0; n1 < N1; ++n1) dst[(size_t)(N2 * n1 + c.n2) * M + m] = v[n1];
+            for (int n1 = 0; n1 < N1; ++n1) {
+                const int x = N2 * n1 + c.n2;
+                if (!EXT || x < NH) dst[(size_t)x * M + m] = v[n1];
+            }
         }
     };
     inv_stage1<N1, N2>(v, xs, c);
@@ -339,13 +353,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-template <int N1, int N2, int MODE>
+template <int N1, int N2, int MODE, int EXT = 0>
 int xpass_launch_tile(const XpassArgs& A, cudaStream_t st, const char* slot) {
     constexpr int P = 256 / N2;
     const size_t smem = (size_t)N1 * N2 * P * sizeof(float2);
     static bool attr = false;   // one flag per instantiation
     if (!attr) {
-        const int rc = check_cuda(cudaFuncSetAttribute(xpass_kernel<N1, N2, MODE>,
+        const int rc = check_cuda(cudaFuncSetAttribute(xpass_kernel<N1, N2, MODE, EXT>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                                   "x-pass shared memory attribute");
         if (rc) return rc;
@@ -354,8 +368,9 @@ int xpass_launch_tile(const XpassArgs& A, cudaStream_t st, const char* slot) {
     const int blocks = (A.M + P - 1) / P;
     if (A.n_xpart_out) *A.n_xpart_out = blocks;
     EVX_TIMED(slot, st,
-              xpass_kernel<N1, N2, MODE><<<blocks, 256, smem, st>>>(A.spec, A.spec_h, A.dspec, A.xpart, A.M, A.nzh,
-                                                                  A.nz, A.kx2, A.ky2, A.kz2, A.sym, A.dt, A.invN));
+              (xpass_kernel<N1, N2, MODE, EXT><<<blocks, 256, smem, st>>>(A.spec, A.spec_h, A.dspec, A.xpart, A.M,
+                                                                        A.nzh, A.nz, A.kx2, A.ky2, A.kz2, A.sym,
+                                                                        A.dt, A.invN)));
     count_launch();
     return check_launch("xpass_kernel");
 }
@@ -413,6 +428,11 @@ int xpass_launch_m(const XpassArgs& A, cudaStream_t st) {
 
 template <int N1, int N2>
 int xpass_launch_t(const XpassArgs& A, cudaStream_t st) {
+    if (A.ext) {   // mirrored-x forward step: per-tile kernel (odd or even extension)
+        if (A.mode != 0 || A.dspec) return fail(EVX_ERR_UNSUPPORTED, "mirrored-x x-pass: forward only");
+        return A.ext == 2 ? xpass_launch_tile<N1, N2, 0, 2>(A, st, "ch_xpass_fwd_mirror")
+                          : xpass_launch_tile<N1, N2, 0, 1>(A, st, "ch_xpass_fwd_mirror");
+    }
     switch (A.mode) {
         case 0: return xpass_launch_m<N1, N2, 0>(A, st);
         case 1: return xpass_launch_m<N1, N2, 1>(A, st);

@@ -93,15 +93,25 @@ class _BCMixin:
             raise NotImplementedError(
                 "FFT-based timesteppers currently only implement the single non-periodic axis "
                 f"case for x; got {self.bc_type}. Axis permutation is not implemented yet.")
-        if len(nonperiodic) == 1:
-            raise NotImplementedError("evoxels_gb300 implements the periodic spectral step only; "
-                                      "the mirrored-x extension for non-periodic x is not built")
-        self._pad_fft_bc = self.vg.bc.pad_fft_periodic
+        x_bc = self.bc_type[0]
+        if x_bc == "periodic":
+            self._pad_fft_bc = self.vg.bc.pad_fft_periodic
+        elif x_bc == "dirichlet":
+            self._pad_fft_bc = self.vg.bc.pad_fft_dirichlet_periodic
+        elif x_bc == "neumann":
+            self._pad_fft_bc = self.vg.bc.pad_fft_zero_flux_periodic
+        else:
+            raise ValueError("FFT-based timesteppers only support periodic, dirichlet, or "
+                             f"neumann boundary conditions in x, got {x_bc}.")
 
     def pad_fft_bc(self, u):
         return self._pad_fft_bc(u)
 
     def k_squared(self):
+        """(evoxels/problem_definition.py:169-177): the mirrored grid's k^2 for a
+        Neumann or Dirichlet x axis."""
+        if self.bc_type[0] in ("dirichlet", "neumann"):
+            return self.vg.rfft_k_squared_nonperiodic()
         return self.vg.rfft_k_squared()
 
 

@@ -19,20 +19,24 @@ import torch
 
 from . import _lib
 from .problem_definition import CahnHilliard, ReactionDiffusion
-from .voxelgrid import cuda_stream
+from .voxelgrid import cuda_stream, evx_bc
 
 
 class ChPlan:
     """An ``evx_ch_plan`` plus its device workspace (one per grid shape/spacing/device)."""
 
-    def __init__(self, vg, grads=False, cufft3d=False, fused_yz=False):
+    def __init__(self, vg, grads=False, cufft3d=False, fused_yz=False, bc=None):
         self.vg = vg
         self.grid = vg.evx_grid()
         self.grads = grads
         h = C.c_void_p()
         flags = (1 if grads else 0) | (2 if cufft3d else 0) | (4 if fused_yz else 0)
         with torch.cuda.device(vg.device):
-            _lib.check(_lib.lib().evx_ch_plan_create(C.byref(h), self.grid, flags), "evx_ch_plan_create")
+            if bc is None:
+                _lib.check(_lib.lib().evx_ch_plan_create(C.byref(h), self.grid, flags), "evx_ch_plan_create")
+            else:   # normalised BC tuple: the mirrored-x step for a non-periodic x axis
+                _lib.check(_lib.lib().evx_ch_plan_create_bc(C.byref(h), self.grid, evx_bc(bc), flags),
+                           "evx_ch_plan_create_bc")
         self.handle = h
         nbytes = int(_lib.lib().evx_ch_workspace_bytes(h))
         self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=vg.device)
@@ -51,15 +55,19 @@ _plan_lock = threading.Lock()
 _plans = {}
 
 
-def get_plan(vg, grads=False, cufft3d=False, fused_yz=False):
+def get_plan(vg, grads=False, cufft3d=False, fused_yz=False, bc=None):
     """Cached plan per grid; ``cufft3d`` forces cuFFT's 3-D transforms instead of the
     (y, z) transforms plus the fused x-pass used for power-of-two ``Nx``; ``fused_yz``
-    replaces cuFFT's (y, z) transforms by the fused cluster kernels (opt-in)."""
-    key = (vg.shape, vg.spacing, str(vg.device), bool(grads), bool(cufft3d), bool(fused_yz))
+    replaces cuFFT's (y, z) transforms by the fused cluster kernels (opt-in); ``bc``
+    (normalised BC tuple) selects the mirrored-x step for a non-periodic x axis."""
+    if bc is not None and all(kind == "periodic" for kind, _ in bc):
+        bc = None
+    bkey = None if bc is None else tuple((k, tuple(float(x) for x in v) if v is not None else None) for k, v in bc)
+    key = (vg.shape, vg.spacing, str(vg.device), bool(grads), bool(cufft3d), bool(fused_yz), bkey)
     with _plan_lock:
         p = _plans.get(key)
         if p is None:
-            p = ChPlan(vg, grads, cufft3d, fused_yz)
+            p = ChPlan(vg, grads, cufft3d, fused_yz, bc)
             _plans[key] = p
         return p
 
@@ -91,7 +99,7 @@ class PseudoSpectralIMEX(TimeStepper):
             raise NotImplementedError("evoxels_gb300's spectral step is implemented for CahnHilliard")
         self.problem.verify_fft_bc_config()
         self.pad = self.problem.pad_fft_bc
-        self._plan = get_plan(self.problem.vg)
+        self._plan = get_plan(self.problem.vg, bc=self.problem.bc)
         self._params = self.problem.evx_params(self.dt)
         self._nonfinite = None
 

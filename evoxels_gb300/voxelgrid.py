@@ -89,6 +89,14 @@ class CellCenteredBCs:
     def pad_fft_periodic(self, field):
         return field
 
+    def pad_fft_dirichlet_periodic(self, field):
+        """Pad with the negated x-flipped field (evoxels/boundary_conditions.py:64-66)."""
+        return torch.cat((field, -torch.flip(field, [1])), 1)
+
+    def pad_fft_zero_flux_periodic(self, field):
+        """Pad with the x-flipped field (evoxels/boundary_conditions.py:68-70)."""
+        return torch.cat((field, torch.flip(field, [1])), 1)
+
     def trim_boundary_nodes(self, field):
         return field
 
@@ -156,6 +164,14 @@ class VoxelGridGB300:
 
     def rfft_k_squared(self):
         a_x, a_y, _ = self.fft_axes()
+        _, _, a_z = self.rfft_axes()
+        kx, ky, kz = torch.meshgrid(a_x, a_y, a_z, indexing="ij")
+        return kx ** 2 + ky ** 2 + kz ** 2
+
+    def rfft_k_squared_nonperiodic(self):
+        """k^2 of the x-mirrored grid, 2*Nx points along x (evoxels/voxelgrid.py:116-124)."""
+        a_x = 2 * torch.pi * torch.fft.fftfreq(2 * self.shape[0], d=self.spacing[0], device=self.device)
+        _, a_y, _ = self.fft_axes()
         _, _, a_z = self.rfft_axes()
         kx, ky, kz = torch.meshgrid(a_x, a_y, a_z, indexing="ij")
         return kx ** 2 + ky ** 2 + kz ** 2

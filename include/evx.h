@@ -137,6 +137,18 @@ typedef struct evx_ch_plan evx_ch_plan;
  * default a power-of-two nx uses cuFFT over (y, z) and a fused x-pass that
  * does the x transforms and the k-space multiply in one read and write). */
 int evx_ch_plan_create(evx_ch_plan** plan, const evx_grid* g, int flags);
+/* Same for a problem with boundary conditions bc (NULL = periodic): y and z
+ * periodic, x periodic, Neumann or Dirichlet.  A non-periodic x axis runs the
+ * reference's mirrored step (evoxels/boundary_conditions.py:64-70,
+ * evoxels/voxelgrid.py:116-124, evoxels/timesteppers.py:85-89): the rhs with the
+ * BC ghosts, extended along x by its mirror image (Neumann) or the negated
+ * mirror image (Dirichlet) to 2*nx, transformed with the 2*nx-point k-grid,
+ * and trimmed back to nx.  Power-of-two nx <= 256 do the extension inside the
+ * x-pass (no extra HBM traffic); others run cuFFT over (2*nx, ny, nz).  The
+ * adjoint and stored spectra are not built for it (EVX_ERR_UNSUPPORTED);
+ * otherwise EVX_ERR_BAD_BC as the reference's verify_fft_bc_config
+ * (evoxels/problem_definition.py:138-167). */
+int evx_ch_plan_create_bc(evx_ch_plan** plan, const evx_grid* g, const evx_bc* bc, int flags);
 /* flags bit 2: with the x-pass and ny, nz in {64, 128, 256}, use the fused
  * (y, z) kernels (evx_fft_yz_r2c/c2r) instead of cuFFT's (y, z) plans.  Off by
  * default: on GB300 at 256^3 they take 73/68 us per transform against cuFFT's

@@ -239,24 +239,56 @@ def rfft_k_squared(shape, spacing=(1.0, 1.0, 1.0), dtype=torch.float32):
     return kx ** 2 + ky ** 2 + kz ** 2
 
 
-def imex_prefac(shape, dt, eps=3.0, D=1.0, A=0.25, spacing=(1.0, 1.0, 1.0), dtype=torch.float32):
+def rfft_k_squared_nonperiodic(shape, spacing=(1.0, 1.0, 1.0), dtype=torch.float32):
+    """``VoxelGrid.rfft_k_squared_nonperiodic`` for the cell-centred grid
+    (evoxels/voxelgrid.py:116-124): the x frequencies of the mirrored grid,
+    ``2*pi*fftfreq(2*Nx, h_x)``; y and z as in ``rfft_k_squared``."""
+    ax = 2 * torch.pi * torch.fft.fftfreq(2 * shape[0], spacing[0], dtype=dtype)
+    ay = 2 * torch.pi * torch.fft.fftfreq(shape[1], spacing[1], dtype=dtype)
+    az = 2 * torch.pi * torch.fft.rfftfreq(shape[2], spacing[2], dtype=dtype)
+    kx, ky, kz = torch.meshgrid(ax, ay, az, indexing="ij")
+    return kx ** 2 + ky ** 2 + kz ** 2
+
+
+def x_bc_kind(bc):
+    """The x-axis kind of a BC spec: 'periodic', 'neumann' or 'dirichlet'."""
+    return normalize_bc(bc)[0][0]
+
+
+def imex_prefac(shape, dt, eps=3.0, D=1.0, A=0.25, spacing=(1.0, 1.0, 1.0), dtype=torch.float32, bc=None):
     """``PseudoSpectralIMEX._fft_prefac`` for ``CahnHilliard``.
 
     ``symbol = -2*eps*D*A*(k^2)^2`` (evoxels/problem_definition.py:303) and
-    ``prefac = dt / (1 - dt*symbol)`` (evoxels/timesteppers.py:77).
+    ``prefac = dt / (1 - dt*symbol)`` (evoxels/timesteppers.py:77); a Neumann or
+    Dirichlet x axis takes the mirrored-grid k^2 (evoxels/problem_definition.py:169-177).
     """
-    k2 = rfft_k_squared(shape, spacing, dtype)
+    if x_bc_kind(bc) in ("neumann", "dirichlet"):
+        k2 = rfft_k_squared_nonperiodic(shape, spacing, dtype)
+    else:
+        k2 = rfft_k_squared(shape, spacing, dtype)
     symbol = -2 * eps * D * A * k2 ** 2
     return dt / (1 - dt * symbol)
 
 
-def imex_step(u, prefac, rhs_fn):
-    """``PseudoSpectralIMEX.step`` for a periodic problem (evoxels/timesteppers.py:85-89).
+def pad_fft(dc, bc=None):
+    """``CahnHilliard.pad_fft_bc`` on the cell-centred grid
+    (evoxels/boundary_conditions.py:60-70): periodic x is the identity, Neumann x
+    appends the x-flipped field (even extension), Dirichlet x its negative."""
+    kind = x_bc_kind(bc)
+    if kind == "neumann":
+        return torch.cat((dc, torch.flip(dc, [1])), 1)
+    if kind == "dirichlet":
+        return torch.cat((dc, -torch.flip(dc, [1])), 1)
+    return dc
 
-    The FFT pad is the identity for periodic x (evoxels/boundary_conditions.py:61-63);
-    the transform runs over the full 4-D shape including the channel axis.
+
+def imex_step(u, prefac, rhs_fn, bc=None):
+    """``PseudoSpectralIMEX.step`` (evoxels/timesteppers.py:85-89).
+
+    ``dc = pad_fft(rhs(u))``; the transform runs over the full 4-D shape of ``dc``
+    including the channel axis; the update is trimmed back to ``u``'s x extent.
     """
-    dc = rhs_fn(u)
+    dc = pad_fft(rhs_fn(u), bc)
     dc_fft = prefac * torch.fft.rfftn(dc, s=dc.shape)
     update = torch.fft.irfftn(dc_fft, s=dc.shape)[:, :u.shape[1]]
     return u + update
@@ -268,18 +300,19 @@ def fe_step(u, dt, rhs_fn):
 
 
 def ch_imex_run(u0, nsteps, dt=0.1, eps=3.0, D=1.0, A=0.25, spacing=(1.0, 1.0, 1.0),
-                mu_hom=None, k_dtype=None, keep=None):
+                mu_hom=None, k_dtype=None, keep=None, bc=None):
     """``nsteps`` Cahn-Hilliard IMEX steps from ``u0``; returns the final state.
 
     ``keep`` (optional list) receives every intermediate state, ``u0`` first.
+    ``bc``: the problem's BC spec (at most x non-periodic, as the reference allows).
     """
     shape = tuple(u0.shape[1:])
-    prefac = imex_prefac(shape, dt, eps, D, A, spacing, k_dtype or u0.dtype)
+    prefac = imex_prefac(shape, dt, eps, D, A, spacing, k_dtype or u0.dtype, bc)
     u = u0
     if keep is not None:
         keep.append(u)
     for _ in range(nsteps):
-        u = imex_step(u, prefac, lambda v: ch_rhs(v, eps, D, None, spacing, mu_hom))
+        u = imex_step(u, prefac, lambda v: ch_rhs(v, eps, D, bc, spacing, mu_hom), bc)
         if keep is not None:
             keep.append(u)
     return u

@@ -116,6 +116,22 @@ def main():
             u = st.step(0.0, u)
         out[f"ch_imex_{i}"] = dict(u0=u0, u=u.numpy(), shape=np.array(shape), eps=eps, D=D, dt=dt, n=n)
 
+    # 3b) PseudoSpectralIMEX with a non-periodic x axis (mirrored FFT extension)
+    nx_cases = [((16, 12, 10), 24, ("neumann", "periodic", "periodic"), 3.0, 1.0, 0.1, 5),
+                ((8, 16, 12), 25, (("dirichlet", (0.0, 0.0)), "periodic", "periodic"), 2.0, 1.2, 0.1, 5),
+                ((10, 8, 9), 26, (("dirichlet", (0.2, 0.7)), "periodic", "periodic"), 3.0, 1.0, 0.05, 4),
+                ((12, 10, 8), 27, ("neumann", "periodic", "periodic"), 1.5, 0.8, 0.1, 6)]
+    for i, (shape, seed, bc, eps, D, dt, n) in enumerate(nx_cases):
+        _, vg = make_vg(R, shape)
+        prob = PD.CahnHilliard(vg, eps=eps, D=D, bc=bc)
+        st = TS.PseudoSpectralIMEX(prob, dt)
+        u0 = ch_field(shape, seed)
+        u = vg.init_scalar_field(u0)
+        for _ in range(n):
+            u = st.step(0.0, u)
+        out[f"ch_imex_nx_{i}"] = dict(u0=u0, u=u.numpy(), shape=np.array(shape), eps=eps, D=D, dt=dt, n=n,
+                                      bc=np.array(repr(bc)))
+
     # 4) true FP64 CH IMEX (default dtype float64 so the k-grid is fp64 too)
     torch.set_default_dtype(torch.float64)
     shape = (16, 16, 16)

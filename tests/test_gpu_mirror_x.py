@@ -1,0 +1,102 @@
+"""Spectral Cahn-Hilliard step with a Neumann or Dirichlet x axis (the reference's
+mirrored FFT extension): against the reference's own fp32 runs (golden
+fixtures), the FP64 oracle, cuFFT 3-D on the doubled grid, and through the
+solver driver."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import load_golden, parse_bc
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def vg_for(shape):
+    from evoxels_gb300.voxelfields import VoxelFields
+    from evoxels_gb300.voxelgrid import VoxelGridGB300
+    return VoxelGridGB300(VoxelFields(shape, domain_size=shape).grid_info(), device=DEV)
+
+
+def gpu(a):
+    return torch.tensor(np.asarray(a), dtype=torch.float32, device=DEV).unsqueeze(0)
+
+
+@pytest.mark.parametrize("i", range(4))
+def test_mirror_x_vs_reference_golden(cuda_lib, i):
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+    g = load_golden(f"ch_imex_nx_{i}")
+    shape = tuple(int(x) for x in g["shape"])
+    bc = parse_bc(g["bc"])
+    st = PseudoSpectralIMEX(CahnHilliard(vg_for(shape), eps=float(g["eps"]), D=float(g["D"]), bc=bc),
+                            float(g["dt"]))
+    u = gpu(g["u0"])
+    for _ in range(int(g["n"])):
+        u = st.step(0.0, u)
+    # reference fp32 (pocketfft) vs ours (cuFFT / x-pass): float32 FFT rounding
+    assert oracle.rel_to_max(u.cpu().numpy()[0], g["u"][0]) < 2e-6
+    ref = oracle.ch_imex_run(torch.tensor(g["u0"]).unsqueeze(0), int(g["n"]), float(g["dt"]), float(g["eps"]),
+                             float(g["D"]), bc=bc).numpy()
+    assert oracle.rel_to_max(u.cpu().numpy(), ref) <= 1e-5 * int(g["n"])
+
+
+BCS = [("neumann", "periodic", "periodic"), (("dirichlet", (0.0, 0.0)), "periodic", "periodic"),
+       (("dirichlet", (0.3, 0.8)), "periodic", "periodic")]
+
+
+# power-of-two nx up to 256 use the x-pass with the extension inside; others cuFFT 3-D on 2*nx
+@pytest.mark.parametrize("shape", [(32, 20, 36), (8, 12, 16), (64, 16, 24), (24, 16, 20), (256, 8, 8)])
+@pytest.mark.parametrize("b", range(3))
+def test_mirror_x_paths_agree_and_match_fp64(cuda_lib, shape, b):
+    from evoxels_gb300 import _lib
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.timesteppers import get_plan
+    from evoxels_gb300.voxelgrid import cuda_stream
+    vg = vg_for(shape)
+    prob = CahnHilliard(vg, eps=1.7, D=1.3, bc=BCS[b])
+    u0n = oracle.seeded_ch_field(shape, 8 + b)
+    u0 = gpu(u0n)
+    outs = []
+    for cufft3d in (False, True):
+        plan = get_plan(vg, cufft3d=cufft3d, bc=prob.bc)
+        out = torch.empty_like(u0)
+        _lib.check(cuda_lib.evx_ch_forward(plan.handle, u0.data_ptr(), out.data_ptr(), 3, None,
+                                           prob.evx_params(0.1), None, plan.workspace.data_ptr(), cuda_stream()))
+        outs.append(out.cpu().numpy())
+    assert oracle.rel_to_max(outs[0], outs[1]) < 1e-6
+    ref = oracle.ch_imex_run(torch.tensor(u0n).unsqueeze(0), 3, 0.1, 1.7, 1.3, bc=prob.bc).numpy()
+    assert oracle.rel_to_max(outs[0], ref) <= 3e-5
+
+
+def test_mirror_x_driver_and_errors(cuda_lib):
+    from evoxels_gb300 import _lib
+    from evoxels_gb300.problem_definition import CahnHilliard
+    from evoxels_gb300.solvers import TimeDependentSolver
+    from evoxels_gb300.timesteppers import PseudoSpectralIMEX, get_plan
+    from evoxels_gb300.voxelfields import VoxelFields
+    shape = (16, 12, 8)
+    vf = VoxelFields(shape, domain_size=shape)
+    c0 = oracle.seeded_ch_field(shape, 31)
+    vf.add_field("c", c0.copy())
+    bc = ("neumann", "periodic", "periodic")
+    solver = TimeDependentSolver(vf, "c", "torch", problem_cls=CahnHilliard, timestepper_cls=PseudoSpectralIMEX)
+    solver.solve(time_increment=0.1, frames=2, max_iters=6, problem_kwargs={"bc": bc}, jit=False, verbose=False)
+    ref = oracle.ch_imex_run(torch.tensor(c0).unsqueeze(0), 6, 0.1, bc=bc).numpy()[0]
+    assert oracle.rel_to_max(vf.fields["c"], ref) <= 6e-5
+    # the reference-side pieces of the mirrored step are exposed too
+    prob = CahnHilliard(vg_for(shape), bc=(("dirichlet", (0.0, 1.0)), "periodic", "periodic"))
+    st = PseudoSpectralIMEX(prob, 0.1)
+    u = torch.rand((1,) + shape, device=DEV)
+    assert st.pad(u).shape == (1, 2 * shape[0]) + shape[1:]
+    assert torch.equal(st.pad(u)[:, shape[0]:], -torch.flip(u, [1]))
+    assert tuple(prob.k_squared().shape) == (2 * shape[0], shape[1], shape[2] // 2 + 1)
+    # gradients of the mirrored step are not built: a clear error, not a silent periodic run
+    plan = get_plan(prob.vg, bc=prob.bc)
+    lam = torch.zeros_like(u)
+    with pytest.raises(NotImplementedError):
+        _lib.check(cuda_lib.evx_ch_adjoint(plan.handle, torch.cat([u, u]).data_ptr(), 1, lam.data_ptr(),
+                                           torch.empty_like(lam).data_ptr(), prob.evx_params(0.1), None,
+                                           plan.workspace.data_ptr(), 0), "adjoint")

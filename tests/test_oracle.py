@@ -56,6 +56,18 @@ def test_ch_imex_matches_reference(i):
     assert oracle.rel_to_max(u.numpy(), g["u"]) < 1e-6
 
 
+@pytest.mark.parametrize("i", range(4))
+def test_ch_imex_nonperiodic_x_matches_reference(i):
+    """Mirrored-x spectral step (Neumann: even extension, Dirichlet: odd) vs the reference."""
+    g = load_golden(f"ch_imex_nx_{i}")
+    bc = parse_bc(g["bc"])
+    u = oracle.ch_imex_run(t32(g["u0"]), int(g["n"]), float(g["dt"]), float(g["eps"]), float(g["D"]), bc=bc)
+    assert oracle.rel_to_max(u.numpy(), g["u"]) < 1e-6
+    u64 = oracle.ch_imex_run(torch.tensor(g["u0"]).unsqueeze(0), int(g["n"]), float(g["dt"]), float(g["eps"]),
+                             float(g["D"]), bc=bc)
+    assert oracle.rel_to_max(g["u"], u64.numpy()) < 1e-6
+
+
 def test_ch_imex_fp64_matches_reference():
     g = load_golden("ch_imex_fp64")
     u0 = torch.tensor(g["u0"], dtype=torch.float64).unsqueeze(0)
