@@ -51,7 +51,7 @@ class BatchedCahnHilliard:
     """
 
     def __init__(self, shapes, D=1.0, eps=3.0, dt=0.1, A=0.25, mu_hom=None, spacing=None,
-                 tuning: BatchTuning | None = None, device="cuda"):
+                 tuning: BatchTuning | None = None, device="cuda", cufft3d=False):
         self.device = _require_cuda(device)
         self.shapes = [tuple(int(x) for x in s) for s in shapes]
         n = len(self.shapes)
@@ -76,7 +76,10 @@ class BatchedCahnHilliard:
         h = C.c_void_p()
         L = _lib.lib()
         with torch.cuda.device(self.device):
-            _lib.check(L.evx_batch_create(C.byref(h), inst, n, self.tuning.to_c(), 0), "evx_batch_create")
+            # flags bit 1: cuFFT 3-D for every shape group (default: power-of-two nx groups
+            # use cuFFT (y, z) plus the batched x-pass)
+            _lib.check(L.evx_batch_create(C.byref(h), inst, n, self.tuning.to_c(), 2 if cufft3d else 0),
+                       "evx_batch_create")
         self.handle = h
         self.total = int(L.evx_batch_field_floats(h))
         self.work_items = int(L.evx_batch_work_items(h))

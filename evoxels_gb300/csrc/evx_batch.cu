@@ -9,8 +9,12 @@
 // same way.  One IMEX step of the whole batch is
 //   batched rhs (one persistent launch over instance x tile x x-chunk work
 //   items, largest items first, pulled from a global counter)
-//   -> R2C per shape group -> batched k-space multiply (one launch)
-//   -> C2R per shape group,
+//   -> R2C per shape group -> k-space multiply -> C2R per shape group,
+// where a group with a power-of-two nx uses cuFFT's 2-D (y, z) transforms over
+// all its instances' x planes and one batched x-pass launch (FFT along x,
+// multiply, inverse FFT along x; the single-grid kernel of evx_fftx.cu with a
+// per-instance table), and the other groups cuFFT 3-D and one batched k-space
+// launch,
 // with the update fused into the next step's rhs pass as in the single-grid
 // path.  Runs of steps without a stored trajectory are captured once into a
 // CUDA graph on an internal stream and replayed.  The adjoint runs the same
@@ -31,6 +35,7 @@ struct KInst {          // k-space descriptor of one instance
     int nx, ny, nzh;
     int kx, ky, kz;     // offsets of the k^2 tables
     float sym_coef, dt, invN;
+    int xmode;          // 1: its group's multiply is done by the x-pass
 };
 
 struct RInst {          // gradient-reduction descriptor of one instance
@@ -41,6 +46,7 @@ struct RInst {          // gradient-reduction descriptor of one instance
 __global__ void batch_kspace_fwd_kernel(float2* __restrict__ spec, const KInst* __restrict__ ki,
                                         const float* __restrict__ k2) {
     const KInst K = ki[blockIdx.y];
+    if (K.xmode) return;   // uniform in the block
     const size_t total = (size_t)K.nx * K.ny * K.nzh;
     float2* s = spec + K.soff;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -60,6 +66,7 @@ __global__ void batch_kspace_fwd_kernel(float2* __restrict__ spec, const KInst* 
 __global__ void batch_kspace_adj_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h,
                                         const KInst* __restrict__ ki, const float* __restrict__ k2) {
     const KInst K = ki[blockIdx.y];
+    if (K.xmode) return;   // uniform in the block
     const size_t total = (size_t)K.nx * K.ny * K.nzh;
     float2* s = spec + K.soff;
     float2* sh = spec_h ? spec_h + K.soff : nullptr;
@@ -134,6 +141,8 @@ struct evx_batch {
         long long off = 0, soff = 0;   // packed offsets of the group's first instance
         size_t n = 0, nspec = 0;       // per instance
         int first = 0, count = 0;      // internal instance range
+        bool xmode = false;            // cuFFT (y, z) plans + batched x-pass
+        int k2x = 0, k2y = 0, k2z = 0; // offsets of the group's k^2 tables
         std::vector<Plan> plans;
     };
     int n = 0;
@@ -149,6 +158,8 @@ struct evx_batch {
     BatchItem* d_items = nullptr;
     KInst* d_kinst = nullptr;
     RInst* d_rinst = nullptr;
+    XBatchInst* d_xb = nullptr;
+    bool any_kspace = true;                // a group still uses the k-space kernels
     float* d_k2 = nullptr;
     size_t ws_fft = 0;
     size_t off_fft = 0, off_r = 0, off_upd = 0, off_spec = 0, off_ua = 0, off_ub = 0, off_lam = 0, off_part = 0,
@@ -216,14 +227,28 @@ int batch_c2r(evx_batch* b, float2* in, float* out, cudaStream_t st) {
     return EVX_OK;
 }
 
+// x-pass of every power-of-two group: mode 0 forward, 1 adjoint g, 2 adjoint g and h
+int batch_xpass(evx_batch* b, int mode, float2* spec, float2* spec_h, cudaStream_t st) {
+    for (auto& g : b->groups) {
+        if (!g.xmode) continue;
+        int rc = xpass_batch_launch(mode, g.nx, spec, spec_h, b->d_xb + g.first, g.count, g.ny * g.nzh, g.nzh, g.nz,
+                                    b->d_k2 + g.k2x, b->d_k2 + g.k2y, b->d_k2 + g.k2z, st);
+        if (rc) return rc;
+    }
+    return EVX_OK;
+}
+
 // One IMEX step's spectral part: r -> upd
 int batch_spectral(evx_batch* b, float* r, float2* spec, float* upd, cudaStream_t st) {
     int rc;
     if ((rc = batch_r2c(b, r, spec, st))) return rc;
-    EVX_TIMED("batch_kspace_fwd", st,
-              batch_kspace_fwd_kernel<<<dim3(b->kspace_blocks, b->n), 256, 0, st>>>(spec, b->d_kinst, b->d_k2));
-    count_launch();
-    if ((rc = check_launch("batch_kspace_fwd_kernel"))) return rc;
+    if (b->any_kspace) {
+        EVX_TIMED("batch_kspace_fwd", st,
+                  batch_kspace_fwd_kernel<<<dim3(b->kspace_blocks, b->n), 256, 0, st>>>(spec, b->d_kinst, b->d_k2));
+        count_launch();
+        if ((rc = check_launch("batch_kspace_fwd_kernel"))) return rc;
+    }
+    if ((rc = batch_xpass(b, 0, spec, nullptr, st))) return rc;
     return batch_c2r(b, spec, upd, st);
 }
 
@@ -288,7 +313,6 @@ int capture_chunk(evx_batch* b, void* ws, int steps) {
 extern "C" {
 
 int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, const evx_batch_tuning* tune, int flags) {
-    (void)flags;
     if (!out) return fail(EVX_ERR_BAD_ARG, "batch pointer is NULL");
     *out = nullptr;
     if (!inst || n < 1) return fail(EVX_ERR_BAD_ARG, "need at least one instance");
@@ -343,13 +367,16 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
     auto cleanup = [&](int code) { batch_free(b); return code; };
     // cuFFT plans per group (split by fft_group_max)
     size_t wmax = 0;
+    b->any_kspace = false;
     for (auto& g : b->groups) {
+        // flags bit 1: cuFFT's 3-D transforms for every group (as evx_ch_plan_create)
+        g.xmode = xpass_supported(g.nx) && !(flags & 2) && (size_t)g.count * g.nx <= 2147483647ull;
+        if (!g.xmode) b->any_kspace = true;
         const int gm = b->tune.fft_group_max > 0 ? b->tune.fft_group_max : g.count;
         for (int f = 0; f < g.count; f += gm) {
             evx_batch::Plan p;
             p.first = g.first + f;
             p.count = std::min(gm, g.count - f);
-            int dims[3] = {g.nx, g.ny, g.nz};
             size_t w1 = 0, w2 = 0;
             int rc;
             if ((rc = check_cufft(cufftCreate(&p.r2c), "cufftCreate"))) return cleanup(rc);
@@ -357,12 +384,26 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
             cufftSetAutoAllocation(p.r2c, 0);
             cufftSetAutoAllocation(p.c2r, 0);
             g.plans.push_back(p);
-            if ((rc = check_cufft(cufftMakePlanMany(p.r2c, 3, dims, nullptr, 1, (int)g.n, nullptr, 1, (int)g.nspec,
-                                                    CUFFT_R2C, p.count, &w1), "cufftMakePlanMany R2C (batch)")))
-                return cleanup(rc);
-            if ((rc = check_cufft(cufftMakePlanMany(p.c2r, 3, dims, nullptr, 1, (int)g.nspec, nullptr, 1, (int)g.n,
-                                                    CUFFT_C2R, p.count, &w2), "cufftMakePlanMany C2R (batch)")))
-                return cleanup(rc);
+            if (g.xmode) {   // 2-D (y, z) over every x plane of the plan's instances
+                int d2[2] = {g.ny, g.nz};
+                const int pr = g.ny * g.nz, ps = g.ny * g.nzh;
+                if ((rc = check_cufft(cufftMakePlanMany(p.r2c, 2, d2, nullptr, 1, pr, nullptr, 1, ps, CUFFT_R2C,
+                                                        p.count * g.nx, &w1), "cufftMakePlanMany R2C (y,z) (batch)")))
+                    return cleanup(rc);
+                if ((rc = check_cufft(cufftMakePlanMany(p.c2r, 2, d2, nullptr, 1, ps, nullptr, 1, pr, CUFFT_C2R,
+                                                        p.count * g.nx, &w2), "cufftMakePlanMany C2R (y,z) (batch)")))
+                    return cleanup(rc);
+            } else {
+                int dims[3] = {g.nx, g.ny, g.nz};
+                if ((rc = check_cufft(cufftMakePlanMany(p.r2c, 3, dims, nullptr, 1, (int)g.n, nullptr, 1,
+                                                        (int)g.nspec, CUFFT_R2C, p.count, &w1),
+                                      "cufftMakePlanMany R2C (batch)")))
+                    return cleanup(rc);
+                if ((rc = check_cufft(cufftMakePlanMany(p.c2r, 3, dims, nullptr, 1, (int)g.nspec, nullptr, 1,
+                                                        (int)g.n, CUFFT_C2R, p.count, &w2),
+                                      "cufftMakePlanMany C2R (batch)")))
+                    return cleanup(rc);
+            }
             wmax = std::max(wmax, std::max(w1, w2));
         }
     }
@@ -371,6 +412,10 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
     std::vector<BatchInst> hinst(n);
     std::vector<KInst> hk(n);
     std::vector<RInst> hr(n);
+    std::vector<XBatchInst> hxb(n);
+    std::vector<int> group_of(n);
+    for (size_t gi = 0; gi < b->groups.size(); ++gi)
+        for (int k = 0; k < b->groups[gi].count; ++k) group_of[b->groups[gi].first + k] = (int)gi;
     std::vector<BatchItem> items;
     std::vector<float> k2;
     std::map<std::tuple<int, int, int, double, double, double>, int> k2pos;
@@ -417,6 +462,14 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
         hk[ii].sym_coef = s.params.sym_coef;
         hk[ii].dt = s.params.dt;
         hk[ii].invN = (float)(1.0 / ((double)s.nx * s.ny * s.nz));
+        evx_batch::Group& grp = b->groups[group_of[ii]];
+        hk[ii].xmode = grp.xmode ? 1 : 0;
+        grp.k2x = hk[ii].kx; grp.k2y = hk[ii].ky; grp.k2z = hk[ii].kz;
+        hxb[ii].soff = soff_of[ii];
+        hxb[ii].sym = s.params.sym_coef;
+        hxb[ii].dt = s.params.dt;
+        hxb[ii].invN = hk[ii].invN;
+        hxb[ii].pad = 0;
     }
     // largest work items first (longest-processing-time order for the persistent blocks)
     std::stable_sort(items.begin(), items.end(), [&](const BatchItem& a, const BatchItem& c) {
@@ -430,8 +483,9 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
     // one device allocation for the tables
     const size_t s_inst = al256(sizeof(BatchInst) * n), s_items = al256(sizeof(BatchItem) * items.size());
     const size_t s_k = al256(sizeof(KInst) * n), s_r = al256(sizeof(RInst) * n), s_k2 = al256(sizeof(float) * k2.size());
+    const size_t s_xb = al256(sizeof(XBatchInst) * n);
     int rc;
-    if ((rc = check_cuda(cudaMalloc(&b->dev, s_inst + s_items + s_k + s_r + s_k2), "cudaMalloc batch tables")))
+    if ((rc = check_cuda(cudaMalloc(&b->dev, s_inst + s_items + s_k + s_r + s_k2 + s_xb), "cudaMalloc batch tables")))
         return cleanup(rc);
     char* d = static_cast<char*>(b->dev);
     b->d_inst = reinterpret_cast<BatchInst*>(d);
@@ -439,12 +493,14 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
     b->d_kinst = reinterpret_cast<KInst*>(d + s_inst + s_items);
     b->d_rinst = reinterpret_cast<RInst*>(d + s_inst + s_items + s_k);
     b->d_k2 = reinterpret_cast<float*>(d + s_inst + s_items + s_k + s_r);
+    b->d_xb = reinterpret_cast<XBatchInst*>(d + s_inst + s_items + s_k + s_r + s_k2);
     if ((rc = check_cuda(cudaMemcpy(b->d_inst, hinst.data(), sizeof(BatchInst) * n, cudaMemcpyHostToDevice), "copy")) ||
         (rc = check_cuda(cudaMemcpy(b->d_items, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice),
                          "copy")) ||
         (rc = check_cuda(cudaMemcpy(b->d_kinst, hk.data(), sizeof(KInst) * n, cudaMemcpyHostToDevice), "copy")) ||
         (rc = check_cuda(cudaMemcpy(b->d_rinst, hr.data(), sizeof(RInst) * n, cudaMemcpyHostToDevice), "copy")) ||
-        (rc = check_cuda(cudaMemcpy(b->d_k2, k2.data(), sizeof(float) * k2.size(), cudaMemcpyHostToDevice), "copy")))
+        (rc = check_cuda(cudaMemcpy(b->d_k2, k2.data(), sizeof(float) * k2.size(), cudaMemcpyHostToDevice), "copy")) ||
+        (rc = check_cuda(cudaMemcpy(b->d_xb, hxb.data(), sizeof(XBatchInst) * n, cudaMemcpyHostToDevice), "copy")))
         return cleanup(rc);
     // persistent grids
     int dev = 0, sms = 0;
@@ -573,11 +629,14 @@ int evx_batch_adjoint(evx_batch* b, const float* states, int nsteps, const float
     for (int s = nsteps - 1; s >= 0; --s) {
         float* dst = (s % 2 == 0) ? lam_out : B.lam;
         if ((rc = batch_r2c(b, lam, B.spec, st))) return rc;
-        EVX_TIMED("batch_kspace_adj", st,
-                  batch_kspace_adj_kernel<<<dim3(b->kspace_blocks, b->n), 256, 0, st>>>(
-                      B.spec, want ? spec_h : nullptr, b->d_kinst, b->d_k2));
-        count_launch();
-        if ((rc = check_launch("batch_kspace_adj_kernel"))) return rc;
+        if (b->any_kspace) {
+            EVX_TIMED("batch_kspace_adj", st,
+                      batch_kspace_adj_kernel<<<dim3(b->kspace_blocks, b->n), 256, 0, st>>>(
+                          B.spec, want ? spec_h : nullptr, b->d_kinst, b->d_k2));
+            count_launch();
+            if ((rc = check_launch("batch_kspace_adj_kernel"))) return rc;
+        }
+        if ((rc = batch_xpass(b, want ? 2 : 1, B.spec, want ? spec_h : nullptr, st))) return rc;
         if ((rc = batch_c2r(b, B.spec, gbuf, st))) return rc;
         if (want && (rc = batch_c2r(b, spec_h, hbuf, st))) return rc;
         const float* us = states + (size_t)s * T;

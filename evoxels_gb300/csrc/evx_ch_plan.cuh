@@ -78,7 +78,17 @@ struct XpassArgs {
     int* n_xpart_out;                  // optional: partial-sum slots written (mode 3)
     int ext;                           // x mirror extension (mode 0): 1 even, 2 odd; nx = transform length / 2
 };
+// Batched x-pass (one launch per shape group of the batched path): per-instance
+// spectrum offset and IMEX constants, indexed by blockIdx.y.
+struct XBatchInst {
+    long long soff;    // complex values
+    float sym, dt, invN;
+    int pad;
+};
 bool xpass_supported(int nx);
+// mode 0 forward, 1 adjoint g, 2 adjoint g and h (spec_h, same offsets); per-tile kernel
+int xpass_batch_launch(int mode, int nx, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M,
+                       int nzh, int nz, const float* kx2, const float* ky2, const float* kz2, cudaStream_t st);
 size_t xpass_blocks(int nx, int M);
 size_t xpass_spectrum_floats(int nx, int M);
 int xpass_launch(const XpassArgs& a, cudaStream_t st);

@@ -143,13 +143,23 @@ __device__ __forceinline__ void block_sum2(float t1, float t2, double* out) {
 // against dspec into xpart[2*block .. 2*block+1]).  EXT 1 / 2: the spectrum
 // holds N/2 x rows and the transformed sequence is its even / odd mirror
 // extension, x' = N-1-x for x >= N/2 (the mirrored-x step of a Neumann /
-// Dirichlet x axis); only the first N/2 rows are written back.
+// Dirichlet x axis); only the first N/2 rows are written back.  xb (batched
+// path): instance blockIdx.y of a shape group, its spectrum offset and IMEX
+// constants taken from xb.
 template <int N1, int N2, int MODE, int EXT = 0>
 __global__ void __launch_bounds__(256, MODE == 2 ? 2 : EVX_XPASS_MIN_BLOCKS)
 xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __restrict__ dspec,
              double* __restrict__ xpart, int M, int nzh, int nz,
              const float* __restrict__ kx2, const float* __restrict__ ky2, const float* __restrict__ kz2,
-             float sym_coef, float dt, float invN) {
+             float sym_coef, float dt, float invN, const XBatchInst* __restrict__ xb) {
+    if (xb) {
+        const XBatchInst X = xb[blockIdx.y];
+        spec += X.soff;
+        if (spec_h) spec_h += X.soff;
+        sym_coef = X.sym;
+        dt = X.dt;
+        invN = X.invN;
+    }
     using C = Col<N1, N2>;
     constexpr int P = 256 / N2, Q = C::Q;
     extern __shared__ float2 xs[];       // [N1][N2][P], pencil index fastest (conflict-free)
@@ -370,7 +380,7 @@ int xpass_launch_tile(const XpassArgs& A, cudaStream_t st, const char* slot) {
     EVX_TIMED(slot, st,
               (xpass_kernel<N1, N2, MODE, EXT><<<blocks, 256, smem, st>>>(A.spec, A.spec_h, A.dspec, A.xpart, A.M,
                                                                         A.nzh, A.nz, A.kx2, A.ky2, A.kz2, A.sym,
-                                                                        A.dt, A.invN)));
+                                                                        A.dt, A.invN, nullptr)));
     count_launch();
     return check_launch("xpass_kernel");
 }
@@ -471,6 +481,51 @@ size_t xpass_spectrum_floats(int nx, int M) {
     // [tile][element < N1][thread < 256] complex values; N1 = nx / N2
     const int n2 = xpass_split_n2(nx);
     return n2 ? xpass_blocks(nx, M) * (size_t)(nx / n2) * 256 * 2 : 0;
+}
+
+template <int N1, int N2>
+int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M, int nzh, int nz,
+                  const float* kx2, const float* ky2, const float* kz2, cudaStream_t st) {
+    constexpr int P = 256 / N2;
+    const size_t smem = (size_t)N1 * N2 * P * sizeof(float2);
+    const dim3 grid((M + P - 1) / P, count);
+    static bool attr[3] = {false, false, false};   // per mode of this (N1, N2)
+    auto go = [&](auto kern, const char* slot) {
+        if (!attr[mode]) {
+            const int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                                      "x-pass shared memory attribute");
+            if (rc) return rc;
+            attr[mode] = true;
+        }
+        EVX_TIMED(slot, st, (kern<<<grid, 256, smem, st>>>(spec, spec_h, nullptr, nullptr, M, nzh, nz, kx2, ky2, kz2,
+                                                           0.f, 0.f, 0.f, xb)));
+        count_launch();
+        return check_launch("xpass_kernel (batched)");
+    };
+    switch (mode) {
+        case 0: return go(xpass_kernel<N1, N2, 0>, "batch_xpass_fwd");
+        case 1: return go(xpass_kernel<N1, N2, 1>, "batch_xpass_adj");
+        default: return go(xpass_kernel<N1, N2, 2>, "batch_xpass_adj");
+    }
+}
+
+int xpass_batch_launch(int mode, int nx, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M,
+                       int nzh, int nz, const float* kx2, const float* ky2, const float* kz2, cudaStream_t st) {
+    int rc = xpass_init();
+    if (rc) return rc;
+    if (count < 1 || count > 65535) return fail(EVX_ERR_BAD_ARG, "batched x-pass: %d instances", count);
+    if (mode < 0 || mode > 2) return fail(EVX_ERR_BAD_ARG, "batched x-pass mode %d", mode);
+    if (mode == 2 && !spec_h) return fail(EVX_ERR_BAD_ARG, "x-pass mode 2 is missing a buffer");
+    switch (nx) {
+        case 8: return xpass_batch_t<8, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
+        case 16: return xpass_batch_t<16, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
+        case 32: return xpass_batch_t<16, 2>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
+        case 64: return xpass_batch_t<16, 4>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
+        case 128: return xpass_batch_t<16, 8>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
+        case 256: return xpass_batch_t<16, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
+        case 512: return xpass_batch_t<32, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
+        default: return fail(EVX_ERR_UNSUPPORTED, "x-pass needs a power-of-two nx in [8, 512]");
+    }
 }
 
 int xpass_launch(const XpassArgs& A, cudaStream_t st) {

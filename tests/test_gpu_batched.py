@@ -125,3 +125,26 @@ def test_autotuner_returns_a_valid_tuning(cuda_lib, tmp_path, monkeypatch):
     again = autotune.tune_batched(SHAPES[:3], 1.0, 1.0, steps=4, space=space)   # from the cache
     assert again == t
     assert (tmp_path / "cache.json").exists()
+
+
+def test_batched_xpass_groups_match_cufft3d(cuda_lib):
+    """Power-of-two groups (cuFFT (y, z) + batched x-pass) against cuFFT 3-D for every group."""
+    from evoxels_gb300.batched import BatchedCahnHilliard
+    f = fields(7)
+    res = []
+    for cufft3d in (False, True):
+        b = BatchedCahnHilliard(SHAPES, D, EPS, 0.1, cufft3d=cufft3d)
+        n = 4
+        states = torch.empty((n + 1) * b.total, dtype=torch.float32, device="cuda")
+        states[:b.total].copy_(b.pack(f))
+        b.forward(states[:b.total], n, traj=states[b.total:])
+        lam = b.pack([np.random.default_rng(11 + i).random(s) - 0.5 for i, s in enumerate(SHAPES)])
+        grads = torch.zeros((b.n, 3), dtype=torch.float64, device="cuda")
+        out = b.adjoint(states, n, lam, grads)
+        res.append((b.unpack(states[n * b.total:]), b.unpack(out), grads.cpu().numpy()))
+    (ua, la, ga), (ub, lb, gb) = res
+    for i in range(len(SHAPES)):
+        assert oracle.rel_to_max(ua[i].cpu().numpy(), ub[i].cpu().numpy()) < 1e-6, i
+        assert oracle.rel_to_max(la[i].cpu().numpy(), lb[i].cpu().numpy()) < 1e-5, i
+        # real-space gradient sums difference float32 states: the cross-FFT bar
+        np.testing.assert_allclose(ga[i], gb[i], rtol=1e-3, atol=1e-9)
