@@ -8,7 +8,7 @@ gradient, then 10 adjoint steps giving dL/dc0, dL/dD and dL/deps.  A
 voxel-step counts one forward plus one adjoint step of one voxel.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch128_inversion]
+                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch512_fwd_adj|ch128_inversion]
 
 ``--impl reference`` times the CPU oracle (the operation-by-operation torch
 restatement of the reference's own torch path; the reference itself is pure
@@ -264,7 +264,7 @@ class ChForward:
 class FdForward:
     """Explicit FD diffusion, 512^3, Dirichlet x / Neumann y,z, dt = 1/60 (config 2)."""
 
-    def __init__(self, torch, device, n=512, steps_per=100, seed=2, spp=4):
+    def __init__(self, torch, device, n=512, steps_per=100, seed=2, spp=0):
         import warnings
         from evoxels_gb300.problem_definition import ReactionDiffusion
         from evoxels_gb300.timesteppers import ForwardEuler
@@ -280,14 +280,19 @@ class FdForward:
         with warnings.catch_warnings():
             warnings.simplefilter("ignore")
             prob = ReactionDiffusion(vg, D=1.0, bc=(("dirichlet", (0, 0)), "neumann", "neumann"))
-        self.st = ForwardEuler(prob, 0.1 / 6, steps_per_pass=spp)
         u0 = np.random.default_rng(seed).random(self.shape)
         self.c0_host = torch.tensor(u0, dtype=torch.float32).unsqueeze(0).pin_memory()
         self.c0 = self.c0_host.to(device)
+        tuned = spp == 0
+        if tuned:   # fastest of 1, 2, 4 steps per HBM pass on this GPU
+            from evoxels_gb300.autotune import tune_fd_steps_per_pass
+            spp = tune_fd_steps_per_pass(prob, 0.1 / 6, self.c0, steps=8, use_cache=False)
+        self.st = ForwardEuler(prob, 0.1 / 6, steps_per_pass=spp)
         self.out_host = torch.empty_like(self.c0_host).pin_memory()
         self.units_per_step = self.n * self.T
         self.config = {"workload": f"fd{n}", "grid": list(self.shape), "fe_steps_per_bench_step": self.T,
                        "dt": 0.1 / 6, "D": 1.0, "bc": "dirichlet(0,0) x, neumann y, z", "steps_per_pass": spp,
+                       "steps_per_pass_autotuned": tuned,
                        "seed": seed, "l2": "inputs larger than L2 (%.2f GB per field)" % (4 * self.n / 1e9)}
 
     def step(self):
@@ -403,13 +408,15 @@ class Batched:
         return a.elapsed_time(b) / steps
 
 
-def make_workload(name, torch, device, inner=None, spp=4, shape=None):
+def make_workload(name, torch, device, inner=None, spp=0, shape=None):
     if name == "batched64_fwd":
         return Batched(torch, device, inner or 50, adjoint=False)
     if name == "batched64_fwd_adj":
         return Batched(torch, device, inner or 20, adjoint=True)
     if name == "ch256_fwd_adj":
         return ChFwdAdj(torch, device, 256, inner or 10, 6, shape=shape)
+    if name == "ch512_fwd_adj":   # large single grid: forward + adjoint with stored trajectory
+        return ChFwdAdj(torch, device, 512, inner or 10, 5, shape=shape)
     if name == "ch128_inversion":
         return ChFwdAdj(torch, device, 128, inner or 200, 3, shape=shape)
     if name == "ch100_fwd":
@@ -446,8 +453,8 @@ def cpu_sample(workload_name, torch, seconds_cap=30.0):
                     oracle.ch_imex_vjp(u, u, 0.1, float(kappa[i] / 2), 1.0, mu_hom=pin)
         units = sum(int(a) ** 3 for a in sides)
         sample = "all 64 instances, 1 IMEX step each%s, fp32" % (" + 1 adjoint step (torch autograd)" if adj else "")
-    elif workload_name in ("ch256_fwd_adj", "ch128_inversion"):
-        n = 256 if workload_name == "ch256_fwd_adj" else 128
+    elif workload_name in ("ch256_fwd_adj", "ch128_inversion", "ch512_fwd_adj"):
+        n = {"ch256_fwd_adj": 256, "ch128_inversion": 128, "ch512_fwd_adj": 512}[workload_name]
         shape = (n, n, n)
         u0 = torch.tensor(oracle.seeded_ch_field(shape, 6), dtype=torch.float32).unsqueeze(0)
         lam = torch.tensor(oracle.seeded_unit_field(shape, 7) - 0.5, dtype=torch.float32).unsqueeze(0)
@@ -502,8 +509,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--inner-steps", type=int, default=None,
                     help="override the IMEX/FE steps per bench step (profiling runs)")
-    ap.add_argument("--fd-steps-per-pass", type=int, default=4, choices=[1, 2, 4],
-                    help="temporal blocking of the finite-difference workload")
+    ap.add_argument("--fd-steps-per-pass", type=int, default=0, choices=[0, 1, 2, 4],
+                    help="temporal blocking of the finite-difference workload (0: autotuned)")
     ap.add_argument("--grid", default=None,
                     help="NX,NY,NZ: run a Cahn-Hilliard workload on another grid (profiling runs; "
                          "the metric then names the grid)")
@@ -625,7 +632,7 @@ def main():
     step_bytes = None
     if args.workload.startswith("batched"):
         step_bytes = (64 if wl.adj else 32) * wl.units_per_step
-    elif args.workload in ("ch256_fwd_adj", "ch128_inversion"):
+    elif args.workload in ("ch256_fwd_adj", "ch128_inversion", "ch512_fwd_adj"):
         step_bytes = 64 * wl.units_per_step    # 32 B forward + 32 B adjoint per voxel-step
     elif args.workload.startswith("ch"):
         step_bytes = 32 * wl.units_per_step
@@ -700,8 +707,8 @@ def run_reference(args, torch, warmup):
         shape = (int(round(units ** (1 / 3))),) * 3
         sample = "all 64 instances, 1 IMEX step each%s per bench step, fp32" % (" + 1 adjoint step" if adj else "")
         n = round(units ** (1 / 3))
-    elif wl in ("ch256_fwd_adj", "ch128_inversion"):
-        n = 256 if wl == "ch256_fwd_adj" else 128
+    elif wl in ("ch256_fwd_adj", "ch128_inversion", "ch512_fwd_adj"):
+        n = {"ch256_fwd_adj": 256, "ch128_inversion": 128, "ch512_fwd_adj": 512}[wl]
         shape = (n, n, n)
         u0 = torch.tensor(oracle.seeded_ch_field(shape, 6), dtype=torch.float32).unsqueeze(0)
         lam = torch.tensor(oracle.seeded_unit_field(shape, 7) - 0.5, dtype=torch.float32).unsqueeze(0)
