@@ -311,6 +311,9 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
     ch_stencil_grid(g, &sg, &lx);
     const double kA = (double)prm->kappa * prm->A, DA = (double)prm->D * prm->A, invD = 1.0 / (double)prm->D;
     const int gmode = spectral ? 2 : (want ? 1 : 0);
+    // spectral gradients on the fast path: the pullback's last block reduces (no reduce launch)
+    int* counter = reinterpret_cast<int*>(part + plan->n_part * 4);
+    if (spectral && (rc = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), st), "reduction counter"))) return rc;
     const float* lam = lam_in;
     for (int s = nsteps - 1; s >= 0; --s) {
         float* dst = (s % 2 == 0) ? lam_out : lbuf;
@@ -338,9 +341,13 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
         const float* hb = gmode == 1 ? hbuf : nullptr;
         const float* u1 = gmode == 1 ? us + N : nullptr;
         int nb = (int)(sg.x * sg.y * sg.z);   // generic kernel's partial sums; the fast launcher sets its own
+        bool reduced = false;
         if (fast_ok(g, {us, gbuf, lam, hb, u1, dst})) {
-            if ((rc = ch_pullback_fast_launch(gmode, us, gbuf, lam, hb, u1, dst, part, plan->n_part, g, G, P, st, &nb)))
+            const GradSink sink{grads, xpart, nxp, counter, kA, DA, invD};
+            if ((rc = ch_pullback_fast_launch(gmode, us, gbuf, lam, hb, u1, dst, part, plan->n_part, g, G, P, st, &nb,
+                                              spectral ? &sink : nullptr)))
                 return rc;
+            reduced = spectral;
         } else if (want) {
             EVX_TIMED("ch_pullback_grads", st,
                       ch_pullback_kernel<true><<<sg, dim3(32, 8), 0, st>>>(us, gbuf, lam, hb, u1, dst, part, G, P, lx));
@@ -354,10 +361,12 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
             if ((rc = check_launch("ch_pullback_kernel"))) return rc;
         }
         if (spectral) {
-            EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_spec_kernel<<<1, 256, 0, st>>>(
-                part, nb, xpart, nxp, grads, kA, DA, invD));
-            count_launch();
-            if ((rc = check_launch("ch_grad_reduce_spec_kernel"))) return rc;
+            if (!reduced) {
+                EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_spec_kernel<<<1, 256, 0, st>>>(
+                    part, nb, xpart, nxp, grads, kA, DA, invD));
+                count_launch();
+                if ((rc = check_launch("ch_grad_reduce_spec_kernel"))) return rc;
+            }
         } else if (want) {
             EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_kernel<<<1, 256, 0, st>>>(part, nb, grads, kA, DA));
             count_launch();

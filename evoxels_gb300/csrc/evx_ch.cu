@@ -451,7 +451,7 @@ int evx_ch_plan_create_bc(evx_ch_plan** out, const evx_grid* g, const evx_bc* bc
     p->off_spec = off; off += align256(2 * p->nspec * sizeof(float2));
     p->off_u = off;    off += align256(p->n * sizeof(float));
     p->off_lam = off;  off += align256(p->n * sizeof(float));
-    p->off_part = off; off += align256((size_t)p->n_part * 4 * sizeof(double));
+    p->off_part = off; off += align256((size_t)p->n_part * 4 * sizeof(double) + 16);   // + reduction counter
     p->n_xpart = p->xmode && !xext ? xpass_blocks(g->nx, g->ny * p->nzh) : 0;
     p->spec_floats = p->xmode && !xext ? xpass_spectrum_floats(g->nx, g->ny * p->nzh) : 0;
     p->off_xpart = off; off += align256(p->n_xpart * 2 * sizeof(double));

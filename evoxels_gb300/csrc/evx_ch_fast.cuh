@@ -117,10 +117,25 @@ int ch_tile_variant(int nz);   // honours evx_set_tile_variant
 
 int ch_rhs_fast_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
                        const Geo& G, const ChP& P, cudaStream_t st);
+// Final gradient reduction of the spectral-gradient pullback (grads == 2), done by
+// the block that finishes last: the blocks' partial sums (part) and the x-pass
+// Parseval partials (xpart: <lam', u'-u>, <K lam', u'-u> per block) in a fixed
+// order, dL/dD += t1/D - kappa*A*t2, dL/dkappa += sK - D*A*t2, dL/dw += sW.
+// counter must be zero before the launch; the last block resets it.
+struct GradSink {
+    double* grads;
+    const double* xpart;
+    int nxpart;
+    int* counter;
+    double kA, DA, invD;
+};
+
 // grads: 0 none, 1 all four partial sums (reads h and u1), 2 the two real-space sums only
+// (sink: optional last-block reduction for grads == 2; else part is left for a reduce kernel)
 int ch_pullback_fast_launch(int grads, const float* u, const float* g, const float* lam, const float* h,
                             const float* u1, float* lam_out, double* part, int n_part_cap, const evx_grid* grid,
-                            const Geo& G, const ChP& P, cudaStream_t st, int* n_part_used);
+                            const Geo& G, const ChP& P, cudaStream_t st, int* n_part_used,
+                            const GradSink* sink = nullptr);
 int ch_pullback_fast_blocks(const evx_grid* g);
 
 // ---- batched (persistent) kernels ------------------------------------------------

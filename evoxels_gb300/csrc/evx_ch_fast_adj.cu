@@ -78,6 +78,46 @@ __device__ __forceinline__ void block_reduce4(float a, float b, float c, float d
     }
 }
 
+// The last block to finish reduces every block's partial sums and the x-pass
+// partials in a fixed order (deterministic) and resets the counter.  Partials
+// of other blocks are read through L2 (__ldcg) after the counter handshake.
+__device__ __noinline__ void last_block_reduce(const double* part, int nblk, const GradSink& sink, double* red) {
+    __shared__ int s_last;
+    const int tid = threadIdx.x;
+    __threadfence();                       // this block's partials before its count
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(sink.counter, 1) == nblk - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double a[4] = {0.0, 0.0, 0.0, 0.0};   // sK, sW, t1, t2
+    for (int b = tid; b < nblk; b += THREADS) {
+        a[0] += __ldcg(part + (size_t)b * 4 + 1);
+        a[1] += __ldcg(part + (size_t)b * 4 + 2);
+    }
+    for (int b = tid; b < sink.nxpart; b += THREADS) {
+        a[2] += __ldcg(sink.xpart + (size_t)b * 2);
+        a[3] += __ldcg(sink.xpart + (size_t)b * 2 + 1);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        for (int o = 16; o > 0; o >>= 1) a[q] += __shfl_down_sync(0xffffffffu, a[q], o);
+    __syncthreads();                       // red was last read by block_reduce4
+    if ((tid & 31) == 0)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) red[q * 8 + (tid >> 5)] = a[q];
+    __syncthreads();
+    if (tid == 0) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int q = 0; q < 4; ++q)
+            for (int w = 0; w < THREADS / 32; ++w) t[q] += red[q * 8 + w];
+        sink.grads[0] += t[2] * sink.invD - sink.kA * t[3];
+        sink.grads[1] += t[0] - sink.DA * t[3];
+        sink.grads[2] += t[1];
+        *sink.counter = 0;
+    }
+}
+
 template <class T, int GR>
 __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const float* __restrict__ gfield,
                                               const float* __restrict__ lam, const float* __restrict__ hfield,
@@ -330,7 +370,7 @@ template <class T, int GR>
 __global__ void __launch_bounds__(THREADS, GR ? 2 : 3)
 ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ gfield, const float* __restrict__ lam,
                         const float* __restrict__ hfield, const float* __restrict__ u1, float* __restrict__ lam_out,
-                        double* __restrict__ part, Geo G, ChP P, int LX) {
+                        double* __restrict__ part, Geo G, ChP P, int LX, GradSink sink) {
     extern __shared__ __align__(16) float smem[];
     float* cs = smem;
     float* gs = cs + RING_C;
@@ -346,6 +386,7 @@ ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ g
     if (GR) {
         const size_t blk = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
         block_reduce4(sD, sK, sW, sH, red, part + blk * 4);
+        if (GR == 2 && sink.counter) last_block_reduce(part, (int)(gridDim.x * gridDim.y * gridDim.z), sink, red);
     }
 }
 
@@ -434,7 +475,9 @@ dim3 pb_grid(const evx_grid* g, int grads, int* lx) {
 template <class T>
 int pb_launch_t(int grads, const float* u, const float* g, const float* lam, const float* h, const float* u1,
                 float* lam_out, double* part, int n_part_cap, const evx_grid* grid_, const Geo& G, const ChP& P,
-                cudaStream_t st, int* n_part_used) {
+                cudaStream_t st, int* n_part_used, const GradSink* sink) {
+    const GradSink none{nullptr, nullptr, 0, nullptr, 0.0, 0.0, 0.0};
+    const GradSink S = (grads == 2 && sink) ? *sink : none;
     int lx;
     const dim3 grid = pb_grid<T>(grid_, grads, &lx);
     const int nb = (int)(grid.x * grid.y * grid.z);
@@ -442,15 +485,15 @@ int pb_launch_t(int grads, const float* u, const float* g, const float* lam, con
     if (n_part_used) *n_part_used = nb;
     if (grads == 1)
         EVX_TIMED("ch_pullback_grads", st,
-                  ch_pullback_fast_kernel<T, 1><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, lx));
+                  ch_pullback_fast_kernel<T, 1><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, lx, S));
     else if (grads == 2)
         EVX_TIMED("ch_pullback_grads_spec", st,
                   ch_pullback_fast_kernel<T, 2><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out, part,
-                                                                                 G, P, lx));
+                                                                                 G, P, lx, S));
     else
         EVX_TIMED("ch_pullback", st,
                   ch_pullback_fast_kernel<T, 0><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
-                                                                                 nullptr, G, P, lx));
+                                                                                 nullptr, G, P, lx, S));
     count_launch();
     return check_launch("ch_pullback_fast_kernel");
 }
@@ -469,11 +512,13 @@ int ch_pullback_fast_blocks(const evx_grid* g) {
 
 int ch_pullback_fast_launch(int grads, const float* u, const float* g, const float* lam, const float* h,
                             const float* u1, float* lam_out, double* part, int n_part_cap, const evx_grid* grid_,
-                            const Geo& G, const ChP& P, cudaStream_t st, int* n_part_used) {
+                            const Geo& G, const ChP& P, cudaStream_t st, int* n_part_used, const GradSink* sink) {
     init_occupancy();
     if (ch_tile_variant(grid_->nz) == 1)
-        return pb_launch_t<TileSquare>(grads, u, g, lam, h, u1, lam_out, part, n_part_cap, grid_, G, P, st, n_part_used);
-    return pb_launch_t<TileWide>(grads, u, g, lam, h, u1, lam_out, part, n_part_cap, grid_, G, P, st, n_part_used);
+        return pb_launch_t<TileSquare>(grads, u, g, lam, h, u1, lam_out, part, n_part_cap, grid_, G, P, st, n_part_used,
+                                       sink);
+    return pb_launch_t<TileWide>(grads, u, g, lam, h, u1, lam_out, part, n_part_cap, grid_, G, P, st, n_part_used,
+                                 sink);
 }
 
 int batch_pullback_blocks_per_sm(bool grads) {

@@ -304,6 +304,11 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
             issue_load((it + 1) % XSTAGES, next);
             if (MODE == 3) prefetch_l2(dspec + (size_t)next * N1 * 256, N1 * 256 * sizeof(float2));
         }
+        if (MODE == 3) {   // this tile's stored spectrum into L1 (it sits in L2 from the previous tile's prefetch)
+            const float2* dp = dspec + (size_t)tile * N1 * 256 + tid;
+#pragma unroll
+            for (int e = 0; e < N1; ++e) asm volatile("prefetch.global.L1 [%0];" ::"l"(dp + e * 256));
+        }
         if (!mbar_wait(&bar[slot], (uint32_t)(it / XSTAGES) & 1u)) atomicOr(&g_dev_status, 1);
         float2* xs = ring + (size_t)slot * TILE;
         const int m = tile * P + c.p;
