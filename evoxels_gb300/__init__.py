@@ -1,8 +1,9 @@
 """evoxels_gb300: the evoxels time-stepping hot path on NVIDIA GB300 (sm_103a).
 
 Drop-in names for the reference's torch path: ``VoxelFields``,
-``run_cahn_hilliard_solver``, ``TimeDependentSolver``, ``CahnHilliard``,
-``ReactionDiffusion``, ``PseudoSpectralIMEX``, ``ForwardEuler``.  All compute
+``run_cahn_hilliard_solver``, ``run_allen_cahn_solver``, ``TimeDependentSolver``,
+``CahnHilliard``, ``ReactionDiffusion``, ``TwoPhaseAllenCahn``,
+``PseudoSpectralIMEX``, ``ForwardEuler``, ``RungeKutta4``.  All compute
 runs in ``libevx.so`` (hand-written CUDA + cuFFT) through the C ABI declared in
 ``include/evx.h``; importing this package does not load the library, the first
 compute call does, and it raises if the library is missing.
@@ -14,11 +15,14 @@ __all__ = [
     "VoxelFields",
     "Grid",
     "run_cahn_hilliard_solver",
+    "run_allen_cahn_solver",
     "TimeDependentSolver",
     "CahnHilliard",
     "ReactionDiffusion",
+    "TwoPhaseAllenCahn",
     "PseudoSpectralIMEX",
     "ForwardEuler",
+    "RungeKutta4",
     "VoxelGridGB300",
 ]
 
@@ -27,13 +31,16 @@ def __getattr__(name):
     if name == "run_cahn_hilliard_solver":
         from .precompiled_solvers.cahn_hilliard import run_cahn_hilliard_solver
         return run_cahn_hilliard_solver
+    if name == "run_allen_cahn_solver":
+        from .precompiled_solvers.allen_cahn import run_allen_cahn_solver
+        return run_allen_cahn_solver
     if name == "TimeDependentSolver":
         from .solvers import TimeDependentSolver
         return TimeDependentSolver
-    if name in ("CahnHilliard", "ReactionDiffusion"):
+    if name in ("CahnHilliard", "ReactionDiffusion", "TwoPhaseAllenCahn"):
         from . import problem_definition
         return getattr(problem_definition, name)
-    if name in ("PseudoSpectralIMEX", "ForwardEuler"):
+    if name in ("PseudoSpectralIMEX", "ForwardEuler", "RungeKutta4"):
         from . import timesteppers
         return getattr(timesteppers, name)
     if name == "VoxelGridGB300":

@@ -42,6 +42,11 @@ class EvxChParams(C.Structure):
                 ("sym_coef", C.c_float), ("dt", C.c_float)]
 
 
+class EvxAcParams(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("w", "eps", "gab", "M", "force", "three_over_eps", "curvature",
+                                         "one_minus_curvature")]
+
+
 class EvxBatchInstance(C.Structure):
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("reserved", C.c_int32),
                 ("h", C.c_double * 3), ("inv_h", C.c_float * 3), ("inv_h2", C.c_float * 3),
@@ -77,6 +82,8 @@ _SIGS = {
     "evx_ch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_spectrum_floats": (C.c_size_t, [_P]),
     "evx_device_status": (C.c_int, [C.c_int]),
+    "evx_ac_rhs": (C.c_int, [_P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.POINTER(EvxAcParams), _P]),
+    "evx_rk4_combine": (C.c_int, [_P, _P, _P, _P, _P, C.c_float, _P, C.c_size_t, _P]),
     "evx_fft_yz_r2c": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
     "evx_fft_yz_c2r": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
     "evx_ch_forward_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),

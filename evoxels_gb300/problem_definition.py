@@ -198,3 +198,67 @@ class ReactionDiffusion(_BCMixin):
             _lib.check(L.evx_rd_rhs(u[ch].data_ptr(), out[ch].data_ptr(), g, self._evx_bc,
                                     float(np.float32(self.D)), cuda_stream()), "evx_rd_rhs")
         return out
+
+
+def ac_params(eps, gab, M, force, curvature, w=None):
+    """``EvxAcParams``: float32 roundings of the python-double values the
+    reference's TwoPhaseAllenCahn.rhs uses (evoxels/problem_definition.py:420-447)."""
+    f = lambda x: float(np.float32(x))  # noqa: E731
+    p = _lib.EvxAcParams()
+    p.w = f(18 / eps if w is None else w)
+    p.eps = f(eps)
+    p.gab = f(gab)
+    p.M = f(M)
+    p.force = f(force)
+    p.three_over_eps = f(3 / eps)
+    p.curvature = f(curvature)
+    p.one_minus_curvature = f(1 - curvature)
+    return p
+
+
+@dataclass
+class TwoPhaseAllenCahn(_BCMixin):
+    """Two-phase Allen-Cahn (evoxels/problem_definition.py:374-447) on the GPU:
+    ``M*(gab*(curvature*L(phi) + (1-curvature)*N(phi) - potential/2/eps)
+    + 3/eps*phi*(1-phi)*force)`` with the 19-point normal Laplacian N, every BC
+    kind, in one fused kernel.  ``potential`` must be the double-well form
+    ``w*u*(1-u)*(1-2u)`` (the default ``w = 18/eps``, or a pinned coefficient)."""
+    vg: VoxelGridGB300
+    eps: float = 2.0
+    gab: float = 1.0
+    M: float = 1.0
+    force: float = 0.0
+    curvature: float = 0.01
+    potential: Callable | None = None
+    bc: tuple = ("neumann", "neumann", "neumann")
+    _fourier_symbol: Any = field(init=False, repr=False, default=None)
+
+    def __post_init__(self):
+        self.initialize_boundary_conditions()
+        self._w = double_well_coefficient(self.potential, self.eps)
+        if self.potential is None:
+            eps = self.eps
+            self.potential = lambda u, lib=None: 18 / eps * u * (1 - u) * (1 - 2 * u)
+        self._params = ac_params(self.eps, self.gab, self.M, self.force, self.curvature, self._w)
+
+    @property
+    def order(self):
+        return 2
+
+    @property
+    def fourier_symbol(self):
+        """``-M*gab*k^2`` as a tensor (evoxels/problem_definition.py:389)."""
+        if self._fourier_symbol is None:
+            self._fourier_symbol = -self.M * self.gab * self.k_squared()
+        return self._fourier_symbol
+
+    def rhs(self, t, phi):
+        """d phi/dt for every channel (evoxels/problem_definition.py:420-447)."""
+        phi = self.vg.check_field(phi)
+        out = torch.empty_like(phi)
+        g = self.vg.evx_grid()
+        L = _lib.lib()
+        for ch in range(phi.shape[0]):
+            _lib.check(L.evx_ac_rhs(phi[ch].data_ptr(), out[ch].data_ptr(), g, self._evx_bc, self._params,
+                                    cuda_stream()), "evx_ac_rhs")
+        return out

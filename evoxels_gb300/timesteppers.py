@@ -183,3 +183,37 @@ class ForwardEuler(TimeStepper):
                                         float(np.float32(pr.D)), float(np.float32(self.dt)), int(nsteps),
                                         int(self.steps_per_pass), cuda_stream()), "evx_fd_forward")
         return out
+
+
+@dataclass
+class RungeKutta4(TimeStepper):
+    """Classical explicit Runge-Kutta scheme of order 4 (evoxels/timesteppers.py:46-61)
+    for any problem with a GPU ``rhs``: four rhs evaluations, the stage inputs
+    ``u + c*k`` and the final ``u + dt/6*(k1 + 2k2 + 2k3 + k4)`` as fused
+    elementwise kernels, in the reference's float32 operation order."""
+    problem: object
+    dt: float
+
+    @property
+    def order(self) -> int:
+        return 4
+
+    def _stage(self, u, k, c):
+        out = torch.empty_like(u)
+        _lib.check(_lib.lib().evx_fe_update(u.data_ptr(), k.data_ptr(), float(np.float32(c)), out.data_ptr(),
+                                            u.numel(), cuda_stream()), "evx_fe_update")
+        return out
+
+    def step(self, t, u):
+        u = self.problem.vg.check_field(u)
+        dt = self.dt
+        k1 = self.problem.rhs(t, u)
+        k2 = self.problem.rhs(t + 0.5 * dt, self._stage(u, k1, 0.5 * dt))
+        k3 = self.problem.rhs(t + 0.5 * dt, self._stage(u, k2, 0.5 * dt))
+        k4 = self.problem.rhs(t + dt, self._stage(u, k3, dt))
+        out = torch.empty_like(u)
+        _lib.check(_lib.lib().evx_rk4_combine(u.data_ptr(), k1.data_ptr(), k2.data_ptr(), k3.data_ptr(),
+                                              k4.data_ptr(), float(np.float32(dt / 6)), out.data_ptr(),
+                                              u.numel(), cuda_stream()), "evx_rk4_combine")
+        return out
+

@@ -70,6 +70,14 @@ typedef struct evx_ch_params {
     float D, kappa, w, A, sym_coef, dt;
 } evx_ch_params;
 
+/* Two-phase Allen-Cahn parameters (evoxels/problem_definition.py:374-447), the
+ * float32 roundings of the python-double values the reference uses:
+ *   w = 18/eps by default (potential w*c*(1-c)*(1-2c)), eps, gab, M, force,
+ *   three_over_eps = 3/eps, curvature, one_minus_curvature = 1 - curvature. */
+typedef struct evx_ac_params {
+    float w, eps, gab, M, force, three_over_eps, curvature, one_minus_curvature;
+} evx_ac_params;
+
 /* ---- library info -------------------------------------------------------- */
 const char* evx_last_error(void);
 int evx_version(void);
@@ -123,6 +131,19 @@ int evx_fd_adjoint(const float* lam_in, float* lam_out, float* scratch,
 int evx_fe_update(const float* u, const float* r, float dt, float* out, size_t n, void* stream);
 
 /* ---- Cahn-Hilliard path ---------------------------------------------------- */
+
+/* TwoPhaseAllenCahn.rhs (evoxels/problem_definition.py:420-447) for any BC:
+ * clip, double-well potential, curvature-weighted 7-point Laplacian plus the
+ * 19-point normal Laplacian (evoxels/fd_stencils.py:77-103), bit-identical to
+ * the reference's float32 arithmetic.  u and r: (nx, ny, nz) float32. */
+int evx_ac_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc,
+               const evx_ac_params* p, void* stream);
+
+/* RungeKutta4.step's combination (evoxels/timesteppers.py:61):
+ * out = u + dt6*(((k1 + 2*k2) + 2*k3) + k4), dt6 = float32(dt/6); the stage
+ * inputs u + c*k are evx_fe_update. */
+int evx_rk4_combine(const float* u, const float* k1, const float* k2, const float* k3, const float* k4,
+                    float dt6, float* out, size_t n, void* stream);
 
 /* CahnHilliard.rhs (evoxels/problem_definition.py:328-371) for any BC. */
 int evx_ch_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc,

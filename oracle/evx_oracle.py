@@ -33,6 +33,14 @@ __all__ = [
     "rfft_k_squared",
     "imex_prefac",
     "imex_step",
+    "rfft_k_squared_nonperiodic",
+    "x_bc_kind",
+    "pad_fft",
+    "grad_center",
+    "normal_laplace",
+    "ac_rhs",
+    "rk4_step",
+    "ac_rk4_run",
     "fe_step",
     "ch_imex_run",
     "rd_fe_run",
@@ -376,6 +384,77 @@ def ch_imex_loss_grads(c0, target, nsteps, dt=0.1, eps=3.0, D=1.0, A=0.25,
 # ----------------------------------------------------------------------------
 # Seeded inputs and error metric
 # ----------------------------------------------------------------------------
+
+# ----------------------------------------------------------------------------
+# Two-phase Allen-Cahn and the classical Runge-Kutta scheme
+# ----------------------------------------------------------------------------
+
+def grad_center(padded, axis, div_dx):
+    """``0.5*(f[i+1] - f[i-1]) * div_dx[axis]`` at cell centres (evoxels/fd_stencils.py:44-54)."""
+    hi = [slice(None), slice(1, -1), slice(1, -1), slice(1, -1)]
+    lo = list(hi)
+    hi[axis + 1] = slice(2, None)
+    lo[axis + 1] = slice(None, -2)
+    return 0.5 * (padded[tuple(hi)] - padded[tuple(lo)]) * div_dx[axis]
+
+
+def normal_laplace(padded, div_dx, div_dx2):
+    """Normal part of the Laplacian, compact 19-point stencil (evoxels/fd_stencils.py:77-103):
+    face second differences weighted by the squared centred gradients, plus the
+    mixed second differences of each plane weighted by gradient products, over
+    ``|grad|^2`` (set to 1 where ``|grad|^2 <= 1e-7``)."""
+    f = padded
+    C = f[:, 1:-1, 1:-1, 1:-1]
+    L, R = f[:, :-2, 1:-1, 1:-1], f[:, 2:, 1:-1, 1:-1]
+    B, T = f[:, 1:-1, :-2, 1:-1], f[:, 1:-1, 2:, 1:-1]
+    Bk, F = f[:, 1:-1, 1:-1, :-2], f[:, 1:-1, 1:-1, 2:]
+    gx, gy, gz = (grad_center(f, a, div_dx) for a in range(3))
+    n = gx ** 2 * (R - 2 * C + L) * div_dx2[0] + \
+        gy ** 2 * (T - 2 * C + B) * div_dx2[1] + \
+        gz ** 2 * (F - 2 * C + Bk) * div_dx2[2] + \
+        0.5 * gx * gy * (f[:, 2:, 2:, 1:-1] + f[:, :-2, :-2, 1:-1] -
+                         f[:, :-2, 2:, 1:-1] - f[:, 2:, :-2, 1:-1]) * div_dx[0] * div_dx[1] + \
+        0.5 * gx * gz * (f[:, 2:, 1:-1, 2:] + f[:, :-2, 1:-1, :-2] -
+                         f[:, :-2, 1:-1, 2:] - f[:, 2:, 1:-1, :-2]) * div_dx[0] * div_dx[2] + \
+        0.5 * gy * gz * (f[:, 1:-1, 2:, 2:] + f[:, 1:-1, :-2, :-2] -
+                         f[:, 1:-1, :-2, 2:] - f[:, 1:-1, 2:, :-2]) * div_dx[1] * div_dx[2]
+    norm2 = gx ** 2 + gy ** 2 + gz ** 2
+    norm2[norm2 <= 1e-7] = 1.0
+    return n / norm2
+
+
+def ac_rhs(phi, eps=2.0, gab=1.0, M=1.0, force=0.0, curvature=0.01, bc=None, spacing=(1.0, 1.0, 1.0),
+           potential=None):
+    """``TwoPhaseAllenCahn.rhs`` (evoxels/problem_definition.py:420-447); BCs default to
+    Neumann on every axis as the reference's dataclass default."""
+    bc = normalize_bc(("neumann", "neumann", "neumann") if bc is None else bc)
+    div_dx, div_dx2 = grid_factors(spacing, phi.dtype)
+    phi = torch.clip(phi, 0, 1)
+    pot = potential(phi) if potential is not None else 18 / eps * phi * (1 - phi) * (1 - 2 * phi)
+    phi_pad = pad_bc(phi, bc)
+    lap = curvature * laplace(phi_pad, div_dx2)
+    n_lap = (1 - curvature) * normal_laplace(phi_pad, div_dx, div_dx2)
+    df = gab * (lap + n_lap - pot / 2 / eps) + 3 / eps * phi * (1 - phi) * force
+    return M * df
+
+
+def rk4_step(u, dt, rhs_fn):
+    """``RungeKutta4.step`` (evoxels/timesteppers.py:46-61)."""
+    k1 = rhs_fn(u)
+    k2 = rhs_fn(u + 0.5 * dt * k1)
+    k3 = rhs_fn(u + 0.5 * dt * k2)
+    k4 = rhs_fn(u + dt * k3)
+    return u + (dt / 6) * (k1 + 2 * k2 + 2 * k3 + k4)
+
+
+def ac_rk4_run(u0, nsteps, dt=0.5, eps=2.0, gab=1.0, M=1.0, force=0.0, curvature=0.01, bc=None,
+               spacing=(1.0, 1.0, 1.0)):
+    """``nsteps`` RungeKutta4 steps of TwoPhaseAllenCahn (``run_allen_cahn_solver``'s scheme)."""
+    u = u0
+    for _ in range(nsteps):
+        u = rk4_step(u, dt, lambda v: ac_rhs(v, eps, gab, M, force, curvature, bc, spacing))
+    return u
+
 
 def seeded_ch_field(shape, seed):
     """``0.5 + 0.1*U[0,1)`` from ``np.random.default_rng(seed)`` (float64, ``(Nx,Ny,Nz)``)."""

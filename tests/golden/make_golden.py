@@ -132,6 +132,33 @@ def main():
         out[f"ch_imex_nx_{i}"] = dict(u0=u0, u=u.numpy(), shape=np.array(shape), eps=eps, D=D, dt=dt, n=n,
                                       bc=np.array(repr(bc)))
 
+    # 3c) TwoPhaseAllenCahn.rhs (19-point normal Laplacian, every BC kind, flat clipped
+    #     regions for the |grad|^2 <= 1e-7 branch) and RungeKutta4 steps
+    ac_cases = [((10, 9, 8), 41, None, dict()),
+                ((8, 12, 10), 42, ("periodic", "periodic", "periodic"), dict(eps=3.0, curvature=0.2)),
+                ((9, 8, 11), 43, (("dirichlet", (0.0, 1.0)), "neumann", "periodic"),
+                 dict(eps=1.5, gab=0.7, M=1.3, force=0.4, curvature=0.05)),
+                ((7, 10, 9), 44, ("periodic", ("dirichlet", (0.2, 0.9)), ("dirichlet", (1.0, 0.0))),
+                 dict(eps=2.5, curvature=0.5))]
+    ac_cases.append(((12, 10, 8), 45, None, dict(curvature=0.1)))   # blocky: flat clipped halves
+    for i, (shape, seed, bc, kw) in enumerate(ac_cases):
+        _, vg = make_vg(R, shape)
+        if bc is not None:
+            kw = dict(kw, bc=bc)
+        prob = PD.TwoPhaseAllenCahn(vg, **kw)
+        u0 = 1.4 * unit_field(shape, seed) - 0.2
+        if i == 4:   # two flat half-spaces (|grad|^2 = 0) with a noisy slab between them
+            u0 = np.where(np.arange(shape[0])[:, None, None] < shape[0] // 2, 1.3, -0.2) + 0 * u0
+            u0[5:7] = unit_field((2,) + shape[1:], seed)
+        u = vg.init_scalar_field(u0)
+        r = prob.rhs(0.0, u)
+        st = TS.RungeKutta4(prob, 0.1)
+        v = u
+        for _ in range(3):
+            v = st.step(0.0, v)
+        out[f"ac_{i}"] = dict(u0=u0, rhs=r.numpy(), u3=v.numpy(), shape=np.array(shape), bc=np.array(repr(bc)),
+                              kw=np.array(repr(kw)))
+
     # 4) true FP64 CH IMEX (default dtype float64 so the k-grid is fp64 too)
     torch.set_default_dtype(torch.float64)
     shape = (16, 16, 16)

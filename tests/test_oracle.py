@@ -68,6 +68,22 @@ def test_ch_imex_nonperiodic_x_matches_reference(i):
     assert oracle.rel_to_max(g["u"], u64.numpy()) < 1e-6
 
 
+@pytest.mark.parametrize("i", range(5))
+def test_allen_cahn_rhs_and_rk4_match_reference(i):
+    """TwoPhaseAllenCahn.rhs (19-point normal Laplacian) and three RungeKutta4 steps, bit-exact."""
+    g = load_golden(f"ac_{i}")
+    bc = parse_bc(g["bc"])
+    kw = eval(str(g["kw"]))   # the fixture's own repr of the keyword dict
+    kw.pop("bc", None)
+    u0 = t32(g["u0"])
+    r = oracle.ac_rhs(u0, bc=bc, **kw)
+    assert np.array_equal(r.numpy(), g["rhs"])
+    v = u0
+    for _ in range(3):
+        v = oracle.rk4_step(v, 0.1, lambda w: oracle.ac_rhs(w, bc=bc, **kw))
+    assert np.array_equal(v.numpy(), g["u3"])
+
+
 def test_ch_imex_fp64_matches_reference():
     g = load_golden("ch_imex_fp64")
     u0 = torch.tensor(g["u0"], dtype=torch.float64).unsqueeze(0)
