@@ -8,7 +8,7 @@ gradient, then 10 adjoint steps giving dL/dc0, dL/dD and dL/deps.  A
 voxel-step counts one forward plus one adjoint step of one voxel.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch512_fwd_adj|ch128_inversion]
+                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch512_fwd_adj|ch128_inversion|ac256_rk4|batched64_fwd|batched64_fwd_adj]
 
 ``--impl reference`` times the CPU oracle (the operation-by-operation torch
 restatement of the reference's own torch path; the reference itself is pure
@@ -85,6 +85,8 @@ def algorithmic_bytes(slot, n, nspec):
         "fd_step": 8 * n,
         "fd_tblock2": 8 * n,
         "fd_tblock4": 8 * n,
+        "ac_rhs": 8 * n,            # read phi, write the rhs (19-point stencil, halos from L2)
+        "rk4_combine": 24 * n,      # read u, k1..k4; write u'
     }
     return table.get(slot)
 
@@ -261,6 +263,49 @@ class ChForward:
         return 4 * self.n, 4 * self.n
 
 
+class AcRk4:
+    """Two-phase Allen-Cahn, RungeKutta4 (run_allen_cahn_solver's scheme), 256^3, Neumann BCs,
+    reference defaults (eps 2, gab 1, M 1, force 0, curvature 0.01), dt 0.5."""
+
+    def __init__(self, torch, device, n=256, steps_per=20, seed=7, shape=None):
+        from evoxels_gb300.problem_definition import TwoPhaseAllenCahn
+        from evoxels_gb300.timesteppers import RungeKutta4
+        from evoxels_gb300.voxelfields import VoxelFields
+        from evoxels_gb300.voxelgrid import VoxelGridGB300
+        self.torch = torch
+        self.shape = tuple(shape) if shape else (n, n, n)
+        self.n = int(np.prod(self.shape))
+        self.nspec = 0
+        self.T = steps_per
+        vf = VoxelFields(self.shape, domain_size=self.shape)
+        vg = VoxelGridGB300(vf.grid_info(), device=device)
+        self.st = RungeKutta4(TwoPhaseAllenCahn(vg), 0.5)
+        u0 = np.random.default_rng(seed).random(self.shape)
+        self.c0_host = torch.tensor(u0, dtype=torch.float32).unsqueeze(0).pin_memory()
+        self.c0 = self.c0_host.to(device)
+        self.out_host = torch.empty_like(self.c0_host).pin_memory()
+        self.units_per_step = self.n * self.T
+        self.config = {"workload": "ac%d_rk4" % self.shape[0], "grid": list(self.shape), "rk4_steps_per_bench_step": self.T,
+                       "dt": 0.5, "eps": 2.0, "gab": 1.0, "M": 1.0, "force": 0.0, "curvature": 0.01,
+                       "bc": "neumann x, y, z", "seed": seed,
+                       "l2": "working set (state, 4 stages, stage input) larger than L2"}
+
+    def step(self):
+        u = self.c0
+        for _ in range(self.T):
+            u = self.st.step(0.0, u)
+        return u
+
+    def step_e2e(self):
+        self.c0.copy_(self.c0_host, non_blocking=True)
+        u = self.step()
+        self.out_host.copy_(u, non_blocking=True)
+        self.torch.cuda.current_stream().synchronize()
+
+    def e2e_bytes(self):
+        return 4 * self.n, 4 * self.n
+
+
 class FdForward:
     """Explicit FD diffusion, 512^3, Dirichlet x / Neumann y,z, dt = 1/60 (config 2)."""
 
@@ -423,6 +468,8 @@ def make_workload(name, torch, device, inner=None, spp=0, shape=None):
         return ChForward(torch, device, 100, inner or 100, 1, shape=shape)
     if name == "ch512_fwd":
         return ChForward(torch, device, 512, inner or 20, 5, shape=shape)
+    if name == "ac256_rk4":
+        return AcRk4(torch, device, 256, inner or 20, 7, shape=shape)
     if name == "fd512":
         return FdForward(torch, device, 512, inner or 100, 2, spp=spp)
     raise SystemExit(f"unknown workload {name}")
@@ -473,6 +520,15 @@ def cpu_sample(workload_name, torch, seconds_cap=30.0):
             oracle.ch_imex_run(u0, 1, 0.1)
         units = n ** 3
         sample = f"{n}^3, 1 IMEX step, fp32"
+    elif workload_name == "ac256_rk4":
+        n = 256
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_unit_field(shape, 7), dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            oracle.ac_rk4_run(u0, 1, 0.5)
+        units = n ** 3
+        sample = f"{n}^3, 1 Allen-Cahn RungeKutta4 step, fp32"
     else:
         n = 512
         shape = (n, n, n)
@@ -638,6 +694,8 @@ def main():
         step_bytes = 32 * wl.units_per_step
     elif args.workload.startswith("fd"):
         step_bytes = 8 * wl.units_per_step
+    elif args.workload.startswith("ac"):
+        step_bytes = 92 * wl.units_per_step    # 4 x rhs 8 + 3 x stage input 12 + combine 24
     step_roofline = None
     if step_bytes:
         gbs = step_bytes * args.steps / (ms / 1e3) / 1e9
@@ -726,6 +784,14 @@ def run_reference(args, torch, warmup):
         def one():
             return oracle.ch_imex_run(u0, 1, 0.1)
         sample = f"{n}^3: 1 IMEX step per bench step, fp32"
+    elif wl == "ac256_rk4":
+        n = 256
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_unit_field(shape, 7), dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            return oracle.ac_rk4_run(u0, 1, 0.5)
+        sample = f"{n}^3: 1 Allen-Cahn RungeKutta4 step per bench step, fp32"
     else:
         n = 512
         shape = (n, n, n)
