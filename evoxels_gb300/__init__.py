@@ -3,7 +3,8 @@
 Drop-in names for the reference's torch path: ``VoxelFields``,
 ``run_cahn_hilliard_solver``, ``run_allen_cahn_solver``, ``TimeDependentSolver``,
 ``CahnHilliard``, ``ReactionDiffusion``, ``TwoPhaseAllenCahn``,
-``PseudoSpectralIMEX``, ``ForwardEuler``, ``RungeKutta4``.  All compute
+``PseudoSpectralIMEX``, ``ForwardEuler``, ``RungeKutta4``, ``ExponentialEuler``,
+``RKC1``, ``RKC2``.  All compute
 runs in ``libevx.so`` (hand-written CUDA + cuFFT) through the C ABI declared in
 ``include/evx.h``; importing this package does not load the library, the first
 compute call does, and it raises if the library is missing.
@@ -23,6 +24,9 @@ __all__ = [
     "PseudoSpectralIMEX",
     "ForwardEuler",
     "RungeKutta4",
+    "ExponentialEuler",
+    "RKC1",
+    "RKC2",
     "VoxelGridGB300",
 ]
 
@@ -40,7 +44,7 @@ def __getattr__(name):
     if name in ("CahnHilliard", "ReactionDiffusion", "TwoPhaseAllenCahn"):
         from . import problem_definition
         return getattr(problem_definition, name)
-    if name in ("PseudoSpectralIMEX", "ForwardEuler", "RungeKutta4"):
+    if name in ("PseudoSpectralIMEX", "ForwardEuler", "RungeKutta4", "ExponentialEuler", "RKC1", "RKC2"):
         from . import timesteppers
         return getattr(timesteppers, name)
     if name == "VoxelGridGB300":

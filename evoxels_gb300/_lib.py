@@ -47,6 +47,10 @@ class EvxAcParams(C.Structure):
                                          "one_minus_curvature")]
 
 
+class EvxRkcCoeffs(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("mu0", "nu", "one_minus_mu0_nu", "mu1_dt", "gamma_dt")]
+
+
 class EvxBatchInstance(C.Structure):
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("reserved", C.c_int32),
                 ("h", C.c_double * 3), ("inv_h", C.c_float * 3), ("inv_h2", C.c_float * 3),
@@ -77,6 +81,7 @@ _SIGS = {
     "evx_ch_plan_create_bc": (C.c_int, [C.POINTER(_P), C.POINTER(EvxGrid), C.POINTER(EvxBC), C.c_int]),
     "evx_ch_plan_destroy": (C.c_int, [_P]),
     "evx_ch_workspace_bytes": (C.c_size_t, [_P]),
+    "evx_spectral_update": (C.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "evx_ch_step": (C.c_int, [_P, _P, _P, C.POINTER(EvxChParams), _P, _P]),
     "evx_ch_forward": (C.c_int, [_P, _P, _P, C.c_int, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
@@ -84,6 +89,7 @@ _SIGS = {
     "evx_device_status": (C.c_int, [C.c_int]),
     "evx_ac_rhs": (C.c_int, [_P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.POINTER(EvxAcParams), _P]),
     "evx_rk4_combine": (C.c_int, [_P, _P, _P, _P, _P, C.c_float, _P, C.c_size_t, _P]),
+    "evx_rkc_stage": (C.c_int, [_P, _P, _P, _P, _P, C.POINTER(EvxRkcCoeffs), _P, C.c_size_t, _P]),
     "evx_fft_yz_r2c": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
     "evx_fft_yz_c2r": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
     "evx_ch_forward_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),

@@ -1,7 +1,8 @@
 // Two-phase Allen-Cahn right-hand side (evoxels/problem_definition.py:374-447)
 // with the compact 19-point normal Laplacian (evoxels/fd_stencils.py:77-103),
-// and the combination step of the classical Runge-Kutta scheme
-// (evoxels/timesteppers.py:46-61).  Compiled with --fmad=false: every float32
+// the combination step of the classical Runge-Kutta scheme
+// (evoxels/timesteppers.py:46-61) and the stage recursion of the
+// Runge-Kutta-Chebyshev schemes (evoxels/timesteppers.py:202-295).  Compiled with --fmad=false: every float32
 // operation rounds separately, in the reference's order, so results are
 // bit-identical to the reference's torch arithmetic.
 //
@@ -141,6 +142,23 @@ __global__ void rk4_combine_kernel(const float* __restrict__ u, const float* __r
     }
 }
 
+// RKC stage (evoxels/timesteppers.py:237-243, 286-294), left to right:
+//   out = mu0*yc + nu*yp + omn*u + m1dt*r [+ gdt*r0]
+template <bool R0>
+__global__ void rkc_stage_kernel(const float* __restrict__ u, const float* __restrict__ yc,
+                                 const float* __restrict__ yp, const float* __restrict__ r,
+                                 const float* __restrict__ r0, float mu0, float nu, float omn, float m1dt, float gdt,
+                                 float* __restrict__ out, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+        float s = __fadd_rn(__fmul_rn(mu0, __ldg(yc + e)), __fmul_rn(nu, __ldg(yp + e)));
+        s = __fadd_rn(s, __fmul_rn(omn, __ldg(u + e)));
+        s = __fadd_rn(s, __fmul_rn(m1dt, __ldg(r + e)));
+        if constexpr (R0) s = __fadd_rn(s, __fmul_rn(gdt, __ldg(r0 + e)));
+        out[e] = s;
+    }
+}
+
 }  // namespace
 }  // namespace evx
 
@@ -180,6 +198,24 @@ int evx_rk4_combine(const float* u, const float* k1, const float* k2, const floa
     EVX_TIMED("rk4_combine", st, rk4_combine_kernel<<<blocks, 256, 0, st>>>(u, k1, k2, k3, k4, dt6, out, n));
     count_launch();
     return check_launch("rk4_combine_kernel");
+}
+
+int evx_rkc_stage(const float* u, const float* y_curr, const float* y_prev, const float* r, const float* r0,
+                  const evx_rkc_coeffs* c, float* out, size_t n, void* stream) {
+    if (!u || !y_curr || !y_prev || !r || !out || !c) return fail(EVX_ERR_BAD_ARG, "NULL pointer");
+    if (n == 0) return EVX_OK;
+    cudaStream_t st = as_stream(stream);
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)152 * 16);
+    if (r0)
+        EVX_TIMED("rkc_stage", st, (rkc_stage_kernel<true><<<blocks, 256, 0, st>>>(
+                                        u, y_curr, y_prev, r, r0, c->mu0, c->nu, c->one_minus_mu0_nu, c->mu1_dt,
+                                        c->gamma_dt, out, n)));
+    else
+        EVX_TIMED("rkc_stage", st, (rkc_stage_kernel<false><<<blocks, 256, 0, st>>>(
+                                        u, y_curr, y_prev, r, nullptr, c->mu0, c->nu, c->one_minus_mu0_nu, c->mu1_dt,
+                                        0.f, out, n)));
+    count_launch();
+    return check_launch("rkc_stage_kernel");
 }
 
 }  // extern "C"

@@ -193,6 +193,29 @@ __global__ void ch_mirror_x_kernel(float* __restrict__ r, int nx, size_t plane, 
     }
 }
 
+// dst = [src, sign * src mirrored along x]: the x extension of a field of nx
+// planes into 2*nx planes (evoxels/boundary_conditions.py:64-70).
+__global__ void mirror_copy_x_kernel(const float* __restrict__ src, float* __restrict__ dst, int nx, size_t plane,
+                                     float sign) {
+    const size_t half = (size_t)nx * plane, stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < half; e += stride) {
+        const size_t j = e / plane, yz = e - j * plane;
+        dst[e] = __ldg(src + e);
+        dst[half + e] = sign * __ldg(src + ((size_t)nx - 1 - j) * plane + yz);
+    }
+}
+
+// spec[i] = (spec[i] * mult[i]) * invN: a real multiplier table on the spectrum
+// (evoxels/timesteppers.py:197) and the 1/N of torch's "backward" irfftn.
+__global__ void spec_mult_kernel(float2* __restrict__ spec, const float* __restrict__ mult, float invN, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+        const float2 a = spec[e];
+        const float m = __ldg(mult + e);
+        spec[e] = make_float2(__fmul_rn(__fmul_rn(a.x, m), invN), __fmul_rn(__fmul_rn(a.y, m), invN));
+    }
+}
+
 // spec[i,j,k] = (spec * prefac) * invN, prefac = dt * (1/(1 - dt*(sym_coef*k4)))
 // (evoxels/timesteppers.py:77,87 and torch's 1/N "backward" irfftn scaling).
 __global__ void ch_kspace_fwd_kernel(float2* __restrict__ spec, int ny, int nzh, size_t total,
@@ -471,6 +494,49 @@ int evx_ch_plan_destroy(evx_ch_plan* p) {
 }
 
 size_t evx_ch_workspace_bytes(const evx_ch_plan* p) { return p ? p->total : 0; }
+
+int evx_spectral_update(evx_ch_plan* plan, const float* u, const float* r, const float* mult, float* out,
+                        void* workspace, void* stream) {
+    if (!plan) return fail(EVX_ERR_BAD_ARG, "plan is NULL");
+    if (!u || !r || !mult || !out) return fail(EVX_ERR_BAD_ARG, "NULL pointer");
+    if (r == out || mult == out) return fail(EVX_ERR_BAD_ARG, "rhs and multiplier must not alias the output");
+    cudaStream_t st = as_stream(stream);
+    int rc = ch_plan_bind(plan, workspace, st, false);
+    if (rc) return rc;
+    const evx_grid* g = &plan->g;
+    const size_t N = plan->n;
+    float* rbuf = reinterpret_cast<float*>(ws_at(workspace, plan->off_r));
+    float* upd = reinterpret_cast<float*>(ws_at(workspace, plan->off_upd));
+    float2* spec = reinterpret_cast<float2*>(ws_at(workspace, plan->off_spec));
+    const float invN = (float)(1.0 / ((double)plan->nxe * g->ny * g->nz));
+    if (plan->xmode) {   // (y, z) transforms of the nx planes; the x-pass extends, transforms, multiplies
+        if ((rc = ch_r2c(plan, r, spec, st))) return rc;
+        const ChP P{};
+        XpassArgs a = xpass_args(plan, 4, spec, P);
+        a.mult = mult;
+        if ((rc = xpass_launch(a, st))) return rc;
+    } else {
+        const float* src = r;
+        if (plan->xext) {
+            EVX_TIMED("mirror_copy_x", st, mirror_copy_x_kernel<<<elementwise_grid(N), 256, 0, st>>>(
+                r, rbuf, g->nx, (size_t)g->ny * g->nz, plan->xext == 2 ? -1.f : 1.f));
+            count_launch();
+            if ((rc = check_launch("mirror_copy_x_kernel"))) return rc;
+            src = rbuf;
+        }
+        if ((rc = ch_r2c(plan, src, spec, st))) return rc;
+        EVX_TIMED("spec_mult", st, spec_mult_kernel<<<elementwise_grid(plan->nspec), 256, 0, st>>>(
+            spec, mult, invN, plan->nspec));
+        count_launch();
+        if ((rc = check_launch("spec_mult_kernel"))) return rc;
+    }
+    if ((rc = ch_c2r(plan, spec, upd, false, st))) return rc;
+    // the first nx planes of the (extended) inverse transform: u + update[:, :nx]
+    EVX_TIMED("ch_axpy", st, ch_axpy_kernel<<<elementwise_grid(N / 4 + 1), 256, 0, st>>>(
+        u, upd, out, nullptr, N, nullptr));
+    count_launch();
+    return check_launch("ch_axpy_kernel");
+}
 
 size_t evx_ch_spectrum_floats(const evx_ch_plan* p) { return p ? p->spec_floats : 0; }
 

@@ -76,7 +76,8 @@ struct XpassArgs {
     const float *kx2, *ky2, *kz2;
     float sym, dt, invN;
     int* n_xpart_out;                  // optional: partial-sum slots written (mode 3)
-    int ext;                           // x mirror extension (mode 0): 1 even, 2 odd; nx = transform length / 2
+    int ext;                           // x mirror extension (mode 0 / 4): 1 even, 2 odd; nx = transform length
+    const float* mult;                 // mode 4: multiplier table [kx < nx][pencil < M]
 };
 // Batched x-pass (one launch per shape group of the batched path): per-instance
 // spectrum offset and IMEX constants, indexed by blockIdx.y.

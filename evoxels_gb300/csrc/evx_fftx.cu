@@ -62,13 +62,15 @@ __device__ int g_dev_status;       // bit 0: an x-pass barrier wait gave up
 // Multiplier stage: forward DFT over k2, multiply, inverse DFT, conjugate
 // twiddle into xs[k1][j] (N2 > 1) or back into v (N2 == 1).  MODE 0 forward
 // (optional store of the product to dsp), 1 adjoint g, 2 adjoint g and h (into
-// hv), 3 adjoint g with the Parseval sums against dsp.  dsp points at the
-// tile's stored spectrum ([element][thread], thread offset included).
+// hv), 3 adjoint g with the Parseval sums against dsp, 4 multiplier table
+// (mult[kx*M + pencil], mrow = mult + pencil).  dsp points at the tile's stored
+// spectrum ([element][thread], thread offset included).
 template <int N1, int N2, int MODE>
 __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 2 ? N1 : 1], float2* xs,
                                           const Col<N1, N2>& c, float ky2v, float kz2v, float wz,
                                           const float* __restrict__ kx2, float sym_coef, float dt, float invN,
-                                          float2* __restrict__ dsp, float& t1, float& t2) {
+                                          float2* __restrict__ dsp, float& t1, float& t2,
+                                          const float* __restrict__ mrow = nullptr, int M = 0) {
     constexpr int N = N1 * N2, Q = N1 / N2;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -81,7 +83,10 @@ __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 
         for (int k2 = 0; k2 < N2; ++k2) {
             const int kx = k1 + N1 * k2;
             const float k2s = __fadd_rn(__fadd_rn(__ldg(kx2 + kx), ky2v), kz2v);
-            if constexpr (MODE == 0) {
+            if constexpr (MODE == 4) {
+                const float mv = __ldg(mrow + (size_t)kx * M);
+                a[k2] = make_float2(__fmul_rn(__fmul_rn(a[k2].x, mv), invN), __fmul_rn(__fmul_rn(a[k2].y, mv), invN));
+            } else if constexpr (MODE == 0) {
                 const float pre = imex_prefac(k2s, sym_coef, dt);
                 a[k2] = make_float2(__fmul_rn(__fmul_rn(a[k2].x, pre), invN), __fmul_rn(__fmul_rn(a[k2].y, pre), invN));
                 if (dsp) dsp[(q * N2 + k2) * 256] = a[k2];
@@ -151,7 +156,8 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 2 : EVX_XPASS_MIN_BLOCKS)
 xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __restrict__ dspec,
              double* __restrict__ xpart, int M, int nzh, int nz,
              const float* __restrict__ kx2, const float* __restrict__ ky2, const float* __restrict__ kz2,
-             float sym_coef, float dt, float invN, const XBatchInst* __restrict__ xb) {
+             float sym_coef, float dt, float invN, const XBatchInst* __restrict__ xb,
+             const float* __restrict__ mult = nullptr) {
     if (xb) {
         const XBatchInst X = xb[blockIdx.y];
         spec += X.soff;
@@ -187,7 +193,8 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
     }
     fwd_stage1<N1, N2>(v, xs, c);
     float2 hv[MODE == 2 ? N1 : 1];
-    mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2);
+    mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2,
+                            mult + mc, M);
     auto store = [&](float2* dst) {
         if (live) {
 #pragma unroll
@@ -269,7 +276,8 @@ template <int N1, int N2, int MODE>
 __global__ void __launch_bounds__(256, N1 >= 32 ? 1 : 2)
 xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ dspec, double* __restrict__ xpart,
                  int M, int nzh, int nz, int ntiles, const float* __restrict__ kx2, const float* __restrict__ ky2,
-                 const float* __restrict__ kz2, float sym_coef, float dt, float invN) {
+                 const float* __restrict__ kz2, float sym_coef, float dt, float invN,
+                 const float* __restrict__ mult) {
     using C = Col<N1, N2>;
     constexpr int P = 256 / N2, N = C::N;
     constexpr int TILE = N * P;                       // complex values per tile
@@ -322,7 +330,8 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         for (int n1 = 0; n1 < N1; ++n1) v[n1] = xs[(N2 * n1 + c.n2) * P + c.p];
         fwd_stage1<N1, N2>(v, xs, c);
         float2 hv[1];
-        mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2);
+        mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2,
+                                mult + mc, M);
         inv_stage1<N1, N2>(v, xs, c);
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) xs[(N2 * n1 + c.n2) * P + c.p] = v[n1];
@@ -385,7 +394,7 @@ int xpass_launch_tile(const XpassArgs& A, cudaStream_t st, const char* slot) {
     EVX_TIMED(slot, st,
               (xpass_kernel<N1, N2, MODE, EXT><<<blocks, 256, smem, st>>>(A.spec, A.spec_h, A.dspec, A.xpart, A.M,
                                                                         A.nzh, A.nz, A.kx2, A.ky2, A.kz2, A.sym,
-                                                                        A.dt, A.invN, nullptr)));
+                                                                        A.dt, A.invN, nullptr, A.mult)));
     count_launch();
     return check_launch("xpass_kernel");
 }
@@ -423,7 +432,8 @@ int xpass_launch_tma(const XpassArgs& A, cudaStream_t st, const char* slot) {
     if (A.n_xpart_out) *A.n_xpart_out = blocks;
     EVX_TIMED(slot, st,
               xpass_tma_kernel<N1, N2, MODE><<<blocks, 256, smem, st>>>(tm, A.dspec, A.xpart, A.M, A.nzh, A.nz, ntiles,
-                                                                      A.kx2, A.ky2, A.kz2, A.sym, A.dt, A.invN));
+                                                                      A.kx2, A.ky2, A.kz2, A.sym, A.dt, A.invN,
+                                                                      A.mult));
     count_launch();
     return check_launch("xpass_tma_kernel");
 }
@@ -431,7 +441,7 @@ int xpass_launch_tma(const XpassArgs& A, cudaStream_t st, const char* slot) {
 template <int N1, int N2, int MODE>
 int xpass_launch_m(const XpassArgs& A, cudaStream_t st) {
     const char* slot = MODE == 0 ? (A.dspec ? "ch_xpass_fwd_store" : "ch_xpass_fwd")
-                                 : (MODE == 3 ? "ch_xpass_adj_spec" : "ch_xpass_adj");
+                                 : (MODE == 3 ? "ch_xpass_adj_spec" : (MODE == 4 ? "xpass_mult" : "ch_xpass_adj"));
     if constexpr (MODE != 2) {
         // TMA needs 16-byte row strides (even M) and a 16-byte aligned base; small M keeps the per-tile kernel
         const bool tma = !g_tma_off && (A.M % 2) == 0 && A.M >= 256 &&
@@ -444,7 +454,11 @@ int xpass_launch_m(const XpassArgs& A, cudaStream_t st) {
 template <int N1, int N2>
 int xpass_launch_t(const XpassArgs& A, cudaStream_t st) {
     if (A.ext) {   // mirrored-x forward step: per-tile kernel (odd or even extension)
-        if (A.mode != 0 || A.dspec) return fail(EVX_ERR_UNSUPPORTED, "mirrored-x x-pass: forward only");
+        if ((A.mode != 0 && A.mode != 4) || A.dspec)
+            return fail(EVX_ERR_UNSUPPORTED, "mirrored-x x-pass: forward only");
+        if (A.mode == 4)
+            return A.ext == 2 ? xpass_launch_tile<N1, N2, 4, 2>(A, st, "xpass_mult_mirror")
+                              : xpass_launch_tile<N1, N2, 4, 1>(A, st, "xpass_mult_mirror");
         return A.ext == 2 ? xpass_launch_tile<N1, N2, 0, 2>(A, st, "ch_xpass_fwd_mirror")
                           : xpass_launch_tile<N1, N2, 0, 1>(A, st, "ch_xpass_fwd_mirror");
     }
@@ -452,7 +466,8 @@ int xpass_launch_t(const XpassArgs& A, cudaStream_t st) {
         case 0: return xpass_launch_m<N1, N2, 0>(A, st);
         case 1: return xpass_launch_m<N1, N2, 1>(A, st);
         case 2: return xpass_launch_m<N1, N2, 2>(A, st);
-        default: return xpass_launch_m<N1, N2, 3>(A, st);
+        case 3: return xpass_launch_m<N1, N2, 3>(A, st);
+        default: return xpass_launch_m<N1, N2, 4>(A, st);
     }
 }
 
@@ -503,7 +518,7 @@ int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, 
             attr[mode] = true;
         }
         EVX_TIMED(slot, st, (kern<<<grid, 256, smem, st>>>(spec, spec_h, nullptr, nullptr, M, nzh, nz, kx2, ky2, kz2,
-                                                           0.f, 0.f, 0.f, xb)));
+                                                           0.f, 0.f, 0.f, xb, nullptr)));
         count_launch();
         return check_launch("xpass_kernel (batched)");
     };
@@ -536,8 +551,9 @@ int xpass_batch_launch(int mode, int nx, float2* spec, float2* spec_h, const XBa
 int xpass_launch(const XpassArgs& A, cudaStream_t st) {
     int rc = xpass_init();
     if (rc) return rc;
-    if ((A.mode == 3 && (!A.dspec || !A.xpart)) || (A.mode == 2 && !A.spec_h))
+    if ((A.mode == 3 && (!A.dspec || !A.xpart)) || (A.mode == 2 && !A.spec_h) || (A.mode == 4 && !A.mult))
         return fail(EVX_ERR_BAD_ARG, "x-pass mode %d is missing a buffer", A.mode);
+    if (A.mode < 0 || A.mode > 4) return fail(EVX_ERR_BAD_ARG, "x-pass mode %d", A.mode);
     switch (A.nx) {
         case 8: return xpass_launch_t<8, 1>(A, st);
         case 16: return xpass_launch_t<16, 1>(A, st);

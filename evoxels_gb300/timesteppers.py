@@ -6,6 +6,9 @@ constructor, ``order`` and functional ``step(t, u) -> u``.  Both add
 ``advance(u, nsteps)``, which runs ``nsteps`` steps inside the library (the
 IMEX update fused into the next step's rhs pass, forward Euler temporally
 blocked), and which ``TimeDependentSolver`` uses between output frames.
+``RungeKutta4`` (:46-61), ``ExponentialEuler`` (:136-199), ``RKC1`` (:202-244)
+and ``RKC2`` (:246-295) drive any problem whose ``rhs`` runs in the library,
+their stage combinations as fused kernels in the reference's float32 order.
 """
 
 from __future__ import annotations
@@ -217,3 +220,165 @@ class RungeKutta4(TimeStepper):
                                               u.numel(), cuda_stream()), "evx_rk4_combine")
         return out
 
+
+@dataclass
+class ExponentialEuler(TimeStepper):
+    """Exponential Euler / ETD1 (evoxels/timesteppers.py:136-199; Hochbruck,
+    Lubich, Selhofer 1998): ``u + irfftn(dt*phi1(dt*L)*rfftn(pad(rhs(u))))``
+    for any problem with a GPU ``rhs`` and a ``fourier_symbol`` L.  The
+    multiplier table ``dt*phi1(dt*L)`` is built once on the grid's device with
+    the reference's formula (Pade(6,6) for |z| < 0.5); each step is the
+    problem's rhs kernel plus ``evx_spectral_update`` (cuFFT over (y, z), the
+    x-pass with the table multiply and the x mirror extension fused, or cuFFT
+    3-D for other Nx)."""
+    problem: object
+    dt: float
+
+    def __post_init__(self):
+        self.problem.verify_fft_bc_config()
+        self.pad = self.problem.pad_fft_bc
+        self.phi_1_k_squared = self.phi1(self.dt * self.problem.fourier_symbol)
+        self._mult = (self.dt * self.phi_1_k_squared).to(torch.float32).contiguous()
+        self._plan = get_plan(self.problem.vg, bc=self.problem.bc)
+
+    def phi1(self, z):
+        """``(exp(z) - 1)/z`` with the degree-6 Pade form where |z| < 0.5
+        (evoxels/timesteppers.py:154-169)."""
+        Q = 6
+        N = [1, 1 / 26, 5 / 156, 1 / 858, 1 / 5720, 1 / 205920, 1 / 8648640]
+        D = [1, -6 / 13, 5 / 52, -5 / 429, 1 / 1144, -1 / 25740, 1 / 1235520]
+        phi = (torch.exp(z) - 1) / z
+        indx = torch.abs(z) < 0.5
+        return self.problem.vg.set(phi, indx, self.phiPade(z[indx], Q, N, D))
+
+    def phiPade(self, z, Q, Ncoeff, Dcoeff):
+        """``P_Q(z)/R_Q(z)`` by Horner's rule (evoxels/timesteppers.py:171-189)."""
+        numerator = Ncoeff[Q]
+        denominator = Dcoeff[Q]
+        for k in range(Q - 1, -1, -1):
+            numerator = numerator * z + Ncoeff[k]
+            denominator = denominator * z + Dcoeff[k]
+        return numerator / denominator
+
+    @property
+    def order(self) -> int:
+        return 1
+
+    def step(self, t, u):
+        u = self.problem.vg.check_field(u)
+        if u.shape[0] != 1:
+            # the reference transforms over (C, Nx, Ny, Nz) and so couples channels;
+            # evoxels_gb300 builds the single-field step only
+            raise NotImplementedError("ExponentialEuler in evoxels_gb300 steps one field (C == 1)")
+        r = self.problem.rhs(t, u)
+        out = torch.empty_like(u)
+        p = self._plan
+        _lib.check(_lib.lib().evx_spectral_update(p.handle, u.data_ptr(), r.data_ptr(), self._mult.data_ptr(),
+                                                  out.data_ptr(), p.workspace.data_ptr(), cuda_stream()),
+                   "evx_spectral_update")
+        return out
+
+
+def _rkc_chebyshev(polygrad, damping):
+    """``w0``, ``s`` and the Chebyshev values ``T_s(w0)``, ``T_s'(w0)`` for the
+    stage coefficients of evoxels/timesteppers.py:214-217, 258-261, as float32
+    CPU tensors (the reference's ``vg.to_backend`` / ``vg.arange`` precision)."""
+    w0 = torch.tensor(1 + damping / polygrad ** 2, dtype=torch.float32)
+    s = torch.arange(0, polygrad + 1, dtype=torch.float32)
+    theta = torch.arccosh(w0)
+    T = torch.cosh(s * theta)
+    dT = s * torch.sinh(s * theta) / torch.sqrt(w0 ** 2 - 1)
+    return w0, s, T, dT
+
+
+class _RKC(TimeStepper):
+    """Shared step of the Runge-Kutta-Chebyshev schemes: ``polygrad`` rhs
+    evaluations; the first stage is ``evx_fe_update`` with ``mu11*dt``, every
+    later one a fused ``evx_rkc_stage`` over (u, Y_curr, Y_prev, rhs[, rhs_0]).
+    The coefficients are float32 tensors, so ``mu1[j]*dt`` and friends round as
+    in the reference."""
+
+    _second_order = False
+
+    def _stage_coeffs(self, j):
+        dt = self.dt
+        c = _lib.EvxRkcCoeffs()
+        c.mu0 = float(self.mu0[j])
+        c.nu = float(self.nu[j])
+        c.one_minus_mu0_nu = float(1 - self.mu0[j] - self.nu[j])
+        c.mu1_dt = float(self.mu1[j] * dt)
+        c.gamma_dt = float(self.gamma[j] * dt) if self._second_order else 0.0
+        return c
+
+    def step(self, t, u):
+        u = self.problem.vg.check_field(u)
+        L = _lib.lib()
+        n = u.numel()
+        rhs0 = self.problem.rhs(t, u)
+        y_prev, y_curr = u, torch.empty_like(u)
+        _lib.check(L.evx_fe_update(u.data_ptr(), rhs0.data_ptr(), float(self.mu11 * self.dt), y_curr.data_ptr(), n,
+                                   cuda_stream()), "evx_fe_update")
+        r0 = rhs0.data_ptr() if self._second_order else None
+        for j in range(self.polygrad - 1):
+            rhs = self.problem.rhs(t + float(self.c[j] * self.dt), y_curr)
+            y_new = torch.empty_like(u)
+            _lib.check(L.evx_rkc_stage(u.data_ptr(), y_curr.data_ptr(), y_prev.data_ptr(), rhs.data_ptr(), r0,
+                                       C.byref(self._stage_coeffs(j)), y_new.data_ptr(), n, cuda_stream()),
+                       "evx_rkc_stage")
+            y_prev, y_curr = y_curr, y_new
+        return y_curr
+
+
+@dataclass
+class RKC1(_RKC):
+    """Runge-Kutta-Chebyshev scheme of order 1 (evoxels/timesteppers.py:202-244;
+    Verwer, Hundsdorfer, Sommeijer 1990) for any problem with a GPU ``rhs``."""
+    problem: object
+    dt: float
+    polygrad: int = 4
+    damping: float = 0.05
+
+    def __post_init__(self):
+        w0, s, T, dT = _rkc_chebyshev(self.polygrad, self.damping)
+        b = 1 / T
+        w1 = T[-1] / dT[-1]
+        self.mu0 = 2 * w0 * (b[2:] / b[1:-1])
+        self.mu1 = 2 * w1 * (b[2:] / b[1:-1])
+        self.mu11 = w1 / w0
+        self.nu = -(b[2:] / b[:-2])
+        self.c = w1 * (dT / T)[1:-1]
+
+    @property
+    def order(self) -> int:
+        return 1
+
+
+@dataclass
+class RKC2(_RKC):
+    """Runge-Kutta-Chebyshev scheme of order 2 (evoxels/timesteppers.py:246-295)
+    for any problem with a GPU ``rhs``."""
+    problem: object
+    dt: float
+    polygrad: int = 4
+    damping: float = 2 / 13
+
+    _second_order = True
+
+    def __post_init__(self):
+        w0, s, T, dT = _rkc_chebyshev(self.polygrad, self.damping)
+        d2T = (s * s * T - w0 * dT) / (w0 ** 2 - 1)
+        b = d2T / dT ** 2
+        b[0] = b[2]
+        b[1] = b[2]
+        w1 = dT[-1] / d2T[-1]
+        self.mu0 = 2 * w0 * (b[2:] / b[1:-1])
+        self.mu1 = 2 * w1 * (b[2:] / b[1:-1])
+        self.mu11 = b[1] * w1
+        self.nu = -(b[2:] / b[:-2])
+        self.gamma = -(1 - b[1:-1] * T[1:-1]) * self.mu1
+        self.c = w1 * (d2T / dT)[1:-1]
+        self.c[0] = self.c[1] / dT[2]
+
+    @property
+    def order(self) -> int:
+        return 2

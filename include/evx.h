@@ -145,6 +145,21 @@ int evx_ac_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc,
 int evx_rk4_combine(const float* u, const float* k1, const float* k2, const float* k3, const float* k4,
                     float dt6, float* out, size_t n, void* stream);
 
+/* One Runge-Kutta-Chebyshev stage coefficient set (float32, as the reference's
+ * tensors hold them): mu0[j], nu[j], (1 - mu0[j]) - nu[j], mu1[j]*dt and, for
+ * RKC2, gamma[j]*dt (evoxels/timesteppers.py:219-229, 263-280). */
+typedef struct evx_rkc_coeffs {
+    float mu0, nu, one_minus_mu0_nu, mu1_dt, gamma_dt;
+} evx_rkc_coeffs;
+
+/* RKC1.step / RKC2.step stage recursion (evoxels/timesteppers.py:237-243,
+ * 286-294): out = mu0*y_curr + nu*y_prev + (1-mu0-nu)*u + mu1*dt*r
+ * [+ gamma*dt*r0], summed left to right, each product rounded.  r0 = NULL
+ * drops the last term (RKC1).  The first stage u + mu11*dt*rhs(u) is
+ * evx_fe_update. */
+int evx_rkc_stage(const float* u, const float* y_curr, const float* y_prev, const float* r, const float* r0,
+                  const evx_rkc_coeffs* c, float* out, size_t n, void* stream);
+
 /* CahnHilliard.rhs (evoxels/problem_definition.py:328-371) for any BC. */
 int evx_ch_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc,
                const evx_ch_params* p, void* stream);
@@ -178,6 +193,14 @@ int evx_ch_plan_destroy(evx_ch_plan* plan);
 
 /* Bytes of device workspace (256-byte aligned start) the plan's calls need. */
 size_t evx_ch_workspace_bytes(const evx_ch_plan* plan);
+
+/* ExponentialEuler.step's spectral update (evoxels/timesteppers.py:195-199)
+ * for any rhs on the plan's grid: out = u + irfftn(mult * rfftn(pad_fft(r)))[:nx],
+ * pad_fft the plan's x extension (evoxels/boundary_conditions.py:61-71).  mult is
+ * the real multiplier table dt*phi1(dt*symbol) over the (extended) rfft grid,
+ * [nxe][ny][nz/2+1] float32 on the device.  r and u are read only. */
+int evx_spectral_update(evx_ch_plan* plan, const float* u, const float* r, const float* mult, float* out,
+                        void* workspace, void* stream);
 
 /* One PseudoSpectralIMEX step of CahnHilliard (evoxels/timesteppers.py:85-89):
  * u_out = u_in + irfftn(prefac * rfftn(rhs(u_in))).  u_in is read only. */

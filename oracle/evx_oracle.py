@@ -41,6 +41,10 @@ __all__ = [
     "ac_rhs",
     "rk4_step",
     "ac_rk4_run",
+    "rkc_coeffs",
+    "rkc_step",
+    "phi1",
+    "etd1_multiplier",
     "fe_step",
     "ch_imex_run",
     "rd_fe_run",
@@ -302,6 +306,29 @@ def imex_step(u, prefac, rhs_fn, bc=None):
     return u + update
 
 
+def phi1(z):
+    """``ExponentialEuler.phi1`` (evoxels/timesteppers.py:154-189): ``(exp(z)-1)/z``,
+    and where |z| < 0.5 the (6,6) Pade form of Hochbruck, Lubich, Selhofer
+    (1998) by Horner's rule, in ``z``'s dtype."""
+    num = [1, 1 / 26, 5 / 156, 1 / 858, 1 / 5720, 1 / 205920, 1 / 8648640]
+    den = [1, -6 / 13, 5 / 52, -5 / 429, 1 / 1144, -1 / 25740, 1 / 1235520]
+    phi = (torch.exp(z) - 1) / z
+    small = torch.abs(z) < 0.5
+    zs = z[small]
+    p, q = num[6], den[6]
+    for k in range(5, -1, -1):
+        p = p * zs + num[k]
+        q = q * zs + den[k]
+    phi[small] = p / q
+    return phi
+
+
+def etd1_multiplier(symbol, dt):
+    """The ETD1 spectral multiplier ``dt * phi1(dt * symbol)``
+    (evoxels/timesteppers.py:148,197); one ETD1 step is ``imex_step`` with it."""
+    return dt * phi1(dt * symbol)
+
+
 def fe_step(u, dt, rhs_fn):
     """``ForwardEuler.step`` (evoxels/timesteppers.py:42-43): ``u + dt*rhs``."""
     return u + dt * rhs_fn(u)
@@ -454,6 +481,55 @@ def ac_rk4_run(u0, nsteps, dt=0.5, eps=2.0, gab=1.0, M=1.0, force=0.0, curvature
     for _ in range(nsteps):
         u = rk4_step(u, dt, lambda v: ac_rhs(v, eps, gab, M, force, curvature, bc, spacing))
     return u
+
+
+def rkc_coeffs(order, polygrad=4, damping=None, dtype=torch.float64):
+    """Stage coefficients of RKC1 (evoxels/timesteppers.py:214-229) or RKC2
+    (evoxels/timesteppers.py:258-280) from the Chebyshev polynomials T_s at
+    w0 = 1 + damping/s^2 (Verwer, Hundsdorfer, Sommeijer 1990), in ``dtype``."""
+    if damping is None:
+        damping = 0.05 if order == 1 else 2 / 13
+    w0 = torch.tensor(1 + damping / polygrad ** 2, dtype=dtype)
+    s = torch.arange(0, polygrad + 1, dtype=dtype)
+    acw = torch.arccosh(w0)
+    T = torch.cosh(s * acw)
+    dT = s * torch.sinh(s * acw) / torch.sqrt(w0 ** 2 - 1)
+    k = {}
+    if order == 1:
+        b = 1 / T
+        w1 = T[-1] / dT[-1]
+        k["mu11"] = w1 / w0
+        k["c"] = w1 * (dT / T)[1:-1]
+    else:
+        d2T = (s * s * T - w0 * dT) / (w0 ** 2 - 1)
+        b = d2T / dT ** 2
+        b[0] = b[2]
+        b[1] = b[2]
+        w1 = dT[-1] / d2T[-1]
+        k["mu11"] = b[1] * w1
+        c = w1 * (d2T / dT)[1:-1]
+        c[0] = c[1] / dT[2]
+        k["c"] = c
+    k["mu0"] = 2 * w0 * (b[2:] / b[1:-1])
+    k["mu1"] = 2 * w1 * (b[2:] / b[1:-1])
+    k["nu"] = -(b[2:] / b[:-2])
+    if order == 2:
+        k["gamma"] = -(1 - b[1:-1] * T[1:-1]) * k["mu1"]
+    return k
+
+
+def rkc_step(u, dt, rhs_fn, k):
+    """One RKC1 / RKC2 step (evoxels/timesteppers.py:235-244, 284-295) with the
+    coefficients ``k`` of :func:`rkc_coeffs`; RKC2 when ``k`` has ``gamma``."""
+    r0 = rhs_fn(u)
+    y_prev, y = u, u + k["mu11"] * dt * r0
+    for j in range(len(k["mu0"])):
+        r = rhs_fn(y)
+        y_new = k["mu0"][j] * y + k["nu"][j] * y_prev + (1 - k["mu0"][j] - k["nu"][j]) * u + k["mu1"][j] * dt * r
+        if "gamma" in k:
+            y_new = y_new + k["gamma"][j] * dt * r0
+        y_prev, y = y, y_new
+    return y
 
 
 def seeded_ch_field(shape, seed):

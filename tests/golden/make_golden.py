@@ -159,6 +159,53 @@ def main():
         out[f"ac_{i}"] = dict(u0=u0, rhs=r.numpy(), u3=v.numpy(), shape=np.array(shape), bc=np.array(repr(bc)),
                               kw=np.array(repr(kw)))
 
+    # 3d) RKC1 / RKC2 steps over three problems' rhs; the float32 stage coefficients
+    #     are stored too (libm may round cosh/arccosh differently on another host)
+    rkc_cases = [("RKC1", "TwoPhaseAllenCahn", (10, 9, 8), 61, None, dict(), 0.1, {}),
+                 ("RKC2", "TwoPhaseAllenCahn", (8, 12, 10), 62, (("dirichlet", (0.0, 1.0)), "neumann", "periodic"),
+                  dict(eps=1.5, curvature=0.05), 0.2, {}),
+                 ("RKC1", "ReactionDiffusion", (9, 8, 7), 63, ("neumann", "periodic", ("dirichlet", (1.0, 0.0))),
+                  dict(D=1.0), 0.05, dict(polygrad=7, damping=0.1)),
+                 ("RKC2", "ReactionDiffusion", (8, 8, 8), 64, None, dict(D=0.8), 0.2, dict(polygrad=6)),
+                 ("RKC2", "CahnHilliard", (8, 10, 12), 65, None, dict(eps=3.0, D=1.0), 0.01, {})]
+    for i, (scheme, pname, shape, seed, bc, kw, dt, skw) in enumerate(rkc_cases):
+        _, vg = make_vg(R, shape)
+        if bc is not None:
+            kw = dict(kw, bc=bc)
+        prob = getattr(PD, pname)(vg, **kw)
+        u0 = (1.4 * unit_field(shape, seed) - 0.2) if pname != "CahnHilliard" else ch_field(shape, seed)
+        st = getattr(TS, scheme)(prob, dt, **skw)
+        u = vg.init_scalar_field(u0)
+        for _ in range(3):
+            u = st.step(0.0, u)
+        co = {k: getattr(st, k).numpy() for k in ("mu0", "mu1", "mu11", "nu", "c", "gamma") if hasattr(st, k)}
+        out[f"rkc_{i}"] = dict(u0=u0, u3=u.numpy(), shape=np.array(shape), bc=np.array(repr(bc)), kw=np.array(repr(kw)),
+                               scheme=np.array(scheme), problem=np.array(pname), dt=dt, skw=np.array(repr(skw)),
+                               **co)
+
+    # 3e) ExponentialEuler (ETD1, Pade phi1) steps: periodic and mirrored x, power-of-two
+    #     and other nx, three problems; the phi1 table is stored too
+    etd_cases = [("CahnHilliard", (8, 10, 12), 71, None, dict(eps=3.0, D=1.0), 0.05),
+                 ("CahnHilliard", (12, 8, 10), 72, ("neumann", "periodic", "periodic"), dict(eps=2.0, D=0.7), 0.1),
+                 ("ReactionDiffusion", (10, 8, 8), 73, (("dirichlet", (0.2, 1.0)), "periodic", "periodic"),
+                  dict(D=1.0), 0.5),
+                 ("TwoPhaseAllenCahn", (8, 8, 12), 74, ("periodic", "periodic", "periodic"), dict(eps=2.0), 0.3),
+                 ("CahnHilliard", (16, 12, 10), 75, (("dirichlet", (0.0, 1.0)), "periodic", "periodic"),
+                  dict(eps=3.0, D=1.0), 0.1)]
+    for i, (pname, shape, seed, bc, kw, dt) in enumerate(etd_cases):
+        _, vg = make_vg(R, shape)
+        if bc is not None:
+            kw = dict(kw, bc=bc)
+        prob = getattr(PD, pname)(vg, **kw)
+        u0 = ch_field(shape, seed) if pname == "CahnHilliard" else unit_field(shape, seed)
+        st = TS.ExponentialEuler(prob, dt)
+        u = vg.init_scalar_field(u0)
+        for _ in range(3):
+            u = st.step(0.0, u)
+        out[f"etd1_{i}"] = dict(u0=u0, u3=u.numpy(), shape=np.array(shape), bc=np.array(repr(bc)),
+                                kw=np.array(repr(kw)), problem=np.array(pname), dt=dt,
+                                phi1=st.phi_1_k_squared.numpy())
+
     # 4) true FP64 CH IMEX (default dtype float64 so the k-grid is fp64 too)
     torch.set_default_dtype(torch.float64)
     shape = (16, 16, 16)

@@ -84,6 +84,85 @@ def test_allen_cahn_rhs_and_rk4_match_reference(i):
     assert np.array_equal(v.numpy(), g["u3"])
 
 
+def rkc_case(g, dtype=torch.float32):
+    """(rhs function, kwargs of the scheme) of an ``rkc_*`` fixture."""
+    bc = parse_bc(g["bc"])
+    kw = eval(str(g["kw"]))   # the fixture's own repr of the keyword dict
+    kw.pop("bc", None)
+    pname = str(g["problem"])
+    if pname == "TwoPhaseAllenCahn":
+        fn = lambda w: oracle.ac_rhs(w, bc=bc, **kw)  # noqa: E731
+    elif pname == "ReactionDiffusion":
+        fn = lambda w: oracle.rd_rhs(w, D=kw["D"], bc=bc)  # noqa: E731
+    else:
+        fn = lambda w: oracle.ch_rhs(w, eps=kw["eps"], D=kw["D"], bc=bc)  # noqa: E731
+    return fn, eval(str(g["skw"]))
+
+
+@pytest.mark.parametrize("i", range(5))
+def test_rkc_matches_reference(i):
+    """RKC1 / RKC2: stage coefficients and three steps over AC, RD and CH rhs."""
+    g = load_golden(f"rkc_{i}")
+    fn, skw = rkc_case(g)
+    order = 1 if str(g["scheme"]) == "RKC1" else 2
+    k32 = oracle.rkc_coeffs(order, dtype=torch.float32, **skw)
+    for name, v in k32.items():   # the host's libm may differ from the fixture's by an ulp
+        np.testing.assert_allclose(v.numpy(), g[name], rtol=3e-7, atol=0)
+    kg = {name: torch.tensor(g[name]) for name in k32}
+    v = t32(g["u0"])
+    for _ in range(3):
+        v = oracle.rkc_step(v, float(g["dt"]), fn, kg)
+    assert np.array_equal(v.numpy(), g["u3"])
+    k64 = oracle.rkc_coeffs(order, **skw)
+    v = torch.tensor(g["u0"]).unsqueeze(0)
+    for _ in range(3):
+        v = oracle.rkc_step(v, float(g["dt"]), fn, k64)
+    assert oracle.rel_to_max(v.numpy(), g["u3"]) < 1e-5
+
+
+def etd1_case(g, dtype=torch.float32):
+    """(symbol, rhs function, bc) of an ``etd1_*`` fixture in ``dtype``."""
+    bc = parse_bc(g["bc"])
+    kw = eval(str(g["kw"]))   # the fixture's own repr of the keyword dict
+    kw.pop("bc", None)
+    shape = tuple(int(x) for x in g["shape"])
+    mirrored = oracle.x_bc_kind(bc) in ("neumann", "dirichlet")
+    k2 = (oracle.rfft_k_squared_nonperiodic if mirrored else oracle.rfft_k_squared)(shape, dtype=dtype)
+    pname = str(g["problem"])
+    if pname == "CahnHilliard":
+        sym = -2 * kw["eps"] * kw["D"] * 0.25 * k2 ** 2
+        fn = lambda w: oracle.ch_rhs(w, eps=kw["eps"], D=kw["D"], bc=bc)  # noqa: E731
+    elif pname == "ReactionDiffusion":
+        sym = -kw["D"] * 0.25 * k2
+        fn = lambda w: oracle.rd_rhs(w, D=kw["D"], bc=bc)  # noqa: E731
+    else:
+        sym = -1.0 * 1.0 * k2
+        fn = lambda w: oracle.ac_rhs(w, bc=bc, **kw)  # noqa: E731
+    return sym, fn, bc
+
+
+@pytest.mark.parametrize("i", range(5))
+def test_etd1_matches_reference(i):
+    """ExponentialEuler: the phi1 table and three steps (fp32: identical torch ops)."""
+    g = load_golden(f"etd1_{i}")
+    dt = float(g["dt"])
+    sym, fn, bc = etd1_case(g)
+    # float32 exp of this host against the fixture's: an ulp or so on the table
+    np.testing.assert_allclose(oracle.phi1(dt * sym).numpy(), g["phi1"], rtol=3e-7, atol=0)
+    mult = oracle.etd1_multiplier(sym, dt)
+    v = t32(g["u0"])
+    for _ in range(3):
+        v = oracle.imex_step(v, mult, fn, bc)
+    assert oracle.rel_to_max(v.numpy(), g["u3"]) < 1e-6
+    sym64, fn64, _ = etd1_case(g, torch.float64)
+    np.testing.assert_allclose(oracle.phi1(dt * sym64).numpy(), g["phi1"], rtol=2e-6, atol=0)
+    m64 = oracle.etd1_multiplier(sym64, dt)
+    v = torch.tensor(g["u0"]).unsqueeze(0)
+    for _ in range(3):
+        v = oracle.imex_step(v, m64, fn64, bc)
+    assert oracle.rel_to_max(v.numpy(), g["u3"]) < 1e-5
+
+
 def test_ch_imex_fp64_matches_reference():
     g = load_golden("ch_imex_fp64")
     u0 = torch.tensor(g["u0"], dtype=torch.float64).unsqueeze(0)
