@@ -8,7 +8,7 @@ gradient, then 10 adjoint steps giving dL/dc0, dL/dD and dL/deps.  A
 voxel-step counts one forward plus one adjoint step of one voxel.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch512_fwd_adj|ch128_inversion|ac256_rk4|batched64_fwd|batched64_fwd_adj]
+                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch512_fwd_adj|ch128_inversion|ac256_rk4|ac256_rkc2|ch256_etd1|batched64_fwd|batched64_fwd_adj]
 
 ``--impl reference`` times the CPU oracle (the operation-by-operation torch
 restatement of the reference's own torch path; the reference itself is pure
@@ -87,6 +87,13 @@ def algorithmic_bytes(slot, n, nspec):
         "fd_tblock4": 8 * n,
         "ac_rhs": 8 * n,            # read phi, write the rhs (19-point stencil, halos from L2)
         "rk4_combine": 24 * n,      # read u, k1..k4; write u'
+        "fe_update": 12 * n,        # read u, r; write u + c*r
+        "rkc_stage": 20 * n,        # read u, Y_curr, Y_prev, rhs; write Y_new
+        "rkc2_stage": 24 * n,       # ... and rhs_0
+        "xpass_mult": 20 * nspec,   # read + write the (y,z)-transformed spectrum, read the multiplier table
+        "spec_mult": 20 * nspec,
+        "mirror_copy_x": 12 * n,    # read r; write its 2*nx-plane extension
+        "rd_rhs": 8 * n,
     }
     return table.get(slot)
 
@@ -264,12 +271,13 @@ class ChForward:
 
 
 class AcRk4:
-    """Two-phase Allen-Cahn, RungeKutta4 (run_allen_cahn_solver's scheme), 256^3, Neumann BCs,
-    reference defaults (eps 2, gab 1, M 1, force 0, curvature 0.01), dt 0.5."""
+    """Two-phase Allen-Cahn, RungeKutta4 (run_allen_cahn_solver's scheme) or RKC2
+    (polygrad 4), 256^3, Neumann BCs, reference defaults (eps 2, gab 1, M 1,
+    force 0, curvature 0.01), dt 0.5."""
 
-    def __init__(self, torch, device, n=256, steps_per=20, seed=7, shape=None):
+    def __init__(self, torch, device, n=256, steps_per=20, seed=7, shape=None, scheme="rk4"):
         from evoxels_gb300.problem_definition import TwoPhaseAllenCahn
-        from evoxels_gb300.timesteppers import RungeKutta4
+        from evoxels_gb300.timesteppers import RKC2, RungeKutta4
         from evoxels_gb300.voxelfields import VoxelFields
         from evoxels_gb300.voxelgrid import VoxelGridGB300
         self.torch = torch
@@ -279,16 +287,59 @@ class AcRk4:
         self.T = steps_per
         vf = VoxelFields(self.shape, domain_size=self.shape)
         vg = VoxelGridGB300(vf.grid_info(), device=device)
-        self.st = RungeKutta4(TwoPhaseAllenCahn(vg), 0.5)
+        self.st = (RungeKutta4 if scheme == "rk4" else RKC2)(TwoPhaseAllenCahn(vg), 0.5)
         u0 = np.random.default_rng(seed).random(self.shape)
         self.c0_host = torch.tensor(u0, dtype=torch.float32).unsqueeze(0).pin_memory()
         self.c0 = self.c0_host.to(device)
         self.out_host = torch.empty_like(self.c0_host).pin_memory()
         self.units_per_step = self.n * self.T
-        self.config = {"workload": "ac%d_rk4" % self.shape[0], "grid": list(self.shape), "rk4_steps_per_bench_step": self.T,
+        self.config = {"workload": "ac%d_%s" % (self.shape[0], scheme), "grid": list(self.shape),
+                       f"{scheme}_steps_per_bench_step": self.T,
                        "dt": 0.5, "eps": 2.0, "gab": 1.0, "M": 1.0, "force": 0.0, "curvature": 0.01,
                        "bc": "neumann x, y, z", "seed": seed,
                        "l2": "working set (state, 4 stages, stage input) larger than L2"}
+
+    def step(self):
+        u = self.c0
+        for _ in range(self.T):
+            u = self.st.step(0.0, u)
+        return u
+
+    def step_e2e(self):
+        self.c0.copy_(self.c0_host, non_blocking=True)
+        u = self.step()
+        self.out_host.copy_(u, non_blocking=True)
+        self.torch.cuda.current_stream().synchronize()
+
+    def e2e_bytes(self):
+        return 4 * self.n, 4 * self.n
+
+
+class ChEtd1:
+    """Cahn-Hilliard with ExponentialEuler (ETD1, Pade phi1 table), 256^3 periodic, dt 0.1,
+    eps 3, D 1: the problem's rhs kernel plus evx_spectral_update per step."""
+
+    def __init__(self, torch, device, n=256, steps_per=20, seed=1, shape=None):
+        from evoxels_gb300.problem_definition import CahnHilliard
+        from evoxels_gb300.timesteppers import ExponentialEuler
+        from evoxels_gb300.voxelfields import VoxelFields
+        from evoxels_gb300.voxelgrid import VoxelGridGB300
+        self.torch = torch
+        self.shape = tuple(shape) if shape else (n, n, n)
+        self.n = int(np.prod(self.shape))
+        self.nspec = self.shape[0] * self.shape[1] * (self.shape[2] // 2 + 1)
+        self.T = steps_per
+        vf = VoxelFields(self.shape, domain_size=self.shape)
+        vg = VoxelGridGB300(vf.grid_info(), device=device)
+        self.st = ExponentialEuler(CahnHilliard(vg), 0.1)
+        c0 = 0.5 + 0.1 * np.random.default_rng(seed).random(self.shape)
+        self.c0_host = torch.tensor(c0, dtype=torch.float32).unsqueeze(0).pin_memory()
+        self.c0 = self.c0_host.to(device)
+        self.out_host = torch.empty_like(self.c0_host).pin_memory()
+        self.units_per_step = self.n * self.T
+        self.config = {"workload": "ch%d_etd1" % self.shape[0], "grid": list(self.shape),
+                       "etd1_steps_per_bench_step": self.T, "dt": 0.1, "eps": 3.0, "D": 1.0, "bc": "periodic",
+                       "seed": seed, "l2": "working set (state, rhs, spectrum, table) larger than L2"}
 
     def step(self):
         u = self.c0
@@ -470,6 +521,10 @@ def make_workload(name, torch, device, inner=None, spp=0, shape=None):
         return ChForward(torch, device, 512, inner or 20, 5, shape=shape)
     if name == "ac256_rk4":
         return AcRk4(torch, device, 256, inner or 20, 7, shape=shape)
+    if name == "ac256_rkc2":
+        return AcRk4(torch, device, 256, inner or 20, 7, shape=shape, scheme="rkc2")
+    if name == "ch256_etd1":
+        return ChEtd1(torch, device, 256, inner or 20, 1, shape=shape)
     if name == "fd512":
         return FdForward(torch, device, 512, inner or 100, 2, spp=spp)
     raise SystemExit(f"unknown workload {name}")
@@ -478,6 +533,19 @@ def make_workload(name, torch, device, inner=None, spp=0, shape=None):
 # ---------------------------------------------------------------------------
 # CPU baselines (the oracle port of the reference's torch path)
 # ---------------------------------------------------------------------------
+
+def _oracle_step_fn(workload_name, torch):
+    """One oracle step (fp32, torch CPU) of the 256^3 RKC2 / ETD1 workloads, and its description."""
+    import oracle
+    shape = (256, 256, 256)
+    if workload_name == "ac256_rkc2":
+        u0 = torch.tensor(oracle.seeded_unit_field(shape, 7), dtype=torch.float32).unsqueeze(0)
+        k = oracle.rkc_coeffs(2, dtype=torch.float32)
+        return (lambda: oracle.rkc_step(u0, 0.5, oracle.ac_rhs, k)), "256^3, 1 Allen-Cahn RKC2 step, fp32"
+    u0 = torch.tensor(oracle.seeded_ch_field(shape, 1), dtype=torch.float32).unsqueeze(0)
+    m = oracle.etd1_multiplier(-2 * 3.0 * 1.0 * 0.25 * oracle.rfft_k_squared(shape) ** 2, 0.1)
+    return (lambda: oracle.imex_step(u0, m, oracle.ch_rhs)), "256^3, 1 Cahn-Hilliard ETD1 step, fp32"
+
 
 def cpu_sample(workload_name, torch, seconds_cap=30.0):
     """Time the oracle (torch CPU, all host threads) on a bounded sample of the workload."""
@@ -529,6 +597,9 @@ def cpu_sample(workload_name, torch, seconds_cap=30.0):
             oracle.ac_rk4_run(u0, 1, 0.5)
         units = n ** 3
         sample = f"{n}^3, 1 Allen-Cahn RungeKutta4 step, fp32"
+    elif workload_name in ("ac256_rkc2", "ch256_etd1"):
+        one, sample = _oracle_step_fn(workload_name, torch)
+        units = 256 ** 3
     else:
         n = 512
         shape = (n, n, n)
@@ -690,12 +761,16 @@ def main():
         step_bytes = (64 if wl.adj else 32) * wl.units_per_step
     elif args.workload in ("ch256_fwd_adj", "ch128_inversion", "ch512_fwd_adj"):
         step_bytes = 64 * wl.units_per_step    # 32 B forward + 32 B adjoint per voxel-step
-    elif args.workload.startswith("ch"):
+    elif args.workload in ("ch100_fwd", "ch512_fwd"):
         step_bytes = 32 * wl.units_per_step
     elif args.workload.startswith("fd"):
         step_bytes = 8 * wl.units_per_step
+    elif args.workload == "ac256_rkc2":
+        step_bytes = 116 * wl.units_per_step   # 4 x rhs 8 + first stage 12 + 3 x RKC2 stage 24
     elif args.workload.startswith("ac"):
         step_bytes = 92 * wl.units_per_step    # 4 x rhs 8 + 3 x stage input 12 + combine 24
+    elif args.workload == "ch256_etd1":
+        step_bytes = 46 * wl.units_per_step    # rhs 8, R2C 8, x-pass 10, C2R 8, axpy 12 (nspec ~ n/2)
     step_roofline = None
     if step_bytes:
         gbs = step_bytes * args.steps / (ms / 1e3) / 1e9
@@ -776,7 +851,7 @@ def run_reference(args, torch, warmup):
             oracle.ch_imex_vjp(u0, lam, 0.1, 3.0, 1.0)
             return u1
         sample = f"{n}^3: 1 forward IMEX step + 1 adjoint step (torch autograd) per bench step, fp32"
-    elif wl.startswith("ch"):
+    elif wl in ("ch100_fwd", "ch512_fwd"):
         n = 100 if wl == "ch100_fwd" else 512
         shape = (n, n, n)
         u0 = torch.tensor(oracle.seeded_ch_field(shape, 1), dtype=torch.float32).unsqueeze(0)
@@ -792,6 +867,11 @@ def run_reference(args, torch, warmup):
         def one():
             return oracle.ac_rk4_run(u0, 1, 0.5)
         sample = f"{n}^3: 1 Allen-Cahn RungeKutta4 step per bench step, fp32"
+    elif wl in ("ac256_rkc2", "ch256_etd1"):
+        n = 256
+        shape = (n, n, n)
+        one, sample = _oracle_step_fn(wl, torch)
+        sample += " per bench step"
     else:
         n = 512
         shape = (n, n, n)

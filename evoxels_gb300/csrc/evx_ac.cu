@@ -207,7 +207,7 @@ int evx_rkc_stage(const float* u, const float* y_curr, const float* y_prev, cons
     cudaStream_t st = as_stream(stream);
     const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)152 * 16);
     if (r0)
-        EVX_TIMED("rkc_stage", st, (rkc_stage_kernel<true><<<blocks, 256, 0, st>>>(
+        EVX_TIMED("rkc2_stage", st, (rkc_stage_kernel<true><<<blocks, 256, 0, st>>>(
                                         u, y_curr, y_prev, r, r0, c->mu0, c->nu, c->one_minus_mu0_nu, c->mu1_dt,
                                         c->gamma_dt, out, n)));
     else
