@@ -8,7 +8,7 @@ gradient, then 10 adjoint steps giving dL/dc0, dL/dD and dL/deps.  A
 voxel-step counts one forward plus one adjoint step of one voxel.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch512_fwd_adj|ch128_inversion|ac256_rk4|ac256_rkc2|ch256_etd1|batched64_fwd|batched64_fwd_adj]
+                    [--workload ch256_fwd_adj|ch100_fwd|fd512|ch512_fwd|ch512_fwd_adj|ch128_inversion|ac256_rk4|ac256_rkc2|ch256_etd1|driver256|batched64_fwd|batched64_fwd_adj]
 
 ``--impl reference`` times the CPU oracle (the operation-by-operation torch
 restatement of the reference's own torch path; the reference itself is pure
@@ -357,6 +357,60 @@ class ChEtd1:
         return 4 * self.n, 4 * self.n
 
 
+class Driver:
+    """The drop-in driver end to end: run_cahn_hilliard_solver on a 256^3 host field with the
+    reference defaults (dt 0.1, 10 frames, 100 iterations); every bench step is one solve, host
+    numpy in, 11 exported host frames out (NaN checks included).  The same solve with the
+    synchronous frame export is timed once for comparison."""
+
+    def __init__(self, torch, device, n=256, steps_per=100, seed=1, shape=None):
+        import evoxels_gb300 as evo
+        self.torch = torch
+        self.evo = evo
+        self.shape = tuple(shape) if shape else (n, n, n)
+        self.n = int(np.prod(self.shape))
+        self.nspec = self.shape[0] * self.shape[1] * (self.shape[2] // 2 + 1)
+        self.T = steps_per
+        self.vf = evo.VoxelFields(self.shape, domain_size=self.shape)
+        self.c0 = 0.5 + 0.1 * np.random.default_rng(seed).random(self.shape)
+        self.vf.add_field("c", self.c0.copy())
+        self.units_per_step = self.n * self.T
+        self.config = {"workload": "driver%d" % self.shape[0], "grid": list(self.shape), "max_iters": self.T,
+                       "frames": 10, "dt": 0.1, "eps": 3.0, "D": 1.0, "bc": "periodic", "seed": seed,
+                       "api": "run_cahn_hilliard_solver (host numpy field in, host frames out)",
+                       "l2": "working set larger than L2"}
+
+    def _solve(self, async_output=True):
+        from evoxels_gb300.problem_definition import CahnHilliard
+        from evoxels_gb300.solvers import TimeDependentSolver
+        from evoxels_gb300.timesteppers import PseudoSpectralIMEX
+        self.vf.fields["c"] = self.c0.copy()
+        solver = TimeDependentSolver(self.vf, "c", "torch", problem_cls=CahnHilliard,
+                                     timestepper_cls=PseudoSpectralIMEX, async_output=async_output)
+        solver.solve(time_increment=0.1, frames=10, max_iters=self.T, verbose=False, jit=False)
+
+    def step(self):
+        self.evo.run_cahn_hilliard_solver(self.vf, "c", "torch", jit=False, time_increment=0.1, frames=10,
+                                          max_iters=self.T, verbose=False)
+
+    def step_e2e(self):
+        self.step()
+
+    def e2e_bytes(self):
+        return 4 * self.n, 11 * 4 * self.n
+
+    def sync_reference(self, reps=2):
+        """Seconds per solve with the synchronous frame export, and with the default one."""
+        out = {}
+        for mode in (False, True):
+            self._solve(mode)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                self._solve(mode)
+            out[mode] = (time.perf_counter() - t0) / reps
+        return out
+
+
 class FdForward:
     """Explicit FD diffusion, 512^3, Dirichlet x / Neumann y,z, dt = 1/60 (config 2)."""
 
@@ -525,6 +579,8 @@ def make_workload(name, torch, device, inner=None, spp=0, shape=None):
         return AcRk4(torch, device, 256, inner or 20, 7, shape=shape, scheme="rkc2")
     if name == "ch256_etd1":
         return ChEtd1(torch, device, 256, inner or 20, 1, shape=shape)
+    if name == "driver256":
+        return Driver(torch, device, 256, inner or 100, 1, shape=shape)
     if name == "fd512":
         return FdForward(torch, device, 512, inner or 100, 2, spp=spp)
     raise SystemExit(f"unknown workload {name}")
@@ -600,6 +656,14 @@ def cpu_sample(workload_name, torch, seconds_cap=30.0):
     elif workload_name in ("ac256_rkc2", "ch256_etd1"):
         one, sample = _oracle_step_fn(workload_name, torch)
         units = 256 ** 3
+    elif workload_name == "driver256":
+        shape = (256, 256, 256)
+        u0 = torch.tensor(oracle.seeded_ch_field(shape, 1), dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            oracle.ch_imex_run(u0, 1, 0.1)
+        units = 256 ** 3
+        sample = "256^3, 1 IMEX step of the driver's loop (no frame export), fp32"
     else:
         n = 512
         shape = (n, n, n)
@@ -783,6 +847,11 @@ def main():
         vs_plain = {"plain_ms_per_step": round(plain_ms, 3), "plain_value": round(wl.units_per_step / (plain_ms / 1e3), 1),
                     "speedup": round(plain_ms / (ms / args.steps), 3),
                     "plain_path": "single-grid PseudoSpectralIMEX.advance per instance, same GPU"}
+    if isinstance(wl, Driver):
+        t = wl.sync_reference()
+        vs_plain = {"sync_output_s_per_solve": round(t[False], 4), "async_output_s_per_solve": round(t[True], 4),
+                    "speedup": round(t[False] / t[True], 3),
+                    "plain_path": "the same solve with the synchronous frame export (async_output=False)"}
     out = {
         "metric": (METRIC if args.workload == "ch256_fwd_adj" and not args.shape
                    else f"voxel-steps/s {args.workload}" + ("@%dx%dx%d" % args.shape if args.shape else "")),
@@ -872,6 +941,14 @@ def run_reference(args, torch, warmup):
         shape = (n, n, n)
         one, sample = _oracle_step_fn(wl, torch)
         sample += " per bench step"
+    elif wl == "driver256":
+        n = 256
+        shape = (n, n, n)
+        u0 = torch.tensor(oracle.seeded_ch_field(shape, 1), dtype=torch.float32).unsqueeze(0)
+
+        def one():
+            return oracle.ch_imex_run(u0, 1, 0.1)
+        sample = f"{n}^3: 1 IMEX step of the driver's loop per bench step (no frame export), fp32"
     else:
         n = 512
         shape = (n, n, n)

@@ -3,7 +3,9 @@
 // of an inversion (the loss the reference's parameter-estimation workflow
 // minimises between simulated and observed fields, evoxels/inversion.py:105-124).
 // Per-block partial sums go to caller scratch and one block reduces them in a
-// fixed order, so the loss is deterministic.
+// fixed order, so the loss is deterministic.  Also the frame check of the
+// solver loop: a NaN flag over a field, computed on the device so that the
+// frame's host copy needs no extra pass (evoxels/solvers.py:163-165).
 #include <algorithm>
 
 #include "evx_common.cuh"
@@ -51,6 +53,24 @@ __global__ void mse_reduce_kernel(const double* __restrict__ part, int nblk, dou
     if (threadIdx.x == 0) *loss = s[0] * inv_n;
 }
 
+// *flag = 1 if any x[i] is NaN (the caller zeroes it); float4 loads when aligned.
+__global__ void nan_flag_kernel(const float* __restrict__ x, size_t n, int* __restrict__ flag) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    size_t tail0 = 0;
+    if ((reinterpret_cast<uintptr_t>(x) & 15) == 0) {
+        const float4* x4 = reinterpret_cast<const float4*>(x);
+        const size_t n4 = n / 4;
+        for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += stride) {
+            const float4 v = __ldg(x4 + e);
+            bad |= isnan(v.x) || isnan(v.y) || isnan(v.z) || isnan(v.w);
+        }
+        tail0 = n4 * 4;
+    }
+    for (size_t e = tail0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) bad |= isnan(__ldg(x + e));
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
 int mse_blocks(size_t n) {
     return (int)std::max<size_t>(1, std::min<size_t>((n + MSE_THREADS - 1) / MSE_THREADS, MSE_MAX_BLOCKS));
 }
@@ -78,6 +98,17 @@ int evx_mse_grad(const float* u, const float* target, size_t n, float* lam, doub
     EVX_TIMED("mse_reduce", st, mse_reduce_kernel<<<1, 256, 0, st>>>(part, nb, 1.0 / (double)n, loss));
     count_launch(2);
     return check_launch("evx_mse_grad");
+}
+
+int evx_nan_flag(const float* x, size_t n, int* flag, void* stream) {
+    if (!flag || (n && !x)) return fail(EVX_ERR_BAD_ARG, "NULL pointer");
+    cudaStream_t st = as_stream(stream);
+    int rc = check_cuda(cudaMemsetAsync(flag, 0, sizeof(int), st), "evx_nan_flag reset");
+    if (rc || n == 0) return rc;
+    const int nb = (int)std::max<size_t>(1, std::min<size_t>((n / 4 + MSE_THREADS - 1) / MSE_THREADS, 152 * 8));
+    EVX_TIMED("nan_flag", st, nan_flag_kernel<<<nb, MSE_THREADS, 0, st>>>(x, n, flag));
+    count_launch();
+    return check_launch("nan_flag_kernel");
 }
 
 }  // extern "C"

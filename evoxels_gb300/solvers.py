@@ -5,6 +5,14 @@ printed timing line as evoxels/solvers.py:12-208.  Between output frames the
 loop hands whole runs of steps to the stepper's ``advance`` (one library call
 per frame interval) when the stepper has one; a user ``step_fn`` is called
 step by step exactly as in the reference.
+
+Frame output (evoxels/solvers.py:152-187) is asynchronous by default: at a
+frame the state's NaN flag is computed on the device and the state is copied
+to pinned host memory on a side stream, while the next interval's steps are
+already queued on the compute stream; the host then waits for the copy only,
+exports the fields, applies the NaN abort with the frame's own number and
+time, and writes the VTK file, all overlapped with the GPU's next interval.
+``async_output=False`` restores the reference's synchronous export.
 """
 
 from __future__ import annotations
@@ -49,6 +57,7 @@ class BaseSolver:
     timestepper_cls: Any = None
     step_fn: Callable | None = None
     device: str = "cuda"
+    async_output: bool = True
 
     def __post_init__(self):
         if self.backend not in ("torch", "gb300"):
@@ -99,13 +108,49 @@ class BaseSolver:
         """Export, NaN abort, optional VTK (evoxels/solvers.py:152-187; no plotting)."""
         u_out = u  # trim_ghost_nodes(pad_bc(u)) == u for cell-centred grids
         self._export_fields(u_out)
-        if any(np.isnan(self.vf.fields[name]).any() for name in self.fieldnames):
+        has_nan = any(np.isnan(self.vf.fields[name]).any() for name in self.fieldnames)
+        self._frame_tail(has_nan, frame, time, vtk_out)
+
+    def _frame_tail(self, has_nan, frame, time, vtk_out):
+        if has_nan:
             print(f"NaN detected in frame {frame} at time {time}. Aborting simulation.")
             sys.exit(1)
         if vtk_out:
             cls = self.problem_cls.__name__ if self.problem_cls is not None else "step_fn"
             filename = cls + "_" + self.fieldnames[0] + f"_{frame:03d}.vtk"
             self.vf.export_to_vtk(filename=filename, field_names=self.fieldnames)
+
+    # ---- asynchronous frames --------------------------------------------------
+    def _begin_output(self, u, frame, time):
+        """Queue the frame's NaN flag and host copy on the side stream; returns the pending frame."""
+        from . import _lib
+        dev = self.vg.device
+        pipe = getattr(self, "_pipe", None)
+        if pipe is None or pipe["host"].shape != u.shape:
+            pipe = {"stream": torch.cuda.Stream(dev),
+                    "host": torch.empty(u.shape, dtype=u.dtype).pin_memory(),
+                    "flag_dev": torch.zeros(1, dtype=torch.int32, device=dev),
+                    "flag_host": torch.zeros(1, dtype=torch.int32).pin_memory()}
+            self._pipe = pipe
+        st = pipe["stream"]
+        st.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(st):
+            _lib.check(_lib.lib().evx_nan_flag(u.data_ptr(), u.numel(), pipe["flag_dev"].data_ptr(), st.cuda_stream),
+                       "evx_nan_flag")
+            pipe["host"].copy_(u, non_blocking=True)
+            pipe["flag_host"].copy_(pipe["flag_dev"], non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(st)
+        u.record_stream(st)   # the caching allocator keeps u until the copy has read it
+        return (done, frame, time)
+
+    def _finish_output(self, pending, vtk_out):
+        done, frame, time = pending
+        done.synchronize()
+        host = self._pipe["host"]
+        for i, name in enumerate(self.fieldnames):
+            self.vf.set_field(name, host[i].numpy().copy())
+        self._frame_tail(bool(self._pipe["flag_host"][0]), frame, time, vtk_out)
 
 
 @dataclass
@@ -116,11 +161,15 @@ class TimeDependentSolver(BaseSolver):
         n_out = max_iters // frames
         frame = 0
         advance = getattr(self._stepper, "advance", None)
+        pending = None
         i = 0
         while i < max_iters:
             time = i * time_increment
             if i % n_out == 0:
-                self._handle_outputs(u, frame, time, vtk_out, verbose, plot_bounds, colormap)
+                if self.async_output:
+                    pending = self._begin_output(u, frame, time)
+                else:
+                    self._handle_outputs(u, frame, time, vtk_out, verbose, plot_bounds, colormap)
                 frame += 1
             if advance is not None:
                 n = min(n_out - i % n_out, max_iters - i)
@@ -129,6 +178,12 @@ class TimeDependentSolver(BaseSolver):
             else:
                 u = step(time, u)
                 i += 1
+            if pending is not None:   # the next steps are queued: wait for the frame's copy only
+                self._finish_output(pending, vtk_out)
+                pending = None
         time = max_iters * time_increment
-        self._handle_outputs(u, frame, time, vtk_out, verbose, plot_bounds, colormap)
+        if self.async_output:
+            self._finish_output(self._begin_output(u, frame, time), vtk_out)
+        else:
+            self._handle_outputs(u, frame, time, vtk_out, verbose, plot_bounds, colormap)
         return u

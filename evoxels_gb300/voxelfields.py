@@ -113,28 +113,34 @@ class VoxelFields:
     def meshgrid(self):
         return tuple(np.meshgrid(*self.axes(), indexing="ij"))
 
-    def export_to_vtk(self, filename="output.vtk", field_names=None):
-        """Write fields as cell data of a legacy ASCII VTK image (headless).
+    def export_to_vtk(self, filename="output.vtk", field_names=None, binary=True):
+        """Write fields as cell data of a legacy VTK image (headless).
 
         Same geometry as the reference's pyvista ImageData
         (evoxels/voxelfields.py:196-214): ``(N+1)`` points per axis, origin at
         the lower cell corner, fields flattened in Fortran (x-fastest) order.
+        ``binary`` (the default of pyvista's ``save``): big-endian float32
+        payloads; ``binary=False`` writes ASCII.
         """
         if not str(filename).endswith(".vtk"):
             raise ValueError("filename must end with .vtk")
         names = field_names if field_names else list(self.fields.keys())
         nx, ny, nz = self.shape
         o = [self.origin[i] - self.spacing[i] / 2 for i in range(3)]
-        with open(filename, "w") as f:
-            f.write("# vtk DataFile Version 3.0\nevoxels_gb300 fields\nASCII\nDATASET STRUCTURED_POINTS\n")
-            f.write(f"DIMENSIONS {nx + 1} {ny + 1} {nz + 1}\n")
-            f.write("ORIGIN {} {} {}\n".format(*o))
-            f.write("SPACING {} {} {}\n".format(*self.spacing))
-            f.write(f"CELL_DATA {nx * ny * nz}\n")
+        head = ("# vtk DataFile Version 3.0\nevoxels_gb300 fields\n" + ("BINARY" if binary else "ASCII") +
+                "\nDATASET STRUCTURED_POINTS\n" + f"DIMENSIONS {nx + 1} {ny + 1} {nz + 1}\n" +
+                "ORIGIN {} {} {}\n".format(*o) + "SPACING {} {} {}\n".format(*self.spacing) +
+                f"CELL_DATA {nx * ny * nz}\n")
+        with open(filename, "wb") as f:
+            f.write(head.encode())
             for name in names:
                 data = np.asarray(self.fields[name], dtype=np.float32)
-                f.write(f"SCALARS {name} float 1\nLOOKUP_TABLE default\n")
-                np.savetxt(f, data.flatten(order="F"), fmt="%.7g")
+                f.write(f"SCALARS {name} float 1\nLOOKUP_TABLE default\n".encode())
+                if binary:
+                    f.write(np.ascontiguousarray(data.transpose(2, 1, 0), dtype=">f4").tobytes())
+                    f.write(b"\n")
+                else:
+                    np.savetxt(f, data.flatten(order="F"), fmt="%.9g")
 
     def plot_slice(self, *args, **kwargs):
         raise NotImplementedError("plotting is not part of evoxels_gb300 (no graphics stack)")

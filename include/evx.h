@@ -318,6 +318,10 @@ int evx_batch_adjoint(evx_batch* batch, const float* states, int nsteps,
  * workflow (evoxels/inversion.py:105-124 fits simulated to observed fields).
  * scratch: evx_mse_scratch_bytes(n) bytes of device memory for partial sums. */
 size_t evx_mse_scratch_bytes(size_t n);
+
+/* The solver's frame check (evoxels/solvers.py:163-165) on the device:
+ * *flag (device int) = 1 if any of the n floats at x is NaN, else 0. */
+int evx_nan_flag(const float* x, size_t n, int* flag, void* stream);
 int evx_mse_grad(const float* u, const float* target, size_t n, float* lam, double* loss,
                  void* scratch, size_t scratch_bytes, void* stream);
 
