@@ -21,111 +21,205 @@
 // non-periodic coordinates, then the x, then the y, then the z boundary map of
 // each non-periodic axis the point lies outside of.
 //
-// Tiling: a 32 (z) x 8 (y) block streams along x through a 3-slot ring of
-// shared planes, each (8+2) x (32+2) cells of the ghosted field.
+// Tiling: a 64 (z) x 8 (y) block of 256 threads streams along x; each thread
+// owns two z-adjacent outputs: sums and differences as two-lane .rn
+// instructions, products and divisions as scalar roundings (a two-lane multiply
+// may be fused into a following add by the code generator), every lane exactly
+// the scalar operation in the reference's order.
+// Planes of the ghosted clipped field, (8+2) x (64+2) cells, sit in a 4-slot
+// shared ring, so one block barrier per plane suffices (the slot written next
+// was last read two planes ago).  The next plane's cells are loaded into
+// registers before the current plane is computed.  Per staged cell the
+// wrapped/clamped (y, z) offset and its boundary maps are fixed per tile; per
+// plane only the x index and the x map change.
+#include <algorithm>
+
+#include "evx_ch_fast.cuh"
 #include "evx_common.cuh"
 #include "evx_prof.cuh"
 
 namespace evx {
 namespace {
 
-constexpr int AZ = 32, AY = 8;              // output tile
-constexpr int PZ = AZ + 2, PY = AY + 2;     // plane with halo
-constexpr int PLANE = PZ * PY;
+using fast::f2s;
+
+using fast::exact::add2;
+using fast::exact::mul2;
+using fast::exact::sub2;
+
+constexpr int AZ = 64, AY = 8;                // output tile
+constexpr int PW = AZ + 4;                    // shared row: z in [k0-2, k0+AZ+2), cell z at z-k0+2
+constexpr int PR = AY + 2;                    // rows: y in [j0-1, j0+AY]
+constexpr int PLANE = PR * PW;
+constexpr int NCELL = PR * (AZ + 2);          // staged cells per plane
+constexpr int CPT = (NCELL + 255) / 256;      // staged cells per thread
+constexpr int AC_THREADS = 256;
 
 struct AcP {
     float w, eps, gab, M, force, three_over_eps, curv, one_minus_curv;
 };
 
-// Value of the ghosted (padded) clipped field at (x, y, z), each coordinate in [-1, n].
-__device__ __forceinline__ float ghosted(const float* __restrict__ u, const Geo& G, int x, int y, int z) {
-    const bool ox = x < 0 || x >= G.nx, oy = y < 0 || y >= G.ny, oz = z < 0 || z >= G.nz;
-    auto fix = [](int c, int n, bool per) {
-        if (c < 0) return per ? c + n : 0;
-        if (c >= n) return per ? c - n : n - 1;
-        return c;
-    };
-    const int xi = fix(x, G.nx, G.kind[0] == EVX_BC_PERIODIC);
-    const int yi = fix(y, G.ny, G.kind[1] == EVX_BC_PERIODIC);
-    const int zi = fix(z, G.nz, G.kind[2] == EVX_BC_PERIODIC);
-    float v = clip01(__ldg(u + ((size_t)xi * G.ny + yi) * G.nz + zi));
-    if (ox && G.kind[0] != EVX_BC_PERIODIC) v = x < 0 ? ghost_lo(G, 0, v) : ghost_hi(G, 0, v);
-    if (oy && G.kind[1] != EVX_BC_PERIODIC) v = y < 0 ? ghost_lo(G, 1, v) : ghost_hi(G, 1, v);
-    if (oz && G.kind[2] != EVX_BC_PERIODIC) v = z < 0 ? ghost_lo(G, 2, v) : ghost_hi(G, 2, v);
-    return v;
+// One staged cell: in-plane offset of its source (wrapped / clamped), shared
+// offset, and the y / z boundary maps to apply (0 none, 1 low side, 2 high side).
+struct Cell {
+    int off, soff, fy, fz;
+};
+
+__device__ __forceinline__ float bc_map(const Geo& G, int a, int side, float v) {
+    return side == 1 ? ghost_lo(G, a, v) : (side == 2 ? ghost_hi(G, a, v) : v);
 }
 
-// ((R - 2C) + L)
-__device__ __forceinline__ float d2(float R, float C, float L) {
-    return __fadd_rn(__fsub_rn(R, __fmul_rn(2.f, C)), L);
+// ((R - 2C) + L), two lanes
+__device__ __forceinline__ float2 d2x2(float2 R, float2 C, float2 L) {
+    return add2(sub2(R, mul2(f2s(2.f), C)), L);
 }
 // ((pp + mm) - mp) - pm
-__device__ __forceinline__ float mixed(float pp, float mm, float mp, float pm) {
-    return __fsub_rn(__fsub_rn(__fadd_rn(pp, mm), mp), pm);
+__device__ __forceinline__ float2 mixed2(float2 pp, float2 mm, float2 mp, float2 pm) {
+    return sub2(sub2(add2(pp, mm), mp), pm);
+}
+// ((((0.5*ga)*gb)*m)*ia)*ib
+__device__ __forceinline__ float2 cross2(float2 ga, float2 gb, float2 m, float2 ia, float2 ib) {
+    return mul2(mul2(mul2(mul2(mul2(f2s(0.5f), ga), gb), m), ia), ib);
 }
 
-__global__ void __launch_bounds__(AZ * AY)
+__global__ void __launch_bounds__(AC_THREADS)
 ac_rhs_kernel(const float* __restrict__ u, float* __restrict__ r, Geo G, AcP P, int LX) {
-    __shared__ float ring[3][PLANE];
-    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * AZ + tz;
+    __shared__ __align__(16) float ring[4][PLANE];
+    const int tid = threadIdx.x;
+    const int tx = tid & 31, ty = tid >> 5;
     const int k0 = blockIdx.x * AZ, j0 = blockIdx.y * AY;
     const int x0 = blockIdx.z * LX;
     const int x1 = min(x0 + LX, G.nx);
     if (x0 >= x1) return;   // uniform across the block
-    auto load = [&](int x) {
-        float* dst = ring[(x + 3) % 3];
-        for (int e = tid; e < PLANE; e += AZ * AY) {
-            const int py = e / PZ, pz = e - py * PZ;
-            const int y = j0 + py - 1, z = k0 + pz - 1;
-            // cells beyond the ghost layer are never read by in-domain outputs
-            dst[e] = (y <= G.ny && z <= G.nz) ? ghosted(u, G, x, y, z) : 0.f;
+    const int nx = G.nx, ny = G.ny, nz = G.nz;
+    const size_t plane = (size_t)ny * nz;
+    const bool perx = G.kind[0] == EVX_BC_PERIODIC, pery = G.kind[1] == EVX_BC_PERIODIC,
+               perz = G.kind[2] == EVX_BC_PERIODIC;
+
+    // per-tile staging plan; cells beyond the ghost layer are never read by
+    // in-domain outputs and are staged as 0
+    Cell cell[CPT];
+#pragma unroll
+    for (int s = 0; s < CPT; ++s) {
+        const int e = tid + s * AC_THREADS;
+        Cell c{-1, 0, 0, 0};
+        if (e < NCELL) {
+            const int row = e / (AZ + 2), col = e - row * (AZ + 2);
+            const int y = j0 + row - 1, z = k0 + col - 1;
+            c.soff = row * PW + col + 1;
+            if (y <= ny && z <= nz) {
+                int yi = y, zi = z;
+                if (y < 0) { yi = pery ? y + ny : 0; c.fy = pery ? 0 : 1; }
+                if (y >= ny) { yi = pery ? y - ny : ny - 1; c.fy = pery ? 0 : 2; }
+                if (z < 0) { zi = perz ? z + nz : 0; c.fz = perz ? 0 : 1; }
+                if (z >= nz) { zi = perz ? z - nz : nz - 1; c.fz = perz ? 0 : 2; }
+                c.off = yi * nz + zi;
+            }
+        } else {
+            c.soff = -1;
+        }
+        cell[s] = c;
+    }
+    float pre[CPT];
+    auto fetch = [&](int x) {   // raw values of plane x into registers
+        const int xi = x < 0 ? (perx ? x + nx : 0) : (x >= nx ? (perx ? x - nx : nx - 1) : x);
+        const float* src = u + (size_t)xi * plane;
+#pragma unroll
+        for (int s = 0; s < CPT; ++s) pre[s] = cell[s].off >= 0 ? __ldg(src + cell[s].off) : 0.f;
+    };
+    auto stash = [&](int x) {   // clip, boundary maps in x, y, z order, into the ring
+        float* dst = ring[x & 3];
+        const int fx = perx ? 0 : (x < 0 ? 1 : (x >= nx ? 2 : 0));
+#pragma unroll
+        for (int s = 0; s < CPT; ++s) {
+            if (cell[s].soff < 0) continue;
+            float v = 0.f;
+            if (cell[s].off >= 0) {
+                v = clip01(pre[s]);
+                v = bc_map(G, 0, fx, v);
+                v = bc_map(G, 1, cell[s].fy, v);
+                v = bc_map(G, 2, cell[s].fz, v);
+            }
+            dst[cell[s].soff] = v;
         }
     };
-    const float dx0 = G.ih[0], dx1 = G.ih[1], dx2 = G.ih[2];
-    const float q0 = G.ih2[0], q1 = G.ih2[1], q2 = G.ih2[2];
-    const int j = j0 + ty, k = k0 + tz;
-    const bool out = j < G.ny && k < G.nz;
-    const int c = (ty + 1) * PZ + (tz + 1);
-    load(x0 - 1);
-    load(x0);
+
+    const float2 dx0 = f2s(G.ih[0]), dx1 = f2s(G.ih[1]), dx2 = f2s(G.ih[2]);
+    const float2 q0 = f2s(G.ih2[0]), q1 = f2s(G.ih2[1]), q2 = f2s(G.ih2[2]), qs = f2s(G.ih2sum);
+    const float2 curv = f2s(P.curv), omc = f2s(P.one_minus_curv), w2 = f2s(P.w), gab = f2s(P.gab),
+                 toe = f2s(P.three_over_eps), force = f2s(P.force), M = f2s(P.M);
+    const int j = j0 + ty, k = k0 + 2 * tx;
+    const bool outA = j < ny && k < nz, outB = j < ny && k + 1 < nz;
+    const bool vec = outB && (nz % 2 == 0);
+    const int c = (ty + 1) * PW + 2 * tx + 2;
+
+    fetch(x0 - 1);
+    stash(x0 - 1);
+    fetch(x0);
+    stash(x0);
+    fetch(x0 + 1);
     for (int i = x0; i < x1; ++i) {
-        load(i + 1);
+        stash(i + 1);
+        if (i + 2 <= x1) fetch(i + 2);
         __syncthreads();
-        const float* m = ring[(i + 2) % 3];   // plane i-1
-        const float* o = ring[i % 3];
-        const float* p = ring[(i + 1) % 3];
-        if (out) {
-            const float C = o[c];
-            const float L = m[c], R = p[c];
-            const float B = o[c - PZ], T = o[c + PZ];
-            const float Bk = o[c - 1], F = o[c + 1];
-            const float gx = __fmul_rn(__fmul_rn(0.5f, __fsub_rn(R, L)), dx0);
-            const float gy = __fmul_rn(__fmul_rn(0.5f, __fsub_rn(T, B)), dx1);
-            const float gz = __fmul_rn(__fmul_rn(0.5f, __fsub_rn(F, Bk)), dx2);
-            const float gx2 = __fmul_rn(gx, gx), gy2 = __fmul_rn(gy, gy), gz2 = __fmul_rn(gz, gz);
-            float n = __fmul_rn(__fmul_rn(gx2, d2(R, C, L)), q0);
-            n = __fadd_rn(n, __fmul_rn(__fmul_rn(gy2, d2(T, C, B)), q1));
-            n = __fadd_rn(n, __fmul_rn(__fmul_rn(gz2, d2(F, C, Bk)), q2));
-            // 0.5 * g_a * g_b * (f++ + f-- - f-+ - f+-) * ih_a * ih_b, left to right
-            auto cross = [](float ga, float gb, float m, float ia, float ib) {
-                return __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(0.5f, ga), gb), m), ia), ib);
-            };
-            n = __fadd_rn(n, cross(gx, gy, mixed(p[c + PZ], m[c - PZ], m[c + PZ], p[c - PZ]), dx0, dx1));   // xy
-            n = __fadd_rn(n, cross(gx, gz, mixed(p[c + 1], m[c - 1], m[c + 1], p[c - 1]), dx0, dx2));       // xz
-            n = __fadd_rn(n, cross(gy, gz, mixed(o[c + PZ + 1], o[c - PZ - 1], o[c - PZ + 1], o[c + PZ - 1]),
-                                   dx1, dx2));                                                              // yz
-            float norm2 = __fadd_rn(__fadd_rn(gx2, gy2), gz2);
-            if (norm2 <= 1e-7f) norm2 = 1.f;
-            const float nlap = __fmul_rn(P.one_minus_curv, __fdiv_rn(n, norm2));
-            const float lap = __fmul_rn(P.curv, lap7(G, C, L, R, B, T, Bk, F));
-            const float pot = mu_hom(P.w, C);
-            const float pot2 = __fdiv_rn(__fdiv_rn(pot, 2.f), P.eps);
-            const float df = __fadd_rn(__fmul_rn(P.gab, __fsub_rn(__fadd_rn(lap, nlap), pot2)),
-                                       __fmul_rn(__fmul_rn(__fmul_rn(P.three_over_eps, C), __fsub_rn(1.f, C)),
-                                                 P.force));
-            r[((size_t)i * G.ny + j) * G.nz + k] = __fmul_rn(P.M, df);
+        if (outA) {
+            const float* m = ring[(i - 1) & 3];
+            const float* o = ring[i & 3];
+            const float* p = ring[(i + 1) & 3];
+            const float2 C = *reinterpret_cast<const float2*>(o + c);
+            const float2 L = *reinterpret_cast<const float2*>(m + c);
+            const float2 R = *reinterpret_cast<const float2*>(p + c);
+            const float2 B = *reinterpret_cast<const float2*>(o + c - PW);
+            const float2 T = *reinterpret_cast<const float2*>(o + c + PW);
+            const float2 Bk = make_float2(o[c - 1], C.x), F = make_float2(C.y, o[c + 2]);
+            const float2 gx = mul2(mul2(f2s(0.5f), sub2(R, L)), dx0);
+            const float2 gy = mul2(mul2(f2s(0.5f), sub2(T, B)), dx1);
+            const float2 gz = mul2(mul2(f2s(0.5f), sub2(F, Bk)), dx2);
+            const float2 gx2 = mul2(gx, gx), gy2 = mul2(gy, gy), gz2 = mul2(gz, gz);
+            float2 n = mul2(mul2(gx2, d2x2(R, C, L)), q0);
+            n = add2(n, mul2(mul2(gy2, d2x2(T, C, B)), q1));
+            n = add2(n, mul2(mul2(gz2, d2x2(F, C, Bk)), q2));
+            {   // xy: f(x+1,y+1) + f(x-1,y-1) - f(x-1,y+1) - f(x+1,y-1)
+                const float2 pp = *reinterpret_cast<const float2*>(p + c + PW);
+                const float2 mm = *reinterpret_cast<const float2*>(m + c - PW);
+                const float2 mp = *reinterpret_cast<const float2*>(m + c + PW);
+                const float2 pm = *reinterpret_cast<const float2*>(p + c - PW);
+                n = add2(n, cross2(gx, gy, mixed2(pp, mm, mp, pm), dx0, dx1));
+            }
+            {   // xz
+                const float2 pp = make_float2(R.y, p[c + 2]), mm = make_float2(m[c - 1], L.x);
+                const float2 mp = make_float2(L.y, m[c + 2]), pm = make_float2(p[c - 1], R.x);
+                n = add2(n, cross2(gx, gz, mixed2(pp, mm, mp, pm), dx0, dx2));
+            }
+            {   // yz
+                const float2 pp = make_float2(T.y, o[c + PW + 2]), mm = make_float2(o[c - PW - 1], B.x);
+                const float2 mp = make_float2(B.y, o[c - PW + 2]), pm = make_float2(o[c + PW - 1], T.x);
+                n = add2(n, cross2(gy, gz, mixed2(pp, mm, mp, pm), dx1, dx2));
+            }
+            float2 norm2 = add2(add2(gx2, gy2), gz2);
+            if (norm2.x <= 1e-7f) norm2.x = 1.f;
+            if (norm2.y <= 1e-7f) norm2.y = 1.f;
+            const float2 nlap = mul2(omc, make_float2(__fdiv_rn(n.x, norm2.x), __fdiv_rn(n.y, norm2.y)));
+            // 7-point Laplacian: ((R+L)*ih2x + (T+B)*ih2y) + (F+Bk)*ih2z - (2C)*sum(ih2)
+            float2 t = mul2(add2(R, L), q0);
+            t = add2(t, mul2(add2(T, B), q1));
+            t = add2(t, mul2(add2(F, Bk), q2));
+            const float2 lap = mul2(curv, sub2(t, mul2(mul2(f2s(2.f), C), qs)));
+            // w*c*(1-c)*(1-2c); pot/2 as pot*0.5 (the same correctly rounded value)
+            const float2 omC = sub2(f2s(1.f), C);
+            const float2 pot = mul2(mul2(mul2(w2, C), omC), sub2(f2s(1.f), mul2(f2s(2.f), C)));
+            const float2 ph = mul2(pot, f2s(0.5f));
+            const float2 pot2 = make_float2(__fdiv_rn(ph.x, P.eps), __fdiv_rn(ph.y, P.eps));
+            const float2 df = add2(mul2(gab, sub2(add2(lap, nlap), pot2)), mul2(mul2(mul2(toe, C), omC), force));
+            const float2 res = mul2(M, df);
+            float* dst = r + ((size_t)i * ny + j) * nz + k;
+            if (vec) {
+                *reinterpret_cast<float2*>(dst) = res;
+            } else {
+                dst[0] = res.x;
+                if (outB) dst[1] = res.y;
+            }
         }
-        __syncthreads();   // slot (i+2)%3 is reloaded with plane i+2 next
     }
 }
 
@@ -177,14 +271,23 @@ int evx_ac_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc, co
     if (!(p->eps != 0.f) || !std::isfinite(p->eps)) return fail(EVX_ERR_BAD_ARG, "eps must be finite and non-zero");
     const AcP P{p->w, p->eps, p->gab, p->M, p->force, p->three_over_eps, p->curvature, p->one_minus_curvature};
     const Geo G = make_geo(g, bc);
+    static int slots = 0;   // resident blocks on the device
+    if (!slots) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ac_rhs_kernel, AC_THREADS, 0);
+        slots = std::max(1, sms) * std::max(1, per);
+    }
     const int tz = (g->nz + AZ - 1) / AZ, ty = (g->ny + AY - 1) / AY;
-    // x chunks: about 8 resident blocks per SM on a 152-SM part, at least 4 planes each
+    // x chunks: one wave of resident blocks, at least 8 planes each (the x halo is 2 planes)
     const long tiles = (long)tz * ty;
-    int lx = (int)std::max<long>(4, std::min<long>(g->nx, (long)g->nx * tiles / (8L * 152)));
+    const long chunks = std::max<long>(1, slots / tiles);
+    int lx = (int)std::max<long>(8, (g->nx + chunks - 1) / chunks);
     lx = std::min(lx, g->nx);
     const dim3 grid(tz, ty, (g->nx + lx - 1) / lx);
     cudaStream_t st = as_stream(stream);
-    EVX_TIMED("ac_rhs", st, ac_rhs_kernel<<<grid, dim3(AZ, AY), 0, st>>>(u, r, G, P, lx));
+    EVX_TIMED("ac_rhs", st, ac_rhs_kernel<<<grid, AC_THREADS, 0, st>>>(u, r, G, P, lx));
     count_launch();
     return check_launch("ac_rhs_kernel");
 }

@@ -54,11 +54,37 @@ __device__ __forceinline__ float4 clip4(float4 v) {
 // Two-lane fp32 arithmetic (sm_100 FADD2 / FMUL2 / FFMA2): each lane rounds
 // exactly as the scalar __fadd_rn / __fmul_rn / __fmaf_rn.  sub2 is one
 // rounding of a - b (b*(-1) is exact), i.e. the same as __fsub_rn per lane.
+// A multiply followed by an add may still be fused by the code generator, so
+// the bit-exact kernels use the exact:: variants below.
 __device__ __forceinline__ float2 f2s(float s) { return make_float2(s, s); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2s(-1.f), a); }
+
+// Bit-exact two-point arithmetic for the kernels that must round as the
+// reference: sums and differences as two-lane .rn PTX instructions, products as
+// two scalar roundings.  The code generator may fuse a two-lane multiply into
+// a following two-lane add even with explicit rounding modes (and with
+// --fmad=false); with scalar products there is no two-lane multiply to fuse,
+// and scalar .rn multiplies are never contracted.
+namespace exact {
+__device__ __forceinline__ unsigned long long f2bits(float2 v) { return *reinterpret_cast<unsigned long long*>(&v); }
+__device__ __forceinline__ float2 bits2f(unsigned long long v) { return *reinterpret_cast<float2*>(&v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bits2f(r);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bits2f(r);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
+}
+}  // namespace exact
 
 // Per-thread load plan for one shared field plane (precomputed once per tile).
 struct LoadPlan {

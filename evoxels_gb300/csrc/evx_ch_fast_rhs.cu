@@ -17,9 +17,12 @@ namespace evx {
 namespace {
 
 using namespace fast;
+using exact::add2;
+using exact::mul2;
+using exact::sub2;
 
-// Two z-adjacent points at a time with the two-lane fp32 instructions; every
-// lane performs exactly the scalar operations of lap7 / mu_hom / face_flux
+// Two z-adjacent points at a time (two-lane sums, scalar products); every lane
+// performs exactly the scalar operations of lap7 / mu_hom / face_flux
 // (evx_common.cuh) in the same order, so results stay bit-identical.
 struct RhsK {   // broadcast constants
     float2 ih2x, ih2y, ih2z, ih2sum, w, kappa, D, ihx, ihy, ihz;

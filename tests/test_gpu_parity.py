@@ -345,6 +345,20 @@ def test_ch_rhs_fast_equals_generic_and_oracle(cuda_lib, shape):
     np.testing.assert_array_equal(fast.cpu().numpy(), oracle.ch_rhs(cpu32(u0), 2.0, 0.9).numpy())
 
 
+@pytest.mark.parametrize("spacing", [(0.5, 0.75, 1.25), (0.3, 1.7, 0.9)])
+def test_ch_rhs_fast_bitexact_non_unit_spacing(cuda_lib, spacing):
+    """The two-lane fast path with spacing factors that are not 1 (no product is exact)."""
+    from evoxels_gb300.problem_definition import CahnHilliard
+    shape = (12, 20, 64)
+    u0 = oracle.seeded_ch_field(shape, 23) + 0.6 * (oracle.seeded_unit_field(shape, 24) - 0.5)
+    prob = CahnHilliard(vg_for(shape, spacing), eps=2.3, D=0.7)
+    ug = gpu(u0)
+    fast = prob.rhs(0.0, ug)
+    slow = prob.rhs(0.0, _misaligned_copy(ug))
+    torch.testing.assert_close(fast, slow, rtol=0, atol=0)
+    np.testing.assert_array_equal(fast.cpu().numpy(), oracle.ch_rhs(cpu32(u0), 2.3, 0.7, None, spacing).numpy())
+
+
 @pytest.mark.parametrize("shape", [(10, 20, 100), (12, 17, 4), (36, 40, 72)])
 def test_ch_forward_fast_matches_fp64(cuda_lib, shape):
     from evoxels_gb300.problem_definition import CahnHilliard
