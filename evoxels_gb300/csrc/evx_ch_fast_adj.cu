@@ -3,11 +3,12 @@
 //   lam_s = lam_{s+1} + [0<=u<=1] * ( w*phi'(c)*mub - kappa*L(mub) + sum_faces 0.5*cfb )
 //   mub   = sum_a ih_a*(Gb_{-} - Gb_{+}),  Gb_f = ih*D*(g_lo - g_hi) * cf(1-cf)
 //   cfb_f = (ih*D*(g_lo - g_hi)) * ((mu_hi - mu_lo)*ih) * (1 - 2cf)
-// Per x-plane i a block: stores the prefetched planes i+2 of c = clip(u_s) and
-// g = P lam_{s+1} (4-slot rings) and prefetches plane i+3; computes mu and mub
-// on plane i+1 over the tile grown by one cell (2-slot rings); then lam on
-// plane i.  x faces, the previous plane's c and mub at the patch points are
-// carried in registers.  Optional parameter-gradient partial sums are kept in
+// Per x-plane i a block computes lam on plane i, mu and mub on plane i+2 over
+// the tile grown by one cell (3-slot rings) and stores the prefetched planes
+// i+4 of c = clip(u_s) and g = P lam_{s+1} (5-slot rings), then loads plane
+// i+5 into registers: every phase reads only data finished before the previous
+// barrier, so one block barrier per plane suffices.  x faces, the previous
+// plane's c and mub at the patch points are carried in registers.  Optional parameter-gradient partial sums are kept in
 // float per thread and reduced in double per block: GR = 1 all four sums
 // (<lam',u'-u>/D, -<mub,Lc>, <mub,phi(c)>, <h,u'-u>), GR = 2 only the two that
 // need real space (the mobility sums then come from the spectral x-pass).
@@ -22,7 +23,11 @@ namespace {
 
 using namespace fast;
 
-constexpr int RING_C = 4 * MAX_FIELD, RING_M = 2 * MAX_POT;
+constexpr int NC = 5, NM = 3;   // field / potential ring slots
+constexpr int RING_C = NC * MAX_FIELD, RING_M = NM * MAX_POT;
+// ring slots of plane p (p >= -5)
+__device__ __forceinline__ int cslot(int p) { return (p + 10) % NC; }
+__device__ __forceinline__ int mslot(int p) { return (p + 9) % NM; }
 constexpr size_t ADJ_SMEM = (size_t)(2 * RING_C + 2 * RING_M) * sizeof(float) + 4 * 8 * sizeof(double);
 
 // Two points of a patch row (z-adjacent) are processed together with the
@@ -162,8 +167,8 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         }
     };
     auto stash = [&](int p) {
-        float* dc = cs + (p & 3) * T::FIELD;
-        float* dg = gs + (p & 3) * T::FIELD;
+        float* dc = cs + cslot(p) * T::FIELD;
+        float* dg = gs + cslot(p) * T::FIELD;
 #pragma unroll
         for (int s = 0; s < 2; ++s)
             if (LP.valid[s]) {
@@ -174,22 +179,22 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
 
     float2 gxm[2][2];   // Gbar on the x face below the current potential plane, per patch row
     auto gx_faces = [&](int plo, int m, float2 out[2]) {
-        const float* c0 = cs + (plo & 3) * T::FIELD;
-        const float* c1 = cs + ((plo + 1) & 3) * T::FIELD;
-        const float* g0 = gs + (plo & 3) * T::FIELD;
-        const float* g1 = gs + ((plo + 1) & 3) * T::FIELD;
+        const float* c0 = cs + cslot(plo) * T::FIELD;
+        const float* c1 = cs + cslot(plo + 1) * T::FIELD;
+        const float* g0 = gs + cslot(plo) * T::FIELD;
+        const float* g1 = gs + cslot(plo + 1) * T::FIELD;
         const int a = mr[m] * W + mc[m], b = a + W;
         out[0] = gbar2(lds2(c0 + a), lds2(c1 + a), lds2(g0 + a), lds2(g1 + a), ihDx);
         out[1] = gbar2(lds2(c0 + b), lds2(c1 + b), lds2(g0 + b), lds2(g1 + b), ihDx);
     };
 
     auto compute_mu = [&](int p) {
-        const float* cc = cs + (p & 3) * T::FIELD;
-        const float* cm = cs + ((p - 1) & 3) * T::FIELD;
-        const float* cp = cs + ((p + 1) & 3) * T::FIELD;
-        const float* gc = gs + (p & 3) * T::FIELD;
-        float* mo = ms + (p & 1) * T::POT;
-        float* bo = bs + (p & 1) * T::POT;
+        const float* cc = cs + cslot(p) * T::FIELD;
+        const float* cm = cs + cslot(p - 1) * T::FIELD;
+        const float* cp = cs + cslot(p + 1) * T::FIELD;
+        const float* gc = gs + cslot(p) * T::FIELD;
+        float* mo = ms + mslot(p) * T::POT;
+        float* bo = bs + mslot(p) * T::POT;
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
             if (!mv[m]) continue;
@@ -230,12 +235,12 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     // x face cbar of the output patch between planes plo and plo+1
     float2 cfx_m[2], c_prev[2], b_prev[2];
     auto x_faces_b = [&](int plo, float2 out[2]) {
-        const float* c0 = cs + (plo & 3) * T::FIELD;
-        const float* c1 = cs + ((plo + 1) & 3) * T::FIELD;
-        const float* g0 = gs + (plo & 3) * T::FIELD;
-        const float* g1 = gs + ((plo + 1) & 3) * T::FIELD;
-        const float* m0 = ms + (plo & 1) * T::POT;
-        const float* m1 = ms + ((plo + 1) & 1) * T::POT;
+        const float* c0 = cs + cslot(plo) * T::FIELD;
+        const float* c1 = cs + cslot(plo + 1) * T::FIELD;
+        const float* g0 = gs + cslot(plo) * T::FIELD;
+        const float* g1 = gs + cslot(plo + 1) * T::FIELD;
+        const float* m0 = ms + mslot(plo) * T::POT;
+        const float* m1 = ms + mslot(plo + 1) * T::POT;
         out[0] = cfb2(lds2(c0 + pa), lds2(c1 + pa), lds2(m0 + pa - W), lds2(m1 + pa - W), lds2(g0 + pa),
                       lds2(g1 + pa), ihx, ihDx);
         out[1] = cfb2(lds2(c0 + pb), lds2(c1 + pb), lds2(m0 + pb - W), lds2(m1 + pb - W), lds2(g0 + pb),
@@ -243,11 +248,11 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     };
 
     auto compute_lam = [&](int i) {
-        const float* cc = cs + (i & 3) * T::FIELD;
-        const float* gc = gs + (i & 3) * T::FIELD;
-        const float* mm = ms + (i & 1) * T::POT;
-        const float* bb = bs + (i & 1) * T::POT;
-        const float* bp = bs + ((i + 1) & 1) * T::POT;
+        const float* cc = cs + cslot(i) * T::FIELD;
+        const float* gc = gs + cslot(i) * T::FIELD;
+        const float* mm = ms + mslot(i) * T::POT;
+        const float* bb = bs + mslot(i) * T::POT;
+        const float* bp = bs + mslot(i + 1) * T::POT;
         // acc: sum of cbar-face values around each point (times 0.5 at the end)
         float2 accA, accB;
         {
@@ -300,7 +305,7 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             if (wj1) *reinterpret_cast<float2*>(lam_out + o + nz) = oB;
         }
         if (GR) {
-            const float* cx = cs + ((i + 1) & 3) * T::FIELD;
+            const float* cx = cs + cslot(i + 1) * T::FIELD;
             const float2 lcA = lap2(L, A, c_prev[0], lds2(cx + pa), up, B, zmA, zpA);
             const float2 lcB = lap2(L, B, c_prev[1], lds2(cx + pb), A, dn, zmB, zpB);
             if (wj0) {
@@ -330,35 +335,43 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         b_prev[1] = bB;
     };
 
-    // prologue: planes x0-2 .. x0+1 staged; potentials x0-1, x0; carried x quantities
-    for (int p = x0 - 2; p <= x0 + 1; ++p) {
+    // prologue: planes x0-2 .. x0+2 staged; potentials x0-1 .. x0+1; plane x0+3
+    // staged into the slot of x0-2; carried x quantities.  Planes up to x1+1 and
+    // potentials up to x1 are needed.
+    for (int p = x0 - 2; p <= x0 + 2; ++p) {
         fetch(p);
         stash(p);
     }
-    fetch(x0 + 2);
+    fetch(x0 + 3);
     __syncthreads();
 #pragma unroll
     for (int m = 0; m < 2; ++m)
         if (mv[m]) gx_faces(x0 - 2, m, gxm[m]);
     compute_mu(x0 - 1);
     compute_mu(x0);
+    compute_mu(x0 + 1);
     __syncthreads();
+    if (x0 + 3 <= x1 + 1) stash(x0 + 3);
+    if (x0 + 4 <= x1 + 1) fetch(x0 + 4);
     x_faces_b(x0 - 1, cfx_m);
     {
-        const float* cprev = cs + ((x0 - 1) & 3) * T::FIELD;
-        const float* bprev = bs + ((x0 - 1) & 1) * T::POT;
+        const float* cprev = cs + cslot(x0 - 1) * T::FIELD;
+        const float* bprev = bs + mslot(x0 - 1) * T::POT;
         c_prev[0] = lds2(cprev + pa);
         c_prev[1] = lds2(cprev + pb);
         b_prev[0] = lds2(bprev + pa - W);
         b_prev[1] = lds2(bprev + pb - W);
     }
+    __syncthreads();
+    // plane i: lam(i) reads potentials i, i+1 and planes i, i+1; mu(i+2) reads
+    // planes i+1 .. i+3 and writes the potential slot of i-1; the stash of plane
+    // i+4 overwrites the slot of plane i-1 - all last read before the barrier
     for (int i = x0; i < x1; ++i) {
-        stash(i + 2);
-        if (i + 3 <= x1 + 1) fetch(i + 3);
-        __syncthreads();
-        compute_mu(i + 1);
-        __syncthreads();
         compute_lam(i);
+        if (i + 2 <= x1) compute_mu(i + 2);
+        if (i + 4 <= x1 + 1) stash(i + 4);
+        if (i + 5 <= x1 + 1) fetch(i + 5);
+        __syncthreads();
     }
     sD += aD.x + aD.y;
     sK += aK.x + aK.y;
@@ -370,23 +383,32 @@ template <class T, int GR>
 __global__ void __launch_bounds__(THREADS, GR ? 2 : 3)
 ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ gfield, const float* __restrict__ lam,
                         const float* __restrict__ hfield, const float* __restrict__ u1, float* __restrict__ lam_out,
-                        double* __restrict__ part, Geo G, ChP P, int LX, GradSink sink) {
+                        double* __restrict__ part, Geo G, ChP P, int seg, GradSink sink) {
     extern __shared__ __align__(16) float smem[];
     float* cs = smem;
     float* gs = cs + RING_C;
     float* ms = gs + RING_C;
     float* bs = ms + RING_M;
     double* red = reinterpret_cast<double*>(bs + RING_M);   // [4][8]
-    const int x0 = blockIdx.z * LX;
-    const int x1 = min(x0 + LX, G.nx);
+    // block b owns planes [b*seg, b*seg + seg) of the tile-major sequence of
+    // (tile, x) planes: one wave of equal segments, a segment that crosses a
+    // tile boundary finishes one tile and starts the next
+    const int ntz = (G.nz + T::TZ - 1) / T::TZ, nty = (G.ny + T::TY - 1) / T::TY;
+    const long total = (long)ntz * nty * G.nx;
+    long s0 = (long)blockIdx.x * seg;
+    const long s1 = min(s0 + (long)seg, total);
     float sD = 0.f, sK = 0.f, sW = 0.f, sH = 0.f;
-    if (x0 < x1)
-        pullback_tile<T, GR>(u, gfield, lam, hfield, u1, lam_out, G, P, blockIdx.x * T::TZ, blockIdx.y * T::TY, x0,
-                             x1, cs, gs, ms, bs, sD, sK, sW, sH);
+    while (s0 < s1) {
+        const int t = (int)(s0 / G.nx);
+        const int xa = (int)(s0 - (long)t * G.nx);
+        const int xb = (int)min((long)G.nx, xa + (s1 - s0));
+        pullback_tile<T, GR>(u, gfield, lam, hfield, u1, lam_out, G, P, (t % ntz) * T::TZ, (t / ntz) * T::TY, xa,
+                             xb, cs, gs, ms, bs, sD, sK, sW, sH);
+        s0 += xb - xa;   // the tile's last barrier protects the rings from the next tile's prologue
+    }
     if (GR) {
-        const size_t blk = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-        block_reduce4(sD, sK, sW, sH, red, part + blk * 4);
-        if (GR == 2 && sink.counter) last_block_reduce(part, (int)(gridDim.x * gridDim.y * gridDim.z), sink, red);
+        block_reduce4(sD, sK, sW, sH, red, part + (size_t)blockIdx.x * 4);
+        if (GR == 2 && sink.counter) last_block_reduce(part, (int)gridDim.x, sink, red);
     }
 }
 
@@ -466,10 +488,18 @@ void init_occupancy() {
     setup(ch_pullback_batch_kernel<true>, &g_batch_bps[1]);
 }
 
+// One wave of blocks over equal segments of the tile-major (tile, x) plane
+// sequence, at least 16 planes each (the x halo costs 6 plane loads per piece).
 template <class T>
-dim3 pb_grid(const evx_grid* g, int grads, int* lx) {
+dim3 pb_grid(const evx_grid* g, int grads, int* seg) {
     const int v = std::is_same<T, TileWide>::value ? 0 : 1;
-    return fast_grid<T>(g->nx, g->ny, g->nz, g_bps[v][grads], g_sms, lx);
+    const long tiles = (long)((g->nz + T::TZ - 1) / T::TZ) * ((g->ny + T::TY - 1) / T::TY);
+    const long total = tiles * g->nx;
+    const long slots = (long)std::max(1, g_bps[v][grads]) * std::max(1, g_sms);
+    long len = (total + slots - 1) / slots;
+    len = std::max(len, std::min<long>(16, g->nx));
+    *seg = (int)len;
+    return dim3((unsigned)((total + len - 1) / len));
 }
 
 template <class T>
@@ -478,22 +508,22 @@ int pb_launch_t(int grads, const float* u, const float* g, const float* lam, con
                 cudaStream_t st, int* n_part_used, const GradSink* sink) {
     const GradSink none{nullptr, nullptr, 0, nullptr, 0.0, 0.0, 0.0};
     const GradSink S = (grads == 2 && sink) ? *sink : none;
-    int lx;
-    const dim3 grid = pb_grid<T>(grid_, grads, &lx);
-    const int nb = (int)(grid.x * grid.y * grid.z);
+    int seg;
+    const dim3 grid = pb_grid<T>(grid_, grads, &seg);
+    const int nb = (int)grid.x;
     if (grads && nb > n_part_cap) return fail(EVX_ERR_WORKSPACE, "partial-sum buffer too small (%d > %d)", nb, n_part_cap);
     if (n_part_used) *n_part_used = nb;
     if (grads == 1)
         EVX_TIMED("ch_pullback_grads", st,
-                  ch_pullback_fast_kernel<T, 1><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, lx, S));
+                  ch_pullback_fast_kernel<T, 1><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, seg, S));
     else if (grads == 2)
         EVX_TIMED("ch_pullback_grads_spec", st,
                   ch_pullback_fast_kernel<T, 2><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out, part,
-                                                                                 G, P, lx, S));
+                                                                                 G, P, seg, S));
     else
         EVX_TIMED("ch_pullback", st,
                   ch_pullback_fast_kernel<T, 0><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
-                                                                                 nullptr, G, P, lx, S));
+                                                                                 nullptr, G, P, seg, S));
     count_launch();
     return check_launch("ch_pullback_fast_kernel");
 }
@@ -502,9 +532,9 @@ int pb_launch_t(int grads, const float* u, const float* g, const float* lam, con
 
 int ch_pullback_fast_blocks(const evx_grid* g) {
     init_occupancy();
-    int lx, most = 0;
+    int seg, most = 0;
     for (int grads : {0, 1, 2}) {
-        dim3 a = pb_grid<TileWide>(g, grads, &lx), b = pb_grid<TileSquare>(g, grads, &lx);
+        dim3 a = pb_grid<TileWide>(g, grads, &seg), b = pb_grid<TileSquare>(g, grads, &seg);
         most = std::max(most, (int)std::max(a.x * a.y * a.z, b.x * b.y * b.z));
     }
     return most;
