@@ -43,6 +43,13 @@ using TileSquare = Tile<32, 32>;
 constexpr int MAX_FIELD = TileWide::FIELD > TileSquare::FIELD ? TileWide::FIELD : TileSquare::FIELD;
 constexpr int MAX_POT = TileWide::POT > TileSquare::POT ? TileWide::POT : TileSquare::POT;
 
+// Shared plane rings of the x-streaming tiles: NC field slots and NM potential
+// slots, enough for one block barrier per plane (plane i's output, the
+// potential of plane i+2 and the store of plane i+4 in one step).
+constexpr int NC = 5, NM = 3;
+__device__ __forceinline__ int cslot(int p) { return (p + 10) % NC; }   // p >= -5
+__device__ __forceinline__ int mslot(int p) { return (p + 9) % NM; }
+
 __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void sts2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }

@@ -23,11 +23,7 @@ namespace {
 
 using namespace fast;
 
-constexpr int NC = 5, NM = 3;   // field / potential ring slots
 constexpr int RING_C = NC * MAX_FIELD, RING_M = NM * MAX_POT;
-// ring slots of plane p (p >= -5)
-__device__ __forceinline__ int cslot(int p) { return (p + 10) % NC; }
-__device__ __forceinline__ int mslot(int p) { return (p + 9) % NM; }
 constexpr size_t ADJ_SMEM = (size_t)(2 * RING_C + 2 * RING_M) * sizeof(float) + 4 * 8 * sizeof(double);
 
 // Two points of a patch row (z-adjacent) are processed together with the
@@ -123,7 +119,7 @@ __device__ __noinline__ void last_block_reduce(const double* part, int nblk, con
     }
 }
 
-template <class T, int GR>
+template <class T, int GR, bool ONEBAR = true>
 __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const float* __restrict__ gfield,
                                               const float* __restrict__ lam, const float* __restrict__ hfield,
                                               const float* __restrict__ u1, float* __restrict__ lam_out,
@@ -132,6 +128,9 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
                                               float& sD, float& sK, float& sW, float& sH) {
     const int tid = threadIdx.x;
     const int tx = tid % T::BX, ty = tid / T::BX;
+    // ring slots: NC / NM slots with one barrier per plane, else 4 / 2 slots and two
+    auto cslt = [](int p) { return ONEBAR ? cslot(p) : (p & 3); };
+    auto mslt = [](int p) { return ONEBAR ? mslot(p) : (p & 1); };
     const int W = T::W;
     const int nx = G.nx, ny = G.ny, nz = G.nz;
     const size_t plane = (size_t)ny * nz;
@@ -167,8 +166,8 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         }
     };
     auto stash = [&](int p) {
-        float* dc = cs + cslot(p) * T::FIELD;
-        float* dg = gs + cslot(p) * T::FIELD;
+        float* dc = cs + cslt(p) * T::FIELD;
+        float* dg = gs + cslt(p) * T::FIELD;
 #pragma unroll
         for (int s = 0; s < 2; ++s)
             if (LP.valid[s]) {
@@ -179,22 +178,22 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
 
     float2 gxm[2][2];   // Gbar on the x face below the current potential plane, per patch row
     auto gx_faces = [&](int plo, int m, float2 out[2]) {
-        const float* c0 = cs + cslot(plo) * T::FIELD;
-        const float* c1 = cs + cslot(plo + 1) * T::FIELD;
-        const float* g0 = gs + cslot(plo) * T::FIELD;
-        const float* g1 = gs + cslot(plo + 1) * T::FIELD;
+        const float* c0 = cs + cslt(plo) * T::FIELD;
+        const float* c1 = cs + cslt(plo + 1) * T::FIELD;
+        const float* g0 = gs + cslt(plo) * T::FIELD;
+        const float* g1 = gs + cslt(plo + 1) * T::FIELD;
         const int a = mr[m] * W + mc[m], b = a + W;
         out[0] = gbar2(lds2(c0 + a), lds2(c1 + a), lds2(g0 + a), lds2(g1 + a), ihDx);
         out[1] = gbar2(lds2(c0 + b), lds2(c1 + b), lds2(g0 + b), lds2(g1 + b), ihDx);
     };
 
     auto compute_mu = [&](int p) {
-        const float* cc = cs + cslot(p) * T::FIELD;
-        const float* cm = cs + cslot(p - 1) * T::FIELD;
-        const float* cp = cs + cslot(p + 1) * T::FIELD;
-        const float* gc = gs + cslot(p) * T::FIELD;
-        float* mo = ms + mslot(p) * T::POT;
-        float* bo = bs + mslot(p) * T::POT;
+        const float* cc = cs + cslt(p) * T::FIELD;
+        const float* cm = cs + cslt(p - 1) * T::FIELD;
+        const float* cp = cs + cslt(p + 1) * T::FIELD;
+        const float* gc = gs + cslt(p) * T::FIELD;
+        float* mo = ms + mslt(p) * T::POT;
+        float* bo = bs + mslt(p) * T::POT;
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
             if (!mv[m]) continue;
@@ -235,12 +234,12 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     // x face cbar of the output patch between planes plo and plo+1
     float2 cfx_m[2], c_prev[2], b_prev[2];
     auto x_faces_b = [&](int plo, float2 out[2]) {
-        const float* c0 = cs + cslot(plo) * T::FIELD;
-        const float* c1 = cs + cslot(plo + 1) * T::FIELD;
-        const float* g0 = gs + cslot(plo) * T::FIELD;
-        const float* g1 = gs + cslot(plo + 1) * T::FIELD;
-        const float* m0 = ms + mslot(plo) * T::POT;
-        const float* m1 = ms + mslot(plo + 1) * T::POT;
+        const float* c0 = cs + cslt(plo) * T::FIELD;
+        const float* c1 = cs + cslt(plo + 1) * T::FIELD;
+        const float* g0 = gs + cslt(plo) * T::FIELD;
+        const float* g1 = gs + cslt(plo + 1) * T::FIELD;
+        const float* m0 = ms + mslt(plo) * T::POT;
+        const float* m1 = ms + mslt(plo + 1) * T::POT;
         out[0] = cfb2(lds2(c0 + pa), lds2(c1 + pa), lds2(m0 + pa - W), lds2(m1 + pa - W), lds2(g0 + pa),
                       lds2(g1 + pa), ihx, ihDx);
         out[1] = cfb2(lds2(c0 + pb), lds2(c1 + pb), lds2(m0 + pb - W), lds2(m1 + pb - W), lds2(g0 + pb),
@@ -248,11 +247,11 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     };
 
     auto compute_lam = [&](int i) {
-        const float* cc = cs + cslot(i) * T::FIELD;
-        const float* gc = gs + cslot(i) * T::FIELD;
-        const float* mm = ms + mslot(i) * T::POT;
-        const float* bb = bs + mslot(i) * T::POT;
-        const float* bp = bs + mslot(i + 1) * T::POT;
+        const float* cc = cs + cslt(i) * T::FIELD;
+        const float* gc = gs + cslt(i) * T::FIELD;
+        const float* mm = ms + mslt(i) * T::POT;
+        const float* bb = bs + mslt(i) * T::POT;
+        const float* bp = bs + mslt(i + 1) * T::POT;
         // acc: sum of cbar-face values around each point (times 0.5 at the end)
         float2 accA, accB;
         {
@@ -305,7 +304,7 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             if (wj1) *reinterpret_cast<float2*>(lam_out + o + nz) = oB;
         }
         if (GR) {
-            const float* cx = cs + cslot(i + 1) * T::FIELD;
+            const float* cx = cs + cslt(i + 1) * T::FIELD;
             const float2 lcA = lap2(L, A, c_prev[0], lds2(cx + pa), up, B, zmA, zpA);
             const float2 lcB = lap2(L, B, c_prev[1], lds2(cx + pb), A, dn, zmB, zpB);
             if (wj0) {
@@ -335,43 +334,70 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         b_prev[1] = bB;
     };
 
-    // prologue: planes x0-2 .. x0+2 staged; potentials x0-1 .. x0+1; plane x0+3
-    // staged into the slot of x0-2; carried x quantities.  Planes up to x1+1 and
-    // potentials up to x1 are needed.
-    for (int p = x0 - 2; p <= x0 + 2; ++p) {
-        fetch(p);
-        stash(p);
-    }
-    fetch(x0 + 3);
-    __syncthreads();
+    if (ONEBAR) {
+        // prologue: planes x0-2 .. x0+2 staged; potentials x0-1 .. x0+1; plane
+        // x0+3 staged into the slot of x0-2; carried x quantities.  Planes up to
+        // x1+1 and potentials up to x1 are needed.
+        for (int p = x0 - 2; p <= x0 + 2; ++p) {
+            fetch(p);
+            stash(p);
+        }
+        fetch(x0 + 3);
+        __syncthreads();
 #pragma unroll
-    for (int m = 0; m < 2; ++m)
-        if (mv[m]) gx_faces(x0 - 2, m, gxm[m]);
-    compute_mu(x0 - 1);
-    compute_mu(x0);
-    compute_mu(x0 + 1);
-    __syncthreads();
-    if (x0 + 3 <= x1 + 1) stash(x0 + 3);
-    if (x0 + 4 <= x1 + 1) fetch(x0 + 4);
+        for (int m = 0; m < 2; ++m)
+            if (mv[m]) gx_faces(x0 - 2, m, gxm[m]);
+        compute_mu(x0 - 1);
+        compute_mu(x0);
+        compute_mu(x0 + 1);
+        __syncthreads();
+        if (x0 + 3 <= x1 + 1) stash(x0 + 3);
+        if (x0 + 4 <= x1 + 1) fetch(x0 + 4);
+    } else {
+        // prologue: planes x0-2 .. x0+1 staged; potentials x0-1, x0
+        for (int p = x0 - 2; p <= x0 + 1; ++p) {
+            fetch(p);
+            stash(p);
+        }
+        fetch(x0 + 2);
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+            if (mv[m]) gx_faces(x0 - 2, m, gxm[m]);
+        compute_mu(x0 - 1);
+        compute_mu(x0);
+        __syncthreads();
+    }
     x_faces_b(x0 - 1, cfx_m);
     {
-        const float* cprev = cs + cslot(x0 - 1) * T::FIELD;
-        const float* bprev = bs + mslot(x0 - 1) * T::POT;
+        const float* cprev = cs + cslt(x0 - 1) * T::FIELD;
+        const float* bprev = bs + mslt(x0 - 1) * T::POT;
         c_prev[0] = lds2(cprev + pa);
         c_prev[1] = lds2(cprev + pb);
         b_prev[0] = lds2(bprev + pa - W);
         b_prev[1] = lds2(bprev + pb - W);
     }
-    __syncthreads();
-    // plane i: lam(i) reads potentials i, i+1 and planes i, i+1; mu(i+2) reads
-    // planes i+1 .. i+3 and writes the potential slot of i-1; the stash of plane
-    // i+4 overwrites the slot of plane i-1 - all last read before the barrier
-    for (int i = x0; i < x1; ++i) {
-        compute_lam(i);
-        if (i + 2 <= x1) compute_mu(i + 2);
-        if (i + 4 <= x1 + 1) stash(i + 4);
-        if (i + 5 <= x1 + 1) fetch(i + 5);
+    if (ONEBAR) {
         __syncthreads();
+        // plane i: lam(i) reads potentials i, i+1 and planes i, i+1; mu(i+2) reads
+        // planes i+1 .. i+3 and writes the potential slot of i-1; the stash of
+        // plane i+4 overwrites the slot of plane i-1 - all last read before the barrier
+        for (int i = x0; i < x1; ++i) {
+            compute_lam(i);
+            if (i + 2 <= x1) compute_mu(i + 2);
+            if (i + 4 <= x1 + 1) stash(i + 4);
+            if (i + 5 <= x1 + 1) fetch(i + 5);
+            __syncthreads();
+        }
+    } else {
+        for (int i = x0; i < x1; ++i) {
+            stash(i + 2);
+            if (i + 3 <= x1 + 1) fetch(i + 3);
+            __syncthreads();
+            compute_mu(i + 1);
+            __syncthreads();
+            compute_lam(i);
+        }
     }
     sD += aD.x + aD.y;
     sK += aK.x + aK.y;
@@ -452,11 +478,11 @@ ch_pullback_batch_kernel(const float* __restrict__ u, const float* __restrict__ 
         const size_t o = (size_t)B.off;
         float sD = 0.f, sK = 0.f, sW = 0.f, sH = 0.f;
         if (B.tile == 0)
-            pullback_tile<TileWide, GRADS ? 1 : 0>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
+            pullback_tile<TileWide, GRADS ? 1 : 0, false>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
                                            GRADS ? u1 + o : nullptr, lam_out + o, G, B.P, I.k0, I.j0, I.x0, I.x1, cs,
                                            gs, ms, bs, sD, sK, sW, sH);
         else
-            pullback_tile<TileSquare, GRADS ? 1 : 0>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
+            pullback_tile<TileSquare, GRADS ? 1 : 0, false>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
                                              GRADS ? u1 + o : nullptr, lam_out + o, G, B.P, I.k0, I.j0, I.x0, I.x1,
                                              cs, gs, ms, bs, sD, sK, sW, sH);
         if (GRADS) block_reduce4(sD, sK, sW, sH, red, part + (size_t)I.part * 4);

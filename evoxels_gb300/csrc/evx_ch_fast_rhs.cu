@@ -3,10 +3,10 @@
 // kernel and the reference (evoxels/problem_definition.py:350-371); the
 // translation unit is compiled with --fmad=false, so results are bit-identical.
 //
-// Per x-plane i a tile: stores the prefetched field plane i+2 (clipped) into a
-// 4-slot shared ring and issues the global loads of plane i+3; computes the
-// chemical potential of plane i+1 over the tile grown by one cell (2-slot
-// ring); then computes r on plane i.  Two barriers per plane.
+// Per x-plane i a tile: computes r on plane i, the chemical potential of plane
+// i+2 over the tile grown by one cell (3-slot ring), stores the prefetched
+// field plane i+4 (clipped) into a 5-slot shared ring and issues the global
+// loads of plane i+5.  One barrier per plane.
 //
 // The tile body is shared by the single-grid kernel (one block per tile and
 // x-chunk) and the batched kernel (persistent blocks pulling instance x tile x
@@ -96,16 +96,16 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
         }
     };
     auto stash = [&](int p) {
-        float* dst = cs + (p & 3) * T::FIELD;
+        float* dst = cs + cslot(p) * T::FIELD;
 #pragma unroll
         for (int s = 0; s < 2; ++s)
             if (LP.valid[s]) sts4(dst + LP.soff[s], clip4(pf[s]));
     };
     auto compute_mu = [&](int p) {
-        const float* cc = cs + (p & 3) * T::FIELD;
-        const float* cm = cs + ((p - 1) & 3) * T::FIELD;
-        const float* cp = cs + ((p + 1) & 3) * T::FIELD;
-        float* mo = ms + (p & 1) * T::POT;
+        const float* cc = cs + cslot(p) * T::FIELD;
+        const float* cm = cs + cslot(p - 1) * T::FIELD;
+        const float* cp = cs + cslot(p + 1) * T::FIELD;
+        float* mo = ms + mslot(p) * T::POT;
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
             if (!mv[m]) continue;
@@ -121,18 +121,18 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
 
     float2 fxm[2] = {f2s(0.f), f2s(0.f)};   // x flux on the face below the current plane (rows a, b)
     auto x_faces = [&](int plo, float2 out[2]) {
-        const float* c0 = cs + (plo & 3) * T::FIELD;
-        const float* c1 = cs + ((plo + 1) & 3) * T::FIELD;
-        const float* m0 = ms + (plo & 1) * T::POT;
-        const float* m1 = ms + ((plo + 1) & 1) * T::POT;
+        const float* c0 = cs + cslot(plo) * T::FIELD;
+        const float* c1 = cs + cslot(plo + 1) * T::FIELD;
+        const float* m0 = ms + mslot(plo) * T::POT;
+        const float* m1 = ms + mslot(plo + 1) * T::POT;
         const int a = ra * W + rc, b = a + W;
         out[0] = flux_x2(lds2(c0 + a), lds2(c1 + a), lds2(m0 + a - W), lds2(m1 + a - W), K.ihx);
         out[1] = flux_x2(lds2(c0 + b), lds2(c1 + b), lds2(m0 + b - W), lds2(m1 + b - W), K.ihx);
     };
 
     auto compute_r = [&](int i) {
-        const float* cc = cs + (i & 3) * T::FIELD;
-        const float* mm = ms + (i & 1) * T::POT;
+        const float* cc = cs + cslot(i) * T::FIELD;
+        const float* mm = ms + mslot(i) * T::POT;
         const int a = ra * W + rc, b = a + W;     // field offsets; potential offsets are one row up
         float2 fxp[2];
         x_faces(i, fxp);
@@ -161,24 +161,32 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
         fxm[1] = fxp[1];
     };
 
-    // prologue: field planes x0-2 .. x0+1, potentials x0-1 and x0, first x face
-    for (int p = x0 - 2; p <= x0 + 1; ++p) {
+    // prologue: field planes x0-2 .. x0+2, potentials x0-1 .. x0+1, plane x0+3
+    // into the slot of x0-2, first x face.  Planes up to x1+1 and potentials up
+    // to x1 are needed; every plane is fetched (and, fused, written) once.
+    for (int p = x0 - 2; p <= x0 + 2; ++p) {
         fetch(p);
         stash(p);
     }
-    fetch(x0 + 2);
+    fetch(x0 + 3);
     __syncthreads();
     compute_mu(x0 - 1);
     compute_mu(x0);
+    compute_mu(x0 + 1);
     __syncthreads();
+    if (x0 + 3 <= x1 + 1) stash(x0 + 3);
+    if (x0 + 4 <= x1 + 1) fetch(x0 + 4);
     x_faces(x0 - 1, fxm);
+    __syncthreads();
+    // plane i: r(i) reads potentials i, i+1 and planes i, i+1; mu(i+2) reads
+    // planes i+1 .. i+3 and writes the potential slot of i-1; the store of plane
+    // i+4 overwrites the slot of plane i-1 - all last read before the barrier
     for (int i = x0; i < x1; ++i) {
-        stash(i + 2);
-        if (i + 3 <= x1 + 1) fetch(i + 3);
-        __syncthreads();
-        compute_mu(i + 1);
-        __syncthreads();
         compute_r(i);
+        if (i + 2 <= x1) compute_mu(i + 2);
+        if (i + 4 <= x1 + 1) stash(i + 4);
+        if (i + 5 <= x1 + 1) fetch(i + 5);
+        __syncthreads();
     }
 }
 
@@ -186,8 +194,8 @@ template <class T, bool FUSED>
 __global__ void __launch_bounds__(THREADS, 4)
 ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, float* __restrict__ u_new,
                    float* __restrict__ r, Geo G, ChP P, int LX) {
-    __shared__ __align__(16) float cs[4 * T::FIELD];
-    __shared__ __align__(16) float ms[2 * T::POT];
+    __shared__ __align__(16) float cs[NC * T::FIELD];
+    __shared__ __align__(16) float ms[NM * T::POT];
     const int x0 = blockIdx.z * LX;
     const int x1 = min(x0 + LX, G.nx);
     if (x0 >= x1) return;   // uniform across the block
@@ -208,14 +216,15 @@ __device__ __forceinline__ Geo batch_geo(const BatchInst& B) {
     return G;
 }
 
-// Persistent batched rhs: blocks pull work items until the list is exhausted.
+// Persistent batched rhs: blocks pull work items until the list is exhausted
+// (3 blocks per SM: the item loop's state does not fit the 64 registers of 4).
 template <bool FUSED>
-__global__ void __launch_bounds__(THREADS, 4)
+__global__ void __launch_bounds__(THREADS, 3)
 ch_rhs_batch_kernel(const float* __restrict__ u, const float* __restrict__ upd, float* __restrict__ u_new,
                     float* __restrict__ r, const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
                     int n_items, int* __restrict__ counter) {
-    __shared__ __align__(16) float cs[4 * MAX_FIELD];
-    __shared__ __align__(16) float ms[2 * MAX_POT];
+    __shared__ __align__(16) float cs[NC * MAX_FIELD];
+    __shared__ __align__(16) float ms[NM * MAX_POT];
     __shared__ int s_item;
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
