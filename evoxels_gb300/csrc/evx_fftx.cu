@@ -65,12 +65,14 @@ __device__ int g_dev_status;       // bit 0: an x-pass barrier wait gave up
 // hv), 3 adjoint g with the Parseval sums against dsp, 4 multiplier table
 // (mult[kx*M + pencil], mrow = mult + pencil).  dsp points at the tile's stored
 // spectrum ([element][thread], thread offset included).
-template <int N1, int N2, int MODE>
+// PRE (mode 3): the stored spectrum values come preloaded in dpre[q*N2 + k2].
+template <int N1, int N2, int MODE, bool PRE = false>
 __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 2 ? N1 : 1], float2* xs,
                                           const Col<N1, N2>& c, float ky2v, float kz2v, float wz,
                                           const float* __restrict__ kx2, float sym_coef, float dt, float invN,
                                           float2* __restrict__ dsp, float& t1, float& t2,
-                                          const float* __restrict__ mrow = nullptr, int M = 0) {
+                                          const float* __restrict__ mrow = nullptr, int M = 0,
+                                          const float2 (*dpre)[PRE ? N1 : 1] = nullptr) {
     constexpr int N = N1 * N2, Q = N1 / N2;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -96,7 +98,9 @@ __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 
                 const float sg = pre * invN;
                 if constexpr (MODE == 2) b[k2] = make_float2(a[k2].x * (sg * k4), a[k2].y * (sg * k4));
                 if constexpr (MODE == 3) {
-                    const float2 d = dsp[(q * N2 + k2) * 256];
+                    float2 d;
+                    if constexpr (PRE) d = (*dpre)[q * N2 + k2];
+                    else d = dsp[(q * N2 + k2) * 256];
                     const float re = wz * (a[k2].x * d.x + a[k2].y * d.y);
                     t1 += re;
                     t2 += re * (pre * k4);
@@ -312,7 +316,16 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
             issue_load((it + 1) % XSTAGES, next);
             if (MODE == 3) prefetch_l2(dspec + (size_t)next * N1 * 256, N1 * 256 * sizeof(float2));
         }
-        if (MODE == 3) {   // this tile's stored spectrum into L1 (it sits in L2 from the previous tile's prefetch)
+        // mode 3: this tile's stored spectrum (in L2 from the previous tile's
+        // prefetch) into registers now, in flight while the tile's data arrives
+        // and its first stage runs; N1 = 32 prefetches into L1 instead
+        constexpr bool PRE = MODE == 3 && N1 <= 16;
+        float2 dpre[PRE ? N1 : 1];
+        if constexpr (PRE) {
+            const float2* dp = dspec + (size_t)tile * N1 * 256 + tid;
+#pragma unroll
+            for (int e = 0; e < N1; ++e) dpre[e] = __ldcs(dp + e * 256);
+        } else if (MODE == 3) {
             const float2* dp = dspec + (size_t)tile * N1 * 256 + tid;
 #pragma unroll
             for (int e = 0; e < N1; ++e) asm volatile("prefetch.global.L1 [%0];" ::"l"(dp + e * 256));
@@ -330,8 +343,8 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         for (int n1 = 0; n1 < N1; ++n1) v[n1] = xs[(N2 * n1 + c.n2) * P + c.p];
         fwd_stage1<N1, N2>(v, xs, c);
         float2 hv[1];
-        mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2,
-                                mult + mc, M);
+        mid_stage<N1, N2, MODE, PRE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1,
+                                     t2, mult + mc, M, &dpre);
         inv_stage1<N1, N2>(v, xs, c);
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) xs[(N2 * n1 + c.n2) * P + c.p] = v[n1];
