@@ -49,8 +49,8 @@ NCU_DRAM_BYTES_PER_VOXEL = {
     "fd_tblock2": (554.379264e6 + 495.615488e6) / 512 ** 3,
     "ch_xpass_adj_spec": (135.378432e6 + 24.717824e6) / 256 ** 3,
     "ch_xpass_fwd": (135.399168e6 + 74.517248e6) / (512 * 256 * 256),
-    "ch_pullback_grads_spec": (210.139904e6 + 50.355968e6) / 256 ** 3,
-    "ac_rhs": (68.469504e6 + 26.936320e6) / 256 ** 3,
+    "ch_pullback_grads_spec": (300.036608e6 + 57.321984e6) / 256 ** 3,
+    "ac_rhs": (68.689152e6 + 24.427008e6) / 256 ** 3,
 }
 
 
