@@ -211,22 +211,31 @@ class ChFwdAdj:
                        "stored_spectra": self.spectra is not None,
                        "l2": "inputs larger than L2: the kept trajectory is %.2f GB" % ((self.T + 1) * 4 * self.n / 1e9)}
 
-    def step(self):
+    def step(self, before_loss=None):
         """Device-resident step: forward (trajectory kept), loss gradient, adjoint."""
         r = self.runner
         r.forward(self.traj[0:1], self.T, 1.0, 3.0, traj=self.traj[1:], spectra=self.spectra)
+        if before_loss is not None:
+            before_loss()
         loss = r.mse(self.traj[self.T:self.T + 1], self.target, self.lam)
         grads = self.torch.zeros(3, dtype=self.torch.float64, device=self.c0.device) if self.grads else None
         g0 = r.adjoint(self.traj, self.T, self.lam, 1.0, 3.0, grads, self.spectra)
         return loss, g0, grads
 
     def step_e2e(self):
-        """Same step from host buffers: H2D of c0 and target, D2H of dL/dc0, loss and grads."""
+        """Same step from host buffers: H2D of c0 and target, D2H of dL/dc0, loss and grads.  The
+        target's copy runs on a side stream during the forward steps (the loss is its first use)."""
+        torch = self.torch
+        cur = torch.cuda.current_stream()
+        if not hasattr(self, "side"):
+            self.side = torch.cuda.Stream()
         self.c0.copy_(self.c0_host, non_blocking=True)
-        self.target.copy_(self.t_host, non_blocking=True)
-        loss, g0, grads = self.step()
+        self.side.wait_stream(cur)             # the previous step's loss has read the target
+        with torch.cuda.stream(self.side):
+            self.target.copy_(self.t_host, non_blocking=True)
+        loss, g0, grads = self.step(before_loss=lambda: cur.wait_stream(self.side))
         self.g_host.copy_(g0, non_blocking=True)
-        out = self.torch.cat([loss, grads]).cpu()
+        out = torch.cat([loss, grads]).cpu()
         return out
 
     def e2e_bytes(self):
