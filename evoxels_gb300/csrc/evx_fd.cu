@@ -281,14 +281,24 @@ fd_step_reg_kernel(const float* __restrict__ u, float* __restrict__ out, Geo G, 
     int ip = x0 + 1;
     if (ip >= nx) ip -= nx;
     float4 xp = ld4(col + ip * plane);
+    // y and z-edge neighbours of the current plane, loaded one plane ahead
+    float4 ymn = ld4(col + x0 * plane + dym), ypn = ld4(col + x0 * plane + dyp);
+    float eln = left_load ? __ldg(col + x0 * plane + dzl) : 0.f;
+    float ern = right_load ? __ldg(col + x0 * plane + dzr) : 0.f;
     for (int i = x0; i < x1; ++i) {
         const float* cp = col + i * plane;
-        float4 ym = ld4(cp + dym), yp = ld4(cp + dyp);
-        const float el = left_load ? __ldg(cp + dzl) : 0.f;
-        const float er = right_load ? __ldg(cp + dzr) : 0.f;
+        float4 ym = ymn, yp = ypn;
+        const float el = eln, er = ern;
         int in = i + 2;
         while (in >= nx) in -= nx;
         const float4 nxt = ld4(col + in * plane);   // prefetch plane i+2
+        if (i + 1 < x1) {                            // neighbours of plane i+1 (i+1 < nx here)
+            const float* cn = cp + plane;
+            ymn = ld4(cn + dym);
+            ypn = ld4(cn + dyp);
+            eln = left_load ? __ldg(cn + dzl) : 0.f;
+            ern = right_load ? __ldg(cn + dzr) : 0.f;
+        }
         float zl = __shfl_up_sync(0xffffffffu, c.w, 1);
         float zr = __shfl_down_sync(0xffffffffu, c.x, 1);
         if (left_load) zl = el;
