@@ -359,11 +359,26 @@ int fd_step_reg_launch(const float* in, float* out, const Geo& G, float D, float
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_fd_sms, cudaDevAttrMultiProcessorCount, dev);
     }
+    static int bps = 0;   // resident blocks per SM
+    if (!bps) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fd_step_reg_kernel<UNIT>, 128, 0);
+        if (bps < 1) bps = 1;
+    }
     const int nq = G.nz / 4;
     const int bx = (nq + 31) / 32, by = (G.ny + 3) / 4;
-    const long cols = (long)bx * by;
-    long chunks = 16L * g_fd_sms / cols;   // ~16 resident 128-thread blocks per SM
-    if (chunks < 1) chunks = 1;
+    const long cols = (long)bx * by, slots = (long)bps * g_fd_sms;
+    // x chunks per column: whole waves of resident blocks (the least idle tail),
+    // and among those the longest x-runs (2 halo planes per chunk), at least 8 planes
+    long chunks = 1;
+    double best = 1e30;
+    for (long c = 1; c <= std::max(1, G.nx / 8); ++c) {
+        const long blocks = cols * c, waves = (blocks + slots - 1) / slots;
+        const double cost = (double)waves * ((double)((G.nx + c - 1) / c) + 2.0);   // time ~ waves x planes per block
+        if (cost < best - 1e-9) {
+            best = cost;
+            chunks = c;
+        }
+    }
     int lx = (int)((G.nx + chunks - 1) / chunks);
     lx = std::max(lx, std::min(G.nx, 8));
     dim3 grid(bx, by, (G.nx + lx - 1) / lx);
