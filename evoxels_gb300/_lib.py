@@ -92,6 +92,8 @@ _SIGS = {
     "evx_rkc_stage": (C.c_int, [_P, _P, _P, _P, _P, C.POINTER(EvxRkcCoeffs), _P, C.c_size_t, _P]),
     "evx_fft_yz_r2c": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
     "evx_fft_yz_c2r": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
+    "evx_fft_z_r2c": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
+    "evx_fft_z_c2r": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),
     "evx_ch_forward_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_adjoint_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_set_tile_variant": (C.c_int, [C.c_int]),

@@ -28,7 +28,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contra
               "-Xptxas", "-v", "-I", INCLUDE]
 # Forward kernels mirror the reference's float32 rounding op by op: no FMA
 # contraction.  The adjoint has no bitwise-parity requirement and contracts.
-FMAD_ON = {"evx_adjoint.cu", "evx_ch_fast_adj.cu", "evx_fftx.cu", "evx_fftyz.cu"}
+FMAD_ON = {"evx_adjoint.cu", "evx_ch_fast_adj.cu", "evx_fftx.cu", "evx_fftyz.cu", "evx_fftz.cu"}
 
 
 def _fmad(src):

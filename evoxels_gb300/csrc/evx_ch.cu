@@ -279,6 +279,14 @@ int ch_plan_bind(evx_ch_plan* plan, void* workspace, cudaStream_t st, bool need_
     if ((rc = check_cufft(cufftSetWorkArea(plan->c2r, fw), "cufftSetWorkArea"))) return rc;
     if ((rc = check_cufft(cufftSetStream(plan->r2c, st), "cufftSetStream"))) return rc;
     if ((rc = check_cufft(cufftSetStream(plan->c2r, st), "cufftSetStream"))) return rc;
+    if (plan->yc2c) {
+        if ((rc = check_cufft(cufftSetWorkArea(plan->yc2c, fw), "cufftSetWorkArea"))) return rc;
+        if ((rc = check_cufft(cufftSetStream(plan->yc2c, st), "cufftSetStream"))) return rc;
+    }
+    if (plan->yc2c2) {
+        if ((rc = check_cufft(cufftSetWorkArea(plan->yc2c2, fw), "cufftSetWorkArea"))) return rc;
+        if ((rc = check_cufft(cufftSetStream(plan->yc2c2, st), "cufftSetStream"))) return rc;
+    }
     if (need_c2r2) {
         if (!plan->has_c2r2) return fail(EVX_ERR_BAD_ARG, "parameter gradients need a plan created with flags bit 0");
         if ((rc = check_cufft(cufftSetWorkArea(plan->c2r2, fw), "cufftSetWorkArea"))) return rc;
@@ -289,6 +297,14 @@ int ch_plan_bind(evx_ch_plan* plan, void* workspace, cudaStream_t st, bool need_
 
 int ch_r2c(evx_ch_plan* plan, const float* in, float2* out, cudaStream_t st) {
     if (plan->yzmode) return fft_yz_r2c(plan->g.nx, plan->g.ny, plan->g.nz, in, out, st);
+    if (plan->ztmode) {   // z pass into [x][kz][y], then the contiguous y transform in place
+        int rc = fft_zt_r2c(plan->g.nx, plan->g.ny, plan->g.nz, in, out, st);
+        if (rc) return rc;
+        cufftResult r;
+        cufftComplex* s = reinterpret_cast<cufftComplex*>(out);
+        EVX_TIMED("cufft_c2c_y", st, r = cufftExecC2C(plan->yc2c, s, s, CUFFT_FORWARD));
+        return check_cufft(r, "cufftExecC2C (y)");
+    }
     cufftResult r;
     EVX_TIMED("cufft_r2c", st, r = cufftExecR2C(plan->r2c, const_cast<cufftReal*>(in), reinterpret_cast<cufftComplex*>(out)));
     return check_cufft(r, "cufftExecR2C");
@@ -300,6 +316,17 @@ int ch_c2r(evx_ch_plan* plan, float2* in, float* out, bool batch2, cudaStream_t 
         int rc = fft_yz_c2r(g.nx, g.ny, g.nz, in, out, st);
         if (!rc && batch2) rc = fft_yz_c2r(g.nx, g.ny, g.nz, in + plan->nspec, out + plan->n, st);
         return rc;
+    }
+    if (plan->ztmode) {   // inverse y transform in place (the input is consumed, as by a C2R), then z
+        const evx_grid& g = plan->g;
+        if (batch2 && !plan->yc2c2) return fail(EVX_ERR_BAD_ARG, "parameter gradients need a plan created with flags bit 0");
+        cufftResult r;
+        cufftComplex* s = reinterpret_cast<cufftComplex*>(in);
+        EVX_TIMED(batch2 ? "cufft_c2c_y_x2" : "cufft_c2c_y", st,
+                  r = cufftExecC2C(batch2 ? plan->yc2c2 : plan->yc2c, s, s, CUFFT_INVERSE));
+        int rc = check_cufft(r, "cufftExecC2C (y)");
+        if (rc) return rc;
+        return fft_zt_c2r(batch2 ? 2 * g.nx : g.nx, g.ny, g.nz, in, out, st);   // two spectra: 2*nx planes
     }
     cufftResult r;
     EVX_TIMED(batch2 ? "cufft_c2r_x2" : "cufft_c2r", st,
@@ -397,6 +424,8 @@ int evx_ch_plan_create_bc(evx_ch_plan** out, const evx_grid* g, const evx_bc* bc
         if (p->r2c) cufftDestroy(p->r2c);
         if (p->c2r) cufftDestroy(p->c2r);
         if (p->c2r2) cufftDestroy(p->c2r2);
+        if (p->yc2c) cufftDestroy(p->yc2c);
+        if (p->yc2c2) cufftDestroy(p->yc2c2);
         if (p->kx2) cudaFree(p->kx2);
         delete p;
         return code;
@@ -412,6 +441,25 @@ int evx_ch_plan_create_bc(evx_ch_plan** out, const evx_grid* g, const evx_bc* bc
     // power-of-two nx: cuFFT transforms (y, z) for every x plane and the fused x-pass does the rest
     p->xmode = xmode;
     p->yzmode = p->xmode && yz_supported(g->ny, g->nz) && (flags & 4);
+    // z pass of our own with a y-contiguous spectrum unless flags bit 3 keeps cuFFT's 2-D plans
+    p->ztmode = p->xmode && !p->yzmode && zt_supported(g->nz) && !(flags & 8);
+    size_t w4 = 0, w5 = 0;
+    if (p->ztmode) {
+        int ny1[1] = {g->ny};
+        const int cols = g->nx * p->nzh;
+        if ((rc = check_cufft(cufftCreate(&p->yc2c), "cufftCreate"))) return cleanup(rc);
+        cufftSetAutoAllocation(p->yc2c, 0);
+        if ((rc = check_cufft(cufftMakePlanMany(p->yc2c, 1, ny1, nullptr, 1, g->ny, nullptr, 1, g->ny, CUFFT_C2C,
+                                                cols, &w4), "cufftMakePlanMany C2C (y)")))
+            return cleanup(rc);
+        if (flags & 1) {
+            if ((rc = check_cufft(cufftCreate(&p->yc2c2), "cufftCreate"))) return cleanup(rc);
+            cufftSetAutoAllocation(p->yc2c2, 0);
+            if ((rc = check_cufft(cufftMakePlanMany(p->yc2c2, 1, ny1, nullptr, 1, g->ny, nullptr, 1, g->ny, CUFFT_C2C,
+                                                    2 * cols, &w5), "cufftMakePlanMany C2C (y) x2")))
+                return cleanup(rc);
+        }
+    }
     if (p->xmode) {
         int d2[2] = {g->ny, g->nz};
         const int pr = g->ny * g->nz, ps = g->ny * p->nzh;
@@ -444,7 +492,7 @@ int evx_ch_plan_create_bc(evx_ch_plan** out, const evx_grid* g, const evx_bc* bc
         }
         p->has_c2r2 = true;
     }
-    p->ws_fft = std::max(w1, std::max(w2, w3));
+    p->ws_fft = std::max(std::max(w1, std::max(w2, w3)), std::max(w4, w5));
     // k^2 tables, bit-identical to the reference's float32 k-grid (2*nx x points when mirrored)
     const size_t nt = (size_t)p->nxe + g->ny + p->nzh;
     float* host = new float[nt];
@@ -488,6 +536,8 @@ int evx_ch_plan_destroy(evx_ch_plan* p) {
     if (p->r2c) cufftDestroy(p->r2c);
     if (p->c2r) cufftDestroy(p->c2r);
     if (p->c2r2) cufftDestroy(p->c2r2);
+    if (p->yc2c) cufftDestroy(p->yc2c);
+    if (p->yc2c2) cufftDestroy(p->yc2c2);
     if (p->kx2) cudaFree(p->kx2);
     delete p;
     return EVX_OK;

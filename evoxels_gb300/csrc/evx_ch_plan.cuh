@@ -18,6 +18,8 @@ struct evx_ch_plan {
     bool has_c2r2 = false;
     bool xmode = false;      // (y, z) transforms batched over x + fused x-pass (power-of-two nx)
     bool yzmode = false;     // the (y, z) transforms by evx_fftyz.cu instead of cuFFT
+    bool ztmode = false;     // z pass by evx_fftz.cu (spectrum [x][kz][y]) + cuFFT contiguous C2C along y
+    cufftHandle yc2c = 0, yc2c2 = 0;   // ztmode: 1-D C2C along y over nx*(nz/2+1) columns (x2: two spectra)
     size_t ws_fft = 0;       // cuFFT work area (max over plans)
     float* kx2 = nullptr;    // device k^2 tables
     float* ky2 = nullptr;
@@ -77,7 +79,8 @@ struct XpassArgs {
     float sym, dt, invN;
     int* n_xpart_out;                  // optional: partial-sum slots written (mode 3)
     int ext;                           // x mirror extension (mode 0 / 4): 1 even, 2 odd; nx = transform length
-    const float* mult;                 // mode 4: multiplier table [kx < nx][pencil < M]
+    const float* mult;                 // mode 4: multiplier table [kx < nx][ky][kz]
+    int nyk;                           // 0: pencil m = ky*nzh + kz; ny: m = kz*ny + ky (y-contiguous spectrum)
 };
 // Batched x-pass (one launch per shape group of the batched path): per-instance
 // spectrum offset and IMEX constants, indexed by blockIdx.y.
@@ -101,11 +104,16 @@ inline XpassArgs xpass_args(const evx_ch_plan* plan, int mode, float2* spec, con
     a.sym = P.sym_coef; a.dt = P.dt;
     a.invN = (float)(1.0 / ((double)plan->nxe * plan->g.ny * plan->g.nz));
     a.ext = plan->xext;
+    a.nyk = plan->ztmode ? plan->g.ny : 0;
     return a;
 }
 
 // Fused (y, z) R2C / C2R of all x planes (evx_fftyz.cu), cuFFT's layout and scaling.
 bool yz_supported(int ny, int nz);
+// Real transforms along z with a y-contiguous half spectrum (evx_fftz.cu).
+bool zt_supported(int nz);
+int fft_zt_r2c(int nx, int ny, int nz, const float* in, float2* out, cudaStream_t st);
+int fft_zt_c2r(int nx, int ny, int nz, const float2* in, float* out, cudaStream_t st);
 int fft_yz_r2c(int nx, int ny, int nz, const float* in, float2* out, cudaStream_t st);
 int fft_yz_c2r(int nx, int ny, int nz, const float2* in, float* out, cudaStream_t st);
 

@@ -232,6 +232,58 @@ __device__ __forceinline__ void inv_stage1(float2 (&v)[N1], const float2* xs, co
     dft<N1, true>(v);
 }
 
+// Variants with the inter-stage twiddles in registers, for columns whose
+// threads in a warp hold different n2 (one table load per thread instead of
+// divergent reads of the constant table in every stage).
+// tw[k1] = W_N^{n2*k1} (forward stage 1)
+template <int N1, int N2>
+__device__ __forceinline__ void fwd_twiddles(float2 (&tw)[N1], int n2) {
+    constexpr int N = N1 * N2;
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) tw[k1] = w512<false>((n2 * k1) * (512 / N));
+}
+// tw[q*N2 + j] = conj W_N^{j*k1}, k1 = n2*Q + q (inverse stage 2)
+template <int N1, int N2>
+__device__ __forceinline__ void inv_twiddles(float2 (&tw)[N1], int n2) {
+    constexpr int N = N1 * N2, Q = N1 / N2;
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int j = 0; j < N2; ++j) tw[q * N2 + j] = w512<true>((j * (n2 * Q + q)) * (512 / N));
+}
+
+template <int N1, int N2, bool WARP = false, class C>
+__device__ __forceinline__ void fwd_stage1_tw(float2 (&v)[N1], float2* xs, const C& c, const float2 (&tw)[N1]) {
+    constexpr int Q = N1 / N2;
+    dft<N1, false>(v);
+    if constexpr (N2 > 1) {
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) xs[c.xi(k1, c.n2)] = cmul(v[k1], tw[k1]);
+        exchange_sync<WARP>();
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+#pragma unroll
+            for (int j = 0; j < N2; ++j) v[q * N2 + j] = xs[c.xi(c.n2 * Q + q, j)];
+    }
+}
+
+template <int N1, int N2, class C>
+__device__ __forceinline__ void inv_stage2_tw(float2 (&v)[N1], float2* xs, const C& c, const float2 (&tw)[N1]) {
+    constexpr int Q = N1 / N2;
+    if constexpr (N2 > 1) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int k1 = c.n2 * Q + q;
+            float2 a[N2];
+#pragma unroll
+            for (int j = 0; j < N2; ++j) a[j] = v[q * N2 + j];
+            dft<N2, true>(a);
+#pragma unroll
+            for (int j = 0; j < N2; ++j) xs[c.xi(k1, j)] = cmul(a[j], tw[q * N2 + j]);
+        }
+    }
+}
+
 }  // namespace
 }  // namespace fft
 }  // namespace evx

@@ -63,7 +63,7 @@ __device__ int g_dev_status;       // bit 0: an x-pass barrier wait gave up
 // twiddle into xs[k1][j] (N2 > 1) or back into v (N2 == 1).  MODE 0 forward
 // (optional store of the product to dsp), 1 adjoint g, 2 adjoint g and h (into
 // hv), 3 adjoint g with the Parseval sums against dsp, 4 multiplier table
-// (mult[kx*M + pencil], mrow = mult + pencil).  dsp points at the tile's stored
+// (mult[kx*M + ky*nzh + kz], mrow = mult + ky*nzh + kz).  dsp points at the tile's stored
 // spectrum ([element][thread], thread offset included).
 // PRE (mode 3): the stored spectrum values come preloaded in dpre[q*N2 + k2].
 template <int N1, int N2, int MODE, bool PRE = false>
@@ -161,7 +161,7 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
              double* __restrict__ xpart, int M, int nzh, int nz,
              const float* __restrict__ kx2, const float* __restrict__ ky2, const float* __restrict__ kz2,
              float sym_coef, float dt, float invN, const XBatchInst* __restrict__ xb,
-             const float* __restrict__ mult = nullptr) {
+             const float* __restrict__ mult = nullptr, int nyk = 0) {
     if (xb) {
         const XBatchInst X = xb[blockIdx.y];
         spec += X.soff;
@@ -178,7 +178,8 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
     const int m = blockIdx.x * P + c.p;
     const bool live = m < M;
     const int mc = live ? m : 0;
-    const int ky = mc / nzh, kz = mc - ky * nzh;
+    // pencil m = ky*nzh + kz, or kz*ny + ky for the y-contiguous spectrum (nyk = ny)
+    const int ky = nyk ? mc % nyk : mc / nzh, kz = nyk ? mc / nyk : mc % nzh;
     const float ky2v = __ldg(ky2 + ky), kz2v = __ldg(kz2 + kz);
     float2* dsp = dspec ? dspec + (size_t)blockIdx.x * N1 * 256 + tid : nullptr;
     float t1 = 0.f, t2 = 0.f;
@@ -198,7 +199,7 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
     fwd_stage1<N1, N2>(v, xs, c);
     float2 hv[MODE == 2 ? N1 : 1];
     mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2,
-                            mult + mc, M);
+                            mult + (ky * nzh + kz), M);
     auto store = [&](float2* dst) {
         if (live) {
 #pragma unroll
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(256, N1 >= 32 ? 1 : 2)
 xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ dspec, double* __restrict__ xpart,
                  int M, int nzh, int nz, int ntiles, const float* __restrict__ kx2, const float* __restrict__ ky2,
                  const float* __restrict__ kz2, float sym_coef, float dt, float invN,
-                 const float* __restrict__ mult) {
+                 const float* __restrict__ mult, int nyk) {
     using C = Col<N1, N2>;
     constexpr int P = 256 / N2, N = C::N;
     constexpr int TILE = N * P;                       // complex values per tile
@@ -334,7 +335,7 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         float2* xs = ring + (size_t)slot * TILE;
         const int m = tile * P + c.p;
         const int mc = m < M ? m : 0;
-        const int ky = mc / nzh, kz = mc - ky * nzh;
+        const int ky = nyk ? mc % nyk : mc / nzh, kz = nyk ? mc / nyk : mc % nzh;
         const float ky2v = __ldg(ky2 + ky), kz2v = __ldg(kz2 + kz);
         float2* dsp = dspec ? dspec + (size_t)tile * N1 * 256 + tid : nullptr;
 
@@ -344,7 +345,7 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         fwd_stage1<N1, N2>(v, xs, c);
         float2 hv[1];
         mid_stage<N1, N2, MODE, PRE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1,
-                                     t2, mult + mc, M, &dpre);
+                                     t2, mult + (ky * nzh + kz), M, &dpre);
         inv_stage1<N1, N2>(v, xs, c);
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) xs[(N2 * n1 + c.n2) * P + c.p] = v[n1];
@@ -407,7 +408,7 @@ int xpass_launch_tile(const XpassArgs& A, cudaStream_t st, const char* slot) {
     EVX_TIMED(slot, st,
               (xpass_kernel<N1, N2, MODE, EXT><<<blocks, 256, smem, st>>>(A.spec, A.spec_h, A.dspec, A.xpart, A.M,
                                                                         A.nzh, A.nz, A.kx2, A.ky2, A.kz2, A.sym,
-                                                                        A.dt, A.invN, nullptr, A.mult)));
+                                                                        A.dt, A.invN, nullptr, A.mult, A.nyk)));
     count_launch();
     return check_launch("xpass_kernel");
 }
@@ -446,7 +447,7 @@ int xpass_launch_tma(const XpassArgs& A, cudaStream_t st, const char* slot) {
     EVX_TIMED(slot, st,
               xpass_tma_kernel<N1, N2, MODE><<<blocks, 256, smem, st>>>(tm, A.dspec, A.xpart, A.M, A.nzh, A.nz, ntiles,
                                                                       A.kx2, A.ky2, A.kz2, A.sym, A.dt, A.invN,
-                                                                      A.mult));
+                                                                      A.mult, A.nyk));
     count_launch();
     return check_launch("xpass_tma_kernel");
 }
@@ -531,7 +532,7 @@ int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, 
             attr[mode] = true;
         }
         EVX_TIMED(slot, st, (kern<<<grid, 256, smem, st>>>(spec, spec_h, nullptr, nullptr, M, nzh, nz, kx2, ky2, kz2,
-                                                           0.f, 0.f, 0.f, xb, nullptr)));
+                                                           0.f, 0.f, 0.f, xb, nullptr, 0)));
         count_launch();
         return check_launch("xpass_kernel (batched)");
     };

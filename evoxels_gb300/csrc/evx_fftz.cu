@@ -1,0 +1,261 @@
+// Real transforms along z with a y-contiguous half spectrum: the z pass of
+// the (y, z) transforms of the x-pass plans.  R2C reads the real rows
+// in[x][y][z] and writes spec[x][kz][y] (kz in [0, nz/2], unnormalised, cuFFT's
+// values); C2R reads spec[x][kz][y] and writes out[x][y][z] (the imaginary parts
+// of the kz = 0 and kz = nz/2 entries ignored, as a C2R transform does).  With
+// y contiguous, the y transform is one batched contiguous 1-D C2C (cuFFT) over
+// all (x, kz) columns, in place, and the x-pass sees pencils m = kz*ny + ky.
+//
+// A block of 256 threads owns YG = 2*(256/TZ) rows of one x plane at a time
+// (persistent blocks stride over (x, row group) items).  Two real rows a, b are
+// one complex row c = a + i b, transformed by the four-step FFT of evx_fft.cuh
+// with TZ threads per row pair (EZ values each, exchange in shared memory
+// within the warp); A(k) = (C(k) + conj C(nz-k))/2, B(k) = (C(k) - conj
+// C(nz-k))/(2i) with the partner values by warp shuffles.  The row group's
+// half spectrum is staged in shared memory as T[kz][y] (row pitch YG+1) and
+// leaves as coalesced runs of YG values along y.  C2R mirrors it: coalesced
+// runs into T, each pair gathers C(k) = A(k) + i B(k) (k <= nz/2) and
+// C(nz-k) = conj A(k) + i conj B(k), one inverse FFT gives a + i b.
+//
+// No waits of their own: __syncthreads and __syncwarp only.
+#include <algorithm>
+#include <mutex>
+
+#include "evx_ch_plan.cuh"
+#include "evx_fft.cuh"
+
+namespace evx {
+namespace {
+
+using namespace fft;
+
+__host__ __device__ constexpr int zsplit(int n) { return n == 512 ? 32 : (n >= 16 ? 16 : n); }
+
+template <int NZ>
+struct ZT {
+    static constexpr int NH = NZ / 2, NH1 = NH + 1;
+    static constexpr int EZ = zsplit(NZ), TZ = NZ / EZ, QZ = EZ / TZ;
+    static constexpr int PAIRS = 256 / TZ, YG = 2 * PAIRS;   // row pairs / rows per item
+    static constexpr int KS = TZ + 1, PS = EZ * KS;           // padded z exchange per pair
+    static constexpr int TP = YG + 1;                          // staging row pitch (complex)
+    static constexpr size_t SMEM = ((size_t)PAIRS * PS + (size_t)NH1 * TP) * sizeof(float2);
+    static_assert(EZ >= TZ && EZ % TZ == 0, "unsupported split");
+};
+
+// z exchange of one row pair: xi(k1, j) = base + k1*KS + j
+struct ZCol {
+    int base, n2, ks;
+    __device__ __forceinline__ int xi(int k1, int j) const { return base + k1 * ks + j; }
+};
+
+template <int NZ>
+__global__ void __launch_bounds__(256)
+zt_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx, int ny) {
+    using G = ZT<NZ>;
+    constexpr int EZ = G::EZ, TZ = G::TZ, QZ = G::QZ, NH = G::NH, NH1 = G::NH1, YG = G::YG, TP = G::TP;
+    extern __shared__ __align__(16) float2 sm[];
+    float2* Z = sm;                              // [PAIRS][EZ][KS]
+    float2* T = sm + G::PAIRS * G::PS;           // [NH1][TP]
+    const int tid = threadIdx.x;
+    const int t = tid % TZ, g = tid / TZ;
+    const ZCol zc{g * G::PS, t, G::KS};
+    float2 tw[EZ];                               // this thread's stage twiddles
+    fwd_twiddles<EZ, TZ>(tw, t);
+    const int groups = (ny + YG - 1) / YG;
+    const long items = (long)nx * groups;
+    for (long it = blockIdx.x; it < items; it += gridDim.x) {
+        const int x = (int)(it / groups), y0 = (int)(it - (long)x * groups) * YG;
+        const float* plane = in + (size_t)x * ny * NZ;
+        const int ya = y0 + 2 * g, yb = ya + 1;
+        const bool la = ya < ny, lb = yb < ny;
+        float2 v[EZ];
+#pragma unroll
+        for (int e = 0; e < EZ; ++e) {
+            const int z = TZ * e + t;
+            v[e] = make_float2(la ? __ldg(plane + (size_t)ya * NZ + z) : 0.f, lb ? __ldg(plane + (size_t)yb * NZ + z) : 0.f);
+        }
+        fwd_stage1_tw<EZ, TZ, true>(v, Z, zc, tw);   // a pair's TZ threads share a warp
+        fwd_stage2<EZ, TZ>(v);
+        // v[q*TZ + k2] = C(k1 + EZ*k2), k1 = t*QZ + q.  Partner C(NZ - k): for
+        // k1 != 0 it is k1' = EZ - k1, k2' = TZ-1-k2 (lane TZ-t for q = 0, TZ-1-t
+        // otherwise); for k1 = 0 (t = 0, q = 0) it is k2' = (TZ - k2) % TZ, own.
+#pragma unroll
+        for (int q = 0; q < QZ; ++q) {
+            const int k1 = t * QZ + q;
+            const int qs = q == 0 ? 0 : QZ - q;
+            const int src = q == 0 ? (TZ - t) % TZ : TZ - 1 - t;
+#pragma unroll
+            for (int k2 = 0; k2 <= TZ / 2; ++k2) {
+                const float2 pv = v[qs * TZ + (TZ - 1 - k2)];
+                float2 cp;
+                cp.x = __shfl_sync(0xffffffffu, pv.x, src, TZ);
+                cp.y = __shfl_sync(0xffffffffu, pv.y, src, TZ);
+                if (k1 == 0) cp = v[(TZ - k2) % TZ];
+                const float2 c = v[q * TZ + k2];
+                const int kz = k1 + EZ * k2;
+                if (kz > NH || (k2 == TZ / 2 && k1 != 0)) continue;
+                // A = (C + conj Cp)/2, B = (C - conj Cp)/(2i)
+                T[kz * TP + 2 * g] = make_float2(0.5f * (c.x + cp.x), 0.5f * (c.y - cp.y));
+                T[kz * TP + 2 * g + 1] = make_float2(0.5f * (c.y + cp.y), -0.5f * (c.x - cp.x));
+            }
+        }
+        __syncthreads();   // T complete
+        const int rows = min(YG, ny - y0);
+        float2* orow = out + (size_t)x * NH1 * ny + y0;
+        for (int e = tid; e < NH1 * YG; e += 256) {
+            const int kz = e / YG, yl = e - kz * YG;
+            if (yl < rows) orow[(size_t)kz * ny + yl] = T[kz * TP + yl];
+        }
+        __syncthreads();   // T and Z are rewritten by the next item
+    }
+}
+
+template <int NZ>
+__global__ void __launch_bounds__(256)
+zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, int ny) {
+    using G = ZT<NZ>;
+    constexpr int EZ = G::EZ, TZ = G::TZ, QZ = G::QZ, NH = G::NH, NH1 = G::NH1, YG = G::YG, TP = G::TP;
+    extern __shared__ __align__(16) float2 sm[];
+    float2* Z = sm;
+    float2* T = sm + G::PAIRS * G::PS;
+    const int tid = threadIdx.x;
+    const int t = tid % TZ, g = tid / TZ;
+    const ZCol zc{g * G::PS, t, G::KS};
+    float2 tw[EZ];                               // this thread's stage twiddles
+    inv_twiddles<EZ, TZ>(tw, t);
+    const int groups = (ny + YG - 1) / YG;
+    const long items = (long)nx * groups;
+    for (long it = blockIdx.x; it < items; it += gridDim.x) {
+        const int x = (int)(it / groups), y0 = (int)(it - (long)x * groups) * YG;
+        const int rows = min(YG, ny - y0);
+        const float2* irow = in + (size_t)x * NH1 * ny + y0;
+        for (int e = tid; e < NH1 * YG; e += 256) {
+            const int kz = e / YG, yl = e - kz * YG;
+            T[kz * TP + yl] = yl < rows ? __ldg(irow + (size_t)kz * ny + yl) : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        const int a = 2 * g, b = a + 1;
+        float2 v[EZ];
+#pragma unroll
+        for (int q = 0; q < QZ; ++q)
+#pragma unroll
+            for (int k2 = 0; k2 < TZ; ++k2) {
+                const int k = t * QZ + q + EZ * k2;
+                float2 c;
+                if (k == 0 || k == NH) {           // real parts only
+                    c = make_float2(T[k * TP + a].x, T[k * TP + b].x);
+                } else if (k < NH) {
+                    const float2 A = T[k * TP + a], B = T[k * TP + b];
+                    c = make_float2(A.x - B.y, A.y + B.x);
+                } else {
+                    const int kk = NZ - k;
+                    const float2 A = T[kk * TP + a], B = T[kk * TP + b];
+                    c = make_float2(A.x + B.y, B.x - A.y);
+                }
+                v[q * TZ + k2] = c;
+            }
+        inv_stage2_tw<EZ, TZ>(v, Z, zc, tw);
+        inv_stage1<EZ, TZ, true>(v, Z, zc);      // a pair's TZ threads share a warp
+        float* plane = out + (size_t)x * ny * NZ;
+        const int ya = y0 + a, yb = ya + 1;
+        if (ya < ny) {
+#pragma unroll
+            for (int e = 0; e < EZ; ++e) plane[(size_t)ya * NZ + TZ * e + t] = v[e].x;
+        }
+        if (yb < ny) {
+#pragma unroll
+            for (int e = 0; e < EZ; ++e) plane[(size_t)yb * NZ + TZ * e + t] = v[e].y;
+        }
+        __syncthreads();   // T is rewritten by the next item
+    }
+}
+
+constexpr int MAX_DEVICES = 64;
+int g_tw_rc[MAX_DEVICES];
+std::once_flag g_tw_once[MAX_DEVICES];
+
+int zt_init() {
+    int dev = 0;
+    int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= MAX_DEVICES) return fail(EVX_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::call_once(g_tw_once[dev], [dev] { g_tw_rc[dev] = check_cuda(upload_w512(), "twiddle table upload"); });
+    return g_tw_rc[dev];
+}
+
+template <class K>
+int zt_grid(K kern, size_t smem, long items, int* grid) {
+    int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "z transform shared memory attribute");
+    if (rc) return rc;
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, smem), "z transform occupancy")))
+        return rc;
+    *grid = (int)std::max<long>(1, std::min<long>(items, (long)std::max(1, sms) * std::max(1, per)));
+    return EVX_OK;
+}
+
+template <int NZ>
+int zt_launch_t(bool fwd, int nx, int ny, const void* in, void* out, cudaStream_t st) {
+    using G = ZT<NZ>;
+    const long items = (long)nx * ((ny + G::YG - 1) / G::YG);
+    int grid = 0, rc;
+    if (fwd) {
+        if ((rc = zt_grid(zt_r2c_kernel<NZ>, G::SMEM, items, &grid))) return rc;
+        EVX_TIMED("fft_z_r2c", st, zt_r2c_kernel<NZ><<<grid, 256, G::SMEM, st>>>(
+                                       static_cast<const float*>(in), static_cast<float2*>(out), nx, ny));
+    } else {
+        if ((rc = zt_grid(zt_c2r_kernel<NZ>, G::SMEM, items, &grid))) return rc;
+        EVX_TIMED("fft_z_c2r", st, zt_c2r_kernel<NZ><<<grid, 256, G::SMEM, st>>>(
+                                       static_cast<const float2*>(in), static_cast<float*>(out), nx, ny));
+    }
+    count_launch();
+    return check_launch(fwd ? "zt_r2c_kernel" : "zt_c2r_kernel");
+}
+
+int zt_launch(bool fwd, int nx, int ny, int nz, const void* in, void* out, cudaStream_t st) {
+    int rc = zt_init();
+    if (rc) return rc;
+    switch (nz) {
+        case 64: return zt_launch_t<64>(fwd, nx, ny, in, out, st);
+        case 128: return zt_launch_t<128>(fwd, nx, ny, in, out, st);
+        case 256: return zt_launch_t<256>(fwd, nx, ny, in, out, st);
+        default: return fail(EVX_ERR_UNSUPPORTED, "z transform: nz = %d", nz);
+    }
+}
+
+}  // namespace
+
+bool zt_supported(int nz) { return nz == 64 || nz == 128 || nz == 256; }
+
+int fft_zt_r2c(int nx, int ny, int nz, const float* in, float2* out, cudaStream_t st) {
+    return zt_launch(true, nx, ny, nz, in, out, st);
+}
+
+int fft_zt_c2r(int nx, int ny, int nz, const float2* in, float* out, cudaStream_t st) {
+    return zt_launch(false, nx, ny, nz, in, out, st);
+}
+
+}  // namespace evx
+
+using namespace evx;
+
+extern "C" {
+
+int evx_fft_z_r2c(const float* in, float* out, int nx, int ny, int nz, void* stream) {
+    if (!in || !out) return fail(EVX_ERR_BAD_ARG, "NULL pointer");
+    if (nx < 1 || ny < 1) return fail(EVX_ERR_BAD_SHAPE, "nx and ny must be >= 1");
+    if (reinterpret_cast<uintptr_t>(out) & 7) return fail(EVX_ERR_BAD_ARG, "out must be 8-byte aligned");
+    return fft_zt_r2c(nx, ny, nz, in, reinterpret_cast<float2*>(out), as_stream(stream));
+}
+
+int evx_fft_z_c2r(const float* in, float* out, int nx, int ny, int nz, void* stream) {
+    if (!in || !out) return fail(EVX_ERR_BAD_ARG, "NULL pointer");
+    if (nx < 1 || ny < 1) return fail(EVX_ERR_BAD_SHAPE, "nx and ny must be >= 1");
+    if (reinterpret_cast<uintptr_t>(in) & 7) return fail(EVX_ERR_BAD_ARG, "in must be 8-byte aligned");
+    return fft_zt_c2r(nx, ny, nz, reinterpret_cast<const float2*>(in), out, as_stream(stream));
+}
+
+}  // extern "C"

@@ -258,6 +258,15 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
 int evx_fft_yz_r2c(const float* in, float* spec, int nx, int ny, int nz, void* stream);
 int evx_fft_yz_c2r(const float* spec, float* out, int nx, int ny, int nz, void* stream);
 
+/* Real transforms along z of every (x, y) row with a y-contiguous half
+ * spectrum: R2C reads in[x][y][z] and writes spec[x][kz][y], kz in [0, nz/2]
+ * (cuFFT's unnormalised values); C2R reads spec[x][kz][y] (imaginary parts of
+ * kz = 0 and nz/2 ignored) and writes out[x][y][z].  nz in {64, 128, 256}, else
+ * EVX_ERR_UNSUPPORTED.  The z pass of the x-pass plans (the y transform is then
+ * one contiguous batched C2C); no reference counterpart. */
+int evx_fft_z_r2c(const float* in, float* spec, int nx, int ny, int nz, void* stream);
+int evx_fft_z_c2r(const float* spec, float* out, int nx, int ny, int nz, void* stream);
+
 /* Device-side status bits, synchronous read (reset != 0 clears them): bit 0 =
  * a bounded wait of the pipelined x-pass on its tile loads gave up (the
  * results of that call are invalid).  Returns -1 if the read itself failed. */
