@@ -40,6 +40,7 @@ struct ZT {
     static constexpr int TP = YG + 1;                          // staging row pitch (complex)
     static constexpr size_t SMEM = ((size_t)PAIRS * PS + (size_t)NH1 * TP) * sizeof(float2);
     static_assert(EZ >= TZ && EZ % TZ == 0, "unsupported split");
+    static_assert((size_t)PAIRS * PS * 2 >= (size_t)YG * NZ, "the exchange area stages the item's rows");
 };
 
 // z exchange of one row pair: xi(k1, j) = base + k1*KS + j
@@ -63,17 +64,26 @@ zt_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx, in
     fwd_twiddles<EZ, TZ>(tw, t);
     const int groups = (ny + YG - 1) / YG;
     const long items = (long)nx * groups;
-    for (long it = blockIdx.x; it < items; it += gridDim.x) {
+    // the item's two rows, loaded one item ahead (in flight during the previous item's transform)
+    auto load_rows = [&](long it, float2 (&w)[EZ]) {
         const int x = (int)(it / groups), y0 = (int)(it - (long)x * groups) * YG;
         const float* plane = in + (size_t)x * ny * NZ;
         const int ya = y0 + 2 * g, yb = ya + 1;
         const bool la = ya < ny, lb = yb < ny;
-        float2 v[EZ];
 #pragma unroll
         for (int e = 0; e < EZ; ++e) {
             const int z = TZ * e + t;
-            v[e] = make_float2(la ? __ldg(plane + (size_t)ya * NZ + z) : 0.f, lb ? __ldg(plane + (size_t)yb * NZ + z) : 0.f);
+            w[e] = make_float2(la ? __ldg(plane + (size_t)ya * NZ + z) : 0.f, lb ? __ldg(plane + (size_t)yb * NZ + z) : 0.f);
         }
+    };
+    float2 vn[EZ];
+    if (blockIdx.x < items) load_rows(blockIdx.x, vn);
+    for (long it = blockIdx.x; it < items; it += gridDim.x) {
+        const int x = (int)(it / groups), y0 = (int)(it - (long)x * groups) * YG;
+        float2 v[EZ];
+#pragma unroll
+        for (int e = 0; e < EZ; ++e) v[e] = vn[e];
+        if (it + gridDim.x < items) load_rows(it + gridDim.x, vn);
         fwd_stage1_tw<EZ, TZ, true>(v, Z, zc, tw);   // a pair's TZ threads share a warp
         fwd_stage2<EZ, TZ>(v);
         // v[q*TZ + k2] = C(k1 + EZ*k2), k1 = t*QZ + q.  Partner C(NZ - k): for
@@ -156,17 +166,20 @@ zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, in
             }
         inv_stage2_tw<EZ, TZ>(v, Z, zc, tw);
         inv_stage1<EZ, TZ, true>(v, Z, zc);      // a pair's TZ threads share a warp
-        float* plane = out + (size_t)x * ny * NZ;
-        const int ya = y0 + a, yb = ya + 1;
-        if (ya < ny) {
+        // the item's rows are contiguous in out: stage them in shared memory (the
+        // exchange area, YG*NZ floats) and leave as full float4 runs
+        __syncthreads();                         // every pair is done with its exchange block
+        float* R = reinterpret_cast<float*>(Z);
 #pragma unroll
-            for (int e = 0; e < EZ; ++e) plane[(size_t)ya * NZ + TZ * e + t] = v[e].x;
+        for (int e = 0; e < EZ; ++e) {
+            R[a * NZ + TZ * e + t] = v[e].x;
+            R[b * NZ + TZ * e + t] = v[e].y;
         }
-        if (yb < ny) {
-#pragma unroll
-            for (int e = 0; e < EZ; ++e) plane[(size_t)yb * NZ + TZ * e + t] = v[e].y;
-        }
-        __syncthreads();   // T is rewritten by the next item
+        __syncthreads();
+        float4* orow4 = reinterpret_cast<float4*>(out + ((size_t)x * ny + y0) * NZ);
+        const float4* R4 = reinterpret_cast<const float4*>(R);
+        for (int e = tid; e < rows * (NZ / 4); e += 256) orow4[e] = R4[e];
+        __syncthreads();   // T and the staging area are rewritten by the next item
     }
 }
 
@@ -255,6 +268,7 @@ int evx_fft_z_c2r(const float* in, float* out, int nx, int ny, int nz, void* str
     if (!in || !out) return fail(EVX_ERR_BAD_ARG, "NULL pointer");
     if (nx < 1 || ny < 1) return fail(EVX_ERR_BAD_SHAPE, "nx and ny must be >= 1");
     if (reinterpret_cast<uintptr_t>(in) & 7) return fail(EVX_ERR_BAD_ARG, "in must be 8-byte aligned");
+    if (reinterpret_cast<uintptr_t>(out) & 15) return fail(EVX_ERR_BAD_ARG, "out must be 16-byte aligned");
     return fft_zt_c2r(nx, ny, nz, reinterpret_cast<const float2*>(in), out, as_stream(stream));
 }
 
