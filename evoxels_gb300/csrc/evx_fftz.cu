@@ -40,7 +40,6 @@ struct ZT {
     static constexpr int TP = YG + 1;                          // staging row pitch (complex)
     static constexpr size_t SMEM = ((size_t)PAIRS * PS + (size_t)NH1 * TP) * sizeof(float2);
     static_assert(EZ >= TZ && EZ % TZ == 0, "unsupported split");
-    static_assert((size_t)PAIRS * PS * 2 >= (size_t)YG * NZ, "the exchange area stages the item's rows");
 };
 
 // z exchange of one row pair: xi(k1, j) = base + k1*KS + j
@@ -139,9 +138,18 @@ zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, in
         const int x = (int)(it / groups), y0 = (int)(it - (long)x * groups) * YG;
         const int rows = min(YG, ny - y0);
         const float2* irow = in + (size_t)x * NH1 * ny + y0;
-        for (int e = tid; e < NH1 * YG; e += 256) {
-            const int kz = e / YG, yl = e - kz * YG;
-            T[kz * TP + yl] = yl < rows ? __ldg(irow + (size_t)kz * ny + yl) : make_float2(0.f, 0.f);
+        // all of the thread's loads in flight at once, then into T
+        constexpr int PER = (NH1 * YG + 255) / 256;
+        float2 w[PER];
+#pragma unroll
+        for (int p = 0; p < PER; ++p) {
+            const int e = tid + 256 * p, kz = e / YG, yl = e - kz * YG;
+            w[p] = (e < NH1 * YG && yl < rows) ? __ldg(irow + (size_t)kz * ny + yl) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int p = 0; p < PER; ++p) {
+            const int e = tid + 256 * p;
+            if (e < NH1 * YG) T[(e / YG) * TP + e % YG] = w[p];
         }
         __syncthreads();
         const int a = 2 * g, b = a + 1;
@@ -166,20 +174,17 @@ zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, in
             }
         inv_stage2_tw<EZ, TZ>(v, Z, zc, tw);
         inv_stage1<EZ, TZ, true>(v, Z, zc);      // a pair's TZ threads share a warp
-        // the item's rows are contiguous in out: stage them in shared memory (the
-        // exchange area, YG*NZ floats) and leave as full float4 runs
-        __syncthreads();                         // every pair is done with its exchange block
-        float* R = reinterpret_cast<float*>(Z);
+        float* plane = out + (size_t)x * ny * NZ;
+        const int ya = y0 + a, yb = ya + 1;
+        if (ya < ny) {
 #pragma unroll
-        for (int e = 0; e < EZ; ++e) {
-            R[a * NZ + TZ * e + t] = v[e].x;
-            R[b * NZ + TZ * e + t] = v[e].y;
+            for (int e = 0; e < EZ; ++e) plane[(size_t)ya * NZ + TZ * e + t] = v[e].x;
         }
-        __syncthreads();
-        float4* orow4 = reinterpret_cast<float4*>(out + ((size_t)x * ny + y0) * NZ);
-        const float4* R4 = reinterpret_cast<const float4*>(R);
-        for (int e = tid; e < rows * (NZ / 4); e += 256) orow4[e] = R4[e];
-        __syncthreads();   // T and the staging area are rewritten by the next item
+        if (yb < ny) {
+#pragma unroll
+            for (int e = 0; e < EZ; ++e) plane[(size_t)yb * NZ + TZ * e + t] = v[e].y;
+        }
+        __syncthreads();   // T is rewritten by the next item
     }
 }
 
@@ -268,7 +273,6 @@ int evx_fft_z_c2r(const float* in, float* out, int nx, int ny, int nz, void* str
     if (!in || !out) return fail(EVX_ERR_BAD_ARG, "NULL pointer");
     if (nx < 1 || ny < 1) return fail(EVX_ERR_BAD_SHAPE, "nx and ny must be >= 1");
     if (reinterpret_cast<uintptr_t>(in) & 7) return fail(EVX_ERR_BAD_ARG, "in must be 8-byte aligned");
-    if (reinterpret_cast<uintptr_t>(out) & 15) return fail(EVX_ERR_BAD_ARG, "out must be 16-byte aligned");
     return fft_zt_c2r(nx, ny, nz, reinterpret_cast<const float2*>(in), out, as_stream(stream));
 }
 
