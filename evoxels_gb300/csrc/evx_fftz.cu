@@ -37,7 +37,7 @@ struct ZT {
     static constexpr int EZ = zsplit(NZ), TZ = NZ / EZ, QZ = EZ / TZ;
     static constexpr int PAIRS = 256 / TZ, YG = 2 * PAIRS;   // row pairs / rows per item
     static constexpr int KS = TZ + 1, PS = EZ * KS;           // padded z exchange per pair
-    static constexpr int TP = YG + 1;                          // staging row pitch (complex)
+    static constexpr int TP = YG + 2;   // staging row pitch (complex): rows a, b of a pair are one 16-byte word
     static constexpr size_t SMEM = ((size_t)PAIRS * PS + (size_t)NH1 * TP) * sizeof(float2);
     static_assert(EZ >= TZ && EZ % TZ == 0, "unsupported split");
 };
@@ -103,9 +103,9 @@ zt_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx, in
                 const float2 c = v[q * TZ + k2];
                 const int kz = k1 + EZ * k2;
                 if (kz > NH || (k2 == TZ / 2 && k1 != 0)) continue;
-                // A = (C + conj Cp)/2, B = (C - conj Cp)/(2i)
-                T[kz * TP + 2 * g] = make_float2(0.5f * (c.x + cp.x), 0.5f * (c.y - cp.y));
-                T[kz * TP + 2 * g + 1] = make_float2(0.5f * (c.y + cp.y), -0.5f * (c.x - cp.x));
+                // A = (C + conj Cp)/2, B = (C - conj Cp)/(2i): rows a, b of the pair in one store
+                *reinterpret_cast<float4*>(T + kz * TP + 2 * g) =
+                    make_float4(0.5f * (c.x + cp.x), 0.5f * (c.y - cp.y), 0.5f * (c.y + cp.y), -0.5f * (c.x - cp.x));
             }
         }
         __syncthreads();   // T complete
@@ -159,17 +159,12 @@ zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, in
 #pragma unroll
             for (int k2 = 0; k2 < TZ; ++k2) {
                 const int k = t * QZ + q + EZ * k2;
+                const int kk = k <= NH ? k : NZ - k;
+                const float4 AB = *reinterpret_cast<const float4*>(T + kk * TP + a);   // (A, B) of the pair
                 float2 c;
-                if (k == 0 || k == NH) {           // real parts only
-                    c = make_float2(T[k * TP + a].x, T[k * TP + b].x);
-                } else if (k < NH) {
-                    const float2 A = T[k * TP + a], B = T[k * TP + b];
-                    c = make_float2(A.x - B.y, A.y + B.x);
-                } else {
-                    const int kk = NZ - k;
-                    const float2 A = T[kk * TP + a], B = T[kk * TP + b];
-                    c = make_float2(A.x + B.y, B.x - A.y);
-                }
+                if (k == 0 || k == NH) c = make_float2(AB.x, AB.z);                    // real parts only
+                else if (k < NH) c = make_float2(AB.x - AB.w, AB.y + AB.z);            // A + iB
+                else c = make_float2(AB.x + AB.w, AB.z - AB.y);                        // conj A + i conj B
                 v[q * TZ + k2] = c;
             }
         inv_stage2_tw<EZ, TZ>(v, Z, zc, tw);
