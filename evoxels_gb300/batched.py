@@ -51,7 +51,7 @@ class BatchedCahnHilliard:
     """
 
     def __init__(self, shapes, D=1.0, eps=3.0, dt=0.1, A=0.25, mu_hom=None, spacing=None,
-                 tuning: BatchTuning | None = None, device="cuda", cufft3d=False):
+                 tuning: BatchTuning | None = None, device="cuda", cufft3d=False, cufft_yz=False, z_pass=False):
         self.device = _require_cuda(device)
         self.shapes = [tuple(int(x) for x in s) for s in shapes]
         n = len(self.shapes)
@@ -78,7 +78,8 @@ class BatchedCahnHilliard:
         with torch.cuda.device(self.device):
             # flags bit 1: cuFFT 3-D for every shape group (default: power-of-two nx groups
             # use cuFFT (y, z) plus the batched x-pass)
-            _lib.check(L.evx_batch_create(C.byref(h), inst, n, self.tuning.to_c(), 2 if cufft3d else 0),
+            flags = (2 if cufft3d else 0) | (8 if cufft_yz else 0) | (16 if z_pass else 0)
+            _lib.check(L.evx_batch_create(C.byref(h), inst, n, self.tuning.to_c(), flags),
                        "evx_batch_create")
         self.handle = h
         self.total = int(L.evx_batch_field_floats(h))

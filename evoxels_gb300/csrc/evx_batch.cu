@@ -142,6 +142,7 @@ struct evx_batch {
         size_t n = 0, nspec = 0;       // per instance
         int first = 0, count = 0;      // internal instance range
         bool xmode = false;            // cuFFT (y, z) plans + batched x-pass
+        bool zt = false;               // xmode with the library's z pass: spectrum [x][kz][y], plans' r2c = C2C along y
         int k2x = 0, k2y = 0, k2z = 0; // offsets of the group's k^2 tables
         std::vector<Plan> plans;
     };
@@ -205,6 +206,14 @@ int batch_r2c(evx_batch* b, const float* in, float2* out, cudaStream_t st) {
             const long long fo = g.off + (long long)(p.first - g.first) * (long long)g.n;
             const long long so = g.soff + (long long)(p.first - g.first) * (long long)g.nspec;
             cufftResult r;
+            if (g.zt) {   // z pass, then the contiguous y transform in place
+                int rc = fft_zt_r2c(p.count * g.nx, g.ny, g.nz, in + fo, out + so, st);
+                if (rc) return rc;
+                cufftComplex* sp = reinterpret_cast<cufftComplex*>(out + so);
+                EVX_TIMED("batch_cufft_c2c_y", st, r = cufftExecC2C(p.r2c, sp, sp, CUFFT_FORWARD));
+                if ((rc = check_cufft(r, "cufftExecC2C (y) (batch)"))) return rc;
+                continue;
+            }
             EVX_TIMED("batch_cufft_r2c", st,
                       r = cufftExecR2C(p.r2c, const_cast<cufftReal*>(in + fo), reinterpret_cast<cufftComplex*>(out + so)));
             int rc = check_cufft(r, "cufftExecR2C (batch)");
@@ -219,6 +228,14 @@ int batch_c2r(evx_batch* b, float2* in, float* out, cudaStream_t st) {
             const long long fo = g.off + (long long)(p.first - g.first) * (long long)g.n;
             const long long so = g.soff + (long long)(p.first - g.first) * (long long)g.nspec;
             cufftResult r;
+            if (g.zt) {   // inverse y transform in place (the input is consumed), then z
+                cufftComplex* sp = reinterpret_cast<cufftComplex*>(in + so);
+                EVX_TIMED("batch_cufft_c2c_y", st, r = cufftExecC2C(p.r2c, sp, sp, CUFFT_INVERSE));
+                int rc = check_cufft(r, "cufftExecC2C (y) (batch)");
+                if (!rc) rc = fft_zt_c2r(p.count * g.nx, g.ny, g.nz, in + so, out + fo, st);
+                if (rc) return rc;
+                continue;
+            }
             EVX_TIMED("batch_cufft_c2r", st,
                       r = cufftExecC2R(p.c2r, reinterpret_cast<cufftComplex*>(in + so), out + fo));
             int rc = check_cufft(r, "cufftExecC2R (batch)");
@@ -232,7 +249,7 @@ int batch_xpass(evx_batch* b, int mode, float2* spec, float2* spec_h, cudaStream
     for (auto& g : b->groups) {
         if (!g.xmode) continue;
         int rc = xpass_batch_launch(mode, g.nx, spec, spec_h, b->d_xb + g.first, g.count, g.ny * g.nzh, g.nzh, g.nz,
-                                    b->d_k2 + g.k2x, b->d_k2 + g.k2y, b->d_k2 + g.k2z, st);
+                                    b->d_k2 + g.k2x, b->d_k2 + g.k2y, b->d_k2 + g.k2z, st, g.zt ? g.ny : 0);
         if (rc) return rc;
     }
     return EVX_OK;
@@ -372,6 +389,8 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
         // flags bit 1: cuFFT's 3-D transforms for every group (as evx_ch_plan_create)
         g.xmode = xpass_supported(g.nx) && !(flags & 2) && (size_t)g.count * g.nx <= 2147483647ull;
         if (!g.xmode) b->any_kspace = true;
+        // the z pass as in evx_ch_plan_create_bc: nz = 256 by default, flags bit 4 always, bit 3 never
+        g.zt = g.xmode && zt_supported(g.nz) && !(flags & 8) && ((flags & 16) || g.nz == 256);
         const int gm = b->tune.fft_group_max > 0 ? b->tune.fft_group_max : g.count;
         for (int f = 0; f < g.count; f += gm) {
             evx_batch::Plan p;
@@ -384,7 +403,12 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
             cufftSetAutoAllocation(p.r2c, 0);
             cufftSetAutoAllocation(p.c2r, 0);
             g.plans.push_back(p);
-            if (g.xmode) {   // 2-D (y, z) over every x plane of the plan's instances
+            if (g.zt) {      // 1-D C2C along the contiguous y of every (x, kz) column, both directions
+                int ny1[1] = {g.ny};
+                if ((rc = check_cufft(cufftMakePlanMany(p.r2c, 1, ny1, nullptr, 1, g.ny, nullptr, 1, g.ny, CUFFT_C2C,
+                                                        p.count * g.nx * g.nzh, &w1), "cufftMakePlanMany C2C (y) (batch)")))
+                    return cleanup(rc);
+            } else if (g.xmode) {   // 2-D (y, z) over every x plane of the plan's instances
                 int d2[2] = {g.ny, g.nz};
                 const int pr = g.ny * g.nz, ps = g.ny * g.nzh;
                 if ((rc = check_cufft(cufftMakePlanMany(p.r2c, 2, d2, nullptr, 1, pr, nullptr, 1, ps, CUFFT_R2C,

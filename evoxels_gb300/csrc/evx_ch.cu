@@ -441,8 +441,9 @@ int evx_ch_plan_create_bc(evx_ch_plan** out, const evx_grid* g, const evx_bc* bc
     // power-of-two nx: cuFFT transforms (y, z) for every x plane and the fused x-pass does the rest
     p->xmode = xmode;
     p->yzmode = p->xmode && yz_supported(g->ny, g->nz) && (flags & 4);
-    // z pass of our own with a y-contiguous spectrum unless flags bit 3 keeps cuFFT's 2-D plans
-    p->ztmode = p->xmode && !p->yzmode && zt_supported(g->nz) && !(flags & 8);
+    // z pass of our own with a y-contiguous spectrum: by default for nz = 256 (faster than cuFFT's
+    // 2-D plans there; not below), flags bit 4 for every supported nz, flags bit 3 never
+    p->ztmode = p->xmode && !p->yzmode && zt_supported(g->nz) && !(flags & 8) && ((flags & 16) || g->nz == 256);
     size_t w4 = 0, w5 = 0;
     if (p->ztmode) {
         int ny1[1] = {g->ny};

@@ -92,7 +92,8 @@ struct XBatchInst {
 bool xpass_supported(int nx);
 // mode 0 forward, 1 adjoint g, 2 adjoint g and h (spec_h, same offsets); per-tile kernel
 int xpass_batch_launch(int mode, int nx, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M,
-                       int nzh, int nz, const float* kx2, const float* ky2, const float* kz2, cudaStream_t st);
+                       int nzh, int nz, const float* kx2, const float* ky2, const float* kz2, cudaStream_t st,
+                       int nyk = 0);
 size_t xpass_blocks(int nx, int M);
 size_t xpass_spectrum_floats(int nx, int M);
 int xpass_launch(const XpassArgs& a, cudaStream_t st);

@@ -519,7 +519,7 @@ size_t xpass_spectrum_floats(int nx, int M) {
 
 template <int N1, int N2>
 int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M, int nzh, int nz,
-                  const float* kx2, const float* ky2, const float* kz2, cudaStream_t st) {
+                  const float* kx2, const float* ky2, const float* kz2, cudaStream_t st, int nyk) {
     constexpr int P = 256 / N2;
     const size_t smem = (size_t)N1 * N2 * P * sizeof(float2);
     const dim3 grid((M + P - 1) / P, count);
@@ -532,7 +532,7 @@ int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, 
             attr[mode] = true;
         }
         EVX_TIMED(slot, st, (kern<<<grid, 256, smem, st>>>(spec, spec_h, nullptr, nullptr, M, nzh, nz, kx2, ky2, kz2,
-                                                           0.f, 0.f, 0.f, xb, nullptr, 0)));
+                                                           0.f, 0.f, 0.f, xb, nullptr, nyk)));
         count_launch();
         return check_launch("xpass_kernel (batched)");
     };
@@ -544,20 +544,21 @@ int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, 
 }
 
 int xpass_batch_launch(int mode, int nx, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M,
-                       int nzh, int nz, const float* kx2, const float* ky2, const float* kz2, cudaStream_t st) {
+                       int nzh, int nz, const float* kx2, const float* ky2, const float* kz2, cudaStream_t st,
+                       int nyk) {
     int rc = xpass_init();
     if (rc) return rc;
     if (count < 1 || count > 65535) return fail(EVX_ERR_BAD_ARG, "batched x-pass: %d instances", count);
     if (mode < 0 || mode > 2) return fail(EVX_ERR_BAD_ARG, "batched x-pass mode %d", mode);
     if (mode == 2 && !spec_h) return fail(EVX_ERR_BAD_ARG, "x-pass mode 2 is missing a buffer");
     switch (nx) {
-        case 8: return xpass_batch_t<8, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
-        case 16: return xpass_batch_t<16, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
-        case 32: return xpass_batch_t<16, 2>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
-        case 64: return xpass_batch_t<16, 4>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
-        case 128: return xpass_batch_t<16, 8>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
-        case 256: return xpass_batch_t<16, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
-        case 512: return xpass_batch_t<32, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st);
+        case 8: return xpass_batch_t<8, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
+        case 16: return xpass_batch_t<16, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
+        case 32: return xpass_batch_t<16, 2>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
+        case 64: return xpass_batch_t<16, 4>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
+        case 128: return xpass_batch_t<16, 8>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
+        case 256: return xpass_batch_t<16, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
+        case 512: return xpass_batch_t<32, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
         default: return fail(EVX_ERR_UNSUPPORTED, "x-pass needs a power-of-two nx in [8, 512]");
     }
 }

@@ -232,6 +232,7 @@ int zt_launch(bool fwd, int nx, int ny, int nz, const void* in, void* out, cudaS
     int rc = zt_init();
     if (rc) return rc;
     switch (nz) {
+        case 32: return zt_launch_t<32>(fwd, nx, ny, in, out, st);
         case 64: return zt_launch_t<64>(fwd, nx, ny, in, out, st);
         case 128: return zt_launch_t<128>(fwd, nx, ny, in, out, st);
         case 256: return zt_launch_t<256>(fwd, nx, ny, in, out, st);
@@ -241,7 +242,7 @@ int zt_launch(bool fwd, int nx, int ny, int nz, const void* in, void* out, cudaS
 
 }  // namespace
 
-bool zt_supported(int nz) { return nz == 64 || nz == 128 || nz == 256; }
+bool zt_supported(int nz) { return nz == 32 || nz == 64 || nz == 128 || nz == 256; }
 
 int fft_zt_r2c(int nx, int ny, int nz, const float* in, float2* out, cudaStream_t st) {
     return zt_launch(true, nx, ny, nz, in, out, st);

@@ -28,12 +28,13 @@ from .voxelgrid import cuda_stream, evx_bc
 class ChPlan:
     """An ``evx_ch_plan`` plus its device workspace (one per grid shape/spacing/device)."""
 
-    def __init__(self, vg, grads=False, cufft3d=False, fused_yz=False, bc=None, cufft_yz=False):
+    def __init__(self, vg, grads=False, cufft3d=False, fused_yz=False, bc=None, cufft_yz=False, z_pass=False):
         self.vg = vg
         self.grid = vg.evx_grid()
         self.grads = grads
         h = C.c_void_p()
-        flags = (1 if grads else 0) | (2 if cufft3d else 0) | (4 if fused_yz else 0) | (8 if cufft_yz else 0)
+        flags = (1 if grads else 0) | (2 if cufft3d else 0) | (4 if fused_yz else 0) | (8 if cufft_yz else 0) | \
+            (16 if z_pass else 0)
         with torch.cuda.device(vg.device):
             if bc is None:
                 _lib.check(_lib.lib().evx_ch_plan_create(C.byref(h), self.grid, flags), "evx_ch_plan_create")
@@ -58,21 +59,23 @@ _plan_lock = threading.Lock()
 _plans = {}
 
 
-def get_plan(vg, grads=False, cufft3d=False, fused_yz=False, bc=None, cufft_yz=False):
+def get_plan(vg, grads=False, cufft3d=False, fused_yz=False, bc=None, cufft_yz=False, z_pass=False):
     """Cached plan per grid; ``cufft3d`` forces cuFFT's 3-D transforms instead of the
     (y, z) transforms plus the fused x-pass used for power-of-two ``Nx``; ``fused_yz``
-    replaces cuFFT's (y, z) transforms by the fused cluster kernels (opt-in); by
-    default the z pass is the library's own (y-contiguous spectrum, nz in 64/128/256)
-    and ``cufft_yz`` keeps cuFFT's 2-D (y, z) plans instead; ``bc`` (normalised BC
-    tuple) selects the mirrored-x step for a non-periodic x axis."""
+    replaces cuFFT's (y, z) transforms by the fused cluster kernels (opt-in); for
+    nz = 256 the z pass is the library's own by default (y-contiguous spectrum),
+    ``z_pass`` uses it for nz in 32/64/128 too, ``cufft_yz`` keeps cuFFT's 2-D (y, z)
+    plans for every nz; ``bc`` (normalised BC tuple) selects the mirrored-x step for
+    a non-periodic x axis."""
     if bc is not None and all(kind == "periodic" for kind, _ in bc):
         bc = None
     bkey = None if bc is None else tuple((k, tuple(float(x) for x in v) if v is not None else None) for k, v in bc)
-    key = (vg.shape, vg.spacing, str(vg.device), bool(grads), bool(cufft3d), bool(fused_yz), bkey, bool(cufft_yz))
+    key = (vg.shape, vg.spacing, str(vg.device), bool(grads), bool(cufft3d), bool(fused_yz), bkey, bool(cufft_yz),
+           bool(z_pass))
     with _plan_lock:
         p = _plans.get(key)
         if p is None:
-            p = ChPlan(vg, grads, cufft3d, fused_yz, bc, cufft_yz)
+            p = ChPlan(vg, grads, cufft3d, fused_yz, bc, cufft_yz, z_pass)
             _plans[key] = p
         return p
 

@@ -188,7 +188,13 @@ int evx_ch_plan_create_bc(evx_ch_plan** plan, const evx_grid* g, const evx_bc* b
 /* flags bit 2: with the x-pass and ny, nz in {64, 128, 256}, use the fused
  * (y, z) kernels (evx_fft_yz_r2c/c2r) instead of cuFFT's (y, z) plans.  Off by
  * default: on GB300 at 256^3 they take 73/68 us per transform against cuFFT's
- * 65/62 us (latency-bound; one HBM pass instead of two does not pay yet). */
+ * 65/62 us (latency-bound; one HBM pass instead of two does not pay yet).
+ * By default an x-pass plan with nz = 256 keeps the half spectrum y-contiguous,
+ * (nx, nz/2+1, ny): the z pass is evx_fft_z_r2c/c2r and the y transform one
+ * contiguous batched cuFFT C2C (56/61 us per transform at 256^3 against
+ * 64/61 us; for nz = 32, 64 it is slower than cuFFT's plans, for 128 even).
+ * flags bit 4: the same for nz in {32, 64, 128}; bit 3: cuFFT's 2-D (y, z)
+ * plans for every nz.  The same bits apply to evx_batch_create. */
 int evx_ch_plan_destroy(evx_ch_plan* plan);
 
 /* Bytes of device workspace (256-byte aligned start) the plan's calls need. */
@@ -261,7 +267,7 @@ int evx_fft_yz_c2r(const float* spec, float* out, int nx, int ny, int nz, void* 
 /* Real transforms along z of every (x, y) row with a y-contiguous half
  * spectrum: R2C reads in[x][y][z] and writes spec[x][kz][y], kz in [0, nz/2]
  * (cuFFT's unnormalised values); C2R reads spec[x][kz][y] (imaginary parts of
- * kz = 0 and nz/2 ignored) and writes out[x][y][z].  nz in {64, 128, 256}, else
+ * kz = 0 and nz/2 ignored) and writes out[x][y][z].  nz in {32, 64, 128, 256}, else
  * EVX_ERR_UNSUPPORTED.  The z pass of the x-pass plans (the y transform is then
  * one contiguous batched C2C); no reference counterpart. */
 int evx_fft_z_r2c(const float* in, float* spec, int nx, int ny, int nz, void* stream);

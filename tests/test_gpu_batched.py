@@ -127,13 +127,16 @@ def test_autotuner_returns_a_valid_tuning(cuda_lib, tmp_path, monkeypatch):
     assert (tmp_path / "cache.json").exists()
 
 
-def test_batched_xpass_groups_match_cufft3d(cuda_lib):
-    """Power-of-two groups (cuFFT (y, z) + batched x-pass) against cuFFT 3-D for every group."""
+@pytest.mark.parametrize("variant", ["cufft3d", "cufft_yz"])
+def test_batched_xpass_groups_match_cufft3d(cuda_lib, variant):
+    """Power-of-two groups (batched x-pass; with the library's z pass in the second case)
+    against cuFFT 3-D or cuFFT's 2-D (y, z) plans for every group."""
     from evoxels_gb300.batched import BatchedCahnHilliard
     f = fields(7)
     res = []
-    for cufft3d in (False, True):
-        b = BatchedCahnHilliard(SHAPES, D, EPS, 0.1, cufft3d=cufft3d)
+    for other in (False, True):
+        kw = {variant: other} if variant == "cufft3d" else ({"cufft_yz": True} if other else {"z_pass": True})
+        b = BatchedCahnHilliard(SHAPES, D, EPS, 0.1, **kw)
         n = 4
         states = torch.empty((n + 1) * b.total, dtype=torch.float32, device="cuda")
         states[:b.total].copy_(b.pack(f))

@@ -23,7 +23,8 @@ def gpu(a):
     return torch.tensor(np.asarray(a), dtype=torch.float32, device=DEV).reshape((1,) + np.asarray(a).shape[-3:])
 
 
-@pytest.mark.parametrize("shape", [(3, 32, 256), (2, 96, 256), (4, 70, 128), (2, 33, 64), (1, 7, 256), (2, 1, 64)])
+@pytest.mark.parametrize("shape", [(3, 32, 256), (2, 96, 256), (4, 70, 128), (2, 33, 64), (1, 7, 256), (2, 1, 64),
+                                   (3, 40, 32), (2, 300, 32)])
 def test_z_transforms_vs_torch(cuda_lib, shape):
     from evoxels_gb300 import _lib
     from evoxels_gb300.voxelgrid import cuda_stream
@@ -50,7 +51,7 @@ def test_z_transforms_vs_torch(cuda_lib, shape):
         _lib.check(cuda_lib.evx_fft_z_r2c(u.data_ptr(), spec.data_ptr(), nx, ny, 96, cuda_stream()), "r2c")
 
 
-SHAPES = [(32, 64, 64), (64, 40, 128), (16, 48, 256), (128, 8, 64), (8, 20, 128)]
+SHAPES = [(32, 64, 64), (64, 40, 128), (16, 48, 256), (128, 8, 64), (8, 20, 128), (32, 24, 32)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -65,7 +66,7 @@ def test_forward_matches_cufft_yz_plan(cuda_lib, shape):
     for cufft_yz in (False, True):
         for bc in (None, ("neumann", "periodic", "periodic"), (("dirichlet", (0.2, 0.9)), "periodic", "periodic")):
             prob = CahnHilliard(vg, eps=1.8, D=1.1, bc=bc if bc else ("periodic",) * 3)
-            plan = get_plan(vg, bc=prob.bc, cufft_yz=cufft_yz)
+            plan = get_plan(vg, bc=prob.bc, cufft_yz=cufft_yz, z_pass=not cufft_yz)
             out = torch.empty_like(u0)
             _lib.check(cuda_lib.evx_ch_forward(plan.handle, u0.data_ptr(), out.data_ptr(), 4, None,
                                                prob.evx_params(0.1), None, plan.workspace.data_ptr(), cuda_stream()),
@@ -93,7 +94,7 @@ def test_adjoint_matches_cufft_yz_plan(cuda_lib, shape, spectral):
     lam = gpu(oracle.seeded_unit_field(shape, 9) - 0.5)
     res = []
     for cufft_yz in (False, True):
-        plan = get_plan(vg, grads=True, cufft_yz=cufft_yz)
+        plan = get_plan(vg, grads=True, cufft_yz=cufft_yz, z_pass=not cufft_yz)
         nf = int(L.evx_ch_spectrum_floats(plan.handle))
         traj = torch.empty((n + 1,) + shape, dtype=torch.float32, device=DEV)
         traj[0] = u0[0]
@@ -129,7 +130,7 @@ def test_etd1_matches_cufft_yz_plan(cuda_lib):
         r = prob.rhs(0.0, u0)
         outs = []
         for cufft_yz in (False, True):
-            plan = get_plan(vg, bc=prob.bc, cufft_yz=cufft_yz)
+            plan = get_plan(vg, bc=prob.bc, cufft_yz=cufft_yz, z_pass=not cufft_yz)
             out = torch.empty_like(u0)
             _lib.check(cuda_lib.evx_spectral_update(plan.handle, u0.data_ptr(), r.data_ptr(), st._mult.data_ptr(),
                                                     out.data_ptr(), plan.workspace.data_ptr(), cuda_stream()), "etd1")
