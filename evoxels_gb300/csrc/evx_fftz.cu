@@ -50,7 +50,7 @@ struct ZCol {
 
 template <int NZ>
 __global__ void __launch_bounds__(256)
-zt_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx, int ny) {
+zt_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx, int ny, bool vec) {
     using G = ZT<NZ>;
     constexpr int EZ = G::EZ, TZ = G::TZ, QZ = G::QZ, NH = G::NH, NH1 = G::NH1, YG = G::YG, TP = G::TP;
     extern __shared__ __align__(16) float2 sm[];
@@ -111,9 +111,17 @@ zt_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx, in
         __syncthreads();   // T complete
         const int rows = min(YG, ny - y0);
         float2* orow = out + (size_t)x * NH1 * ny + y0;
-        for (int e = tid; e < NH1 * YG; e += 256) {
-            const int kz = e / YG, yl = e - kz * YG;
-            if (yl < rows) orow[(size_t)kz * ny + yl] = T[kz * TP + yl];
+        // two y values per thread and store (vec: even ny, 16-byte aligned output)
+        for (int e = tid; e < NH1 * (YG / 2); e += 256) {
+            const int kz = e / (YG / 2), yl = 2 * (e - kz * (YG / 2));
+            const float4 w = *reinterpret_cast<const float4*>(T + kz * TP + yl);
+            float2* o = orow + (size_t)kz * ny + yl;
+            if (vec && yl + 1 < rows) {
+                *reinterpret_cast<float4*>(o) = w;
+            } else {
+                if (yl < rows) o[0] = make_float2(w.x, w.y);
+                if (yl + 1 < rows) o[1] = make_float2(w.z, w.w);
+            }
         }
         __syncthreads();   // T and Z are rewritten by the next item
     }
@@ -121,7 +129,7 @@ zt_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx, in
 
 template <int NZ>
 __global__ void __launch_bounds__(256)
-zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, int ny) {
+zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, int ny, bool vec) {
     using G = ZT<NZ>;
     constexpr int EZ = G::EZ, TZ = G::TZ, QZ = G::QZ, NH = G::NH, NH1 = G::NH1, YG = G::YG, TP = G::TP;
     extern __shared__ __align__(16) float2 sm[];
@@ -138,18 +146,29 @@ zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, in
         const int x = (int)(it / groups), y0 = (int)(it - (long)x * groups) * YG;
         const int rows = min(YG, ny - y0);
         const float2* irow = in + (size_t)x * NH1 * ny + y0;
-        // all of the thread's loads in flight at once, then into T
-        constexpr int PER = (NH1 * YG + 255) / 256;
-        float2 w[PER];
+        // all of the thread's loads in flight at once (two y values each; vec: even ny,
+        // 16-byte aligned input), then into T
+        constexpr int HY = YG / 2, PER = (NH1 * HY + 255) / 256;
+        float4 w[PER];
 #pragma unroll
         for (int p = 0; p < PER; ++p) {
-            const int e = tid + 256 * p, kz = e / YG, yl = e - kz * YG;
-            w[p] = (e < NH1 * YG && yl < rows) ? __ldg(irow + (size_t)kz * ny + yl) : make_float2(0.f, 0.f);
+            const int e = tid + 256 * p, kz = e / HY, yl = 2 * (e - kz * HY);
+            const float2* src = irow + (size_t)kz * ny + yl;
+            float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (e < NH1 * HY) {
+                if (vec && yl + 1 < rows) {
+                    v4 = __ldg(reinterpret_cast<const float4*>(src));
+                } else {
+                    if (yl < rows) { const float2 q = __ldg(src); v4.x = q.x; v4.y = q.y; }
+                    if (yl + 1 < rows) { const float2 q = __ldg(src + 1); v4.z = q.x; v4.w = q.y; }
+                }
+            }
+            w[p] = v4;
         }
 #pragma unroll
         for (int p = 0; p < PER; ++p) {
             const int e = tid + 256 * p;
-            if (e < NH1 * YG) T[(e / YG) * TP + e % YG] = w[p];
+            if (e < NH1 * HY) *reinterpret_cast<float4*>(T + (e / HY) * TP + 2 * (e % HY)) = w[p];
         }
         __syncthreads();
         const int a = 2 * g, b = a + 1;
@@ -217,12 +236,14 @@ int zt_launch_t(bool fwd, int nx, int ny, const void* in, void* out, cudaStream_
     int grid = 0, rc;
     if (fwd) {
         if ((rc = zt_grid(zt_r2c_kernel<NZ>, G::SMEM, items, &grid))) return rc;
+        const bool vec = (ny % 2) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
         EVX_TIMED("fft_z_r2c", st, zt_r2c_kernel<NZ><<<grid, 256, G::SMEM, st>>>(
-                                       static_cast<const float*>(in), static_cast<float2*>(out), nx, ny));
+                                       static_cast<const float*>(in), static_cast<float2*>(out), nx, ny, vec));
     } else {
         if ((rc = zt_grid(zt_c2r_kernel<NZ>, G::SMEM, items, &grid))) return rc;
+        const bool vec = (ny % 2) == 0 && (reinterpret_cast<uintptr_t>(in) & 15) == 0;
         EVX_TIMED("fft_z_c2r", st, zt_c2r_kernel<NZ><<<grid, 256, G::SMEM, st>>>(
-                                       static_cast<const float2*>(in), static_cast<float*>(out), nx, ny));
+                                       static_cast<const float2*>(in), static_cast<float*>(out), nx, ny, vec));
     }
     count_launch();
     return check_launch(fwd ? "zt_r2c_kernel" : "zt_c2r_kernel");
