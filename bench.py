@@ -45,9 +45,10 @@ FALLBACK_HBM_GBS = 6800.0
 NCU_DRAM_BYTES_PER_VOXEL = {
     "ch_rhs_fused": (153.137408e6 + 92.517888e6) / 256 ** 3,
     "ch_pullback_grads": (344.547840e6 + 54.629120e6) / 256 ** 3,
-    "fd_step": (552.458240e6 + 498.603264e6) / 512 ** 3,
+    "fd_step": (561.215488e6 + 497.061376e6) / 512 ** 3,
     "fd_tblock2": (554.379264e6 + 495.615488e6) / 512 ** 3,
-    "ch_xpass_adj_spec": (135.378432e6 + 24.717824e6) / 256 ** 3,
+    "ch_xpass_adj_spec": (135.314432e6 + 9.799424e6) / 256 ** 3,
+    "ch_xpass_fwd_store": (67.698944e6 + 74.089728e6) / 256 ** 3,
     "ch_xpass_fwd": (135.399168e6 + 74.517248e6) / (512 * 256 * 256),
     "ch_pullback_grads_spec": (300.036608e6 + 57.321984e6) / 256 ** 3,
     "ac_rhs": (68.689152e6 + 24.427008e6) / 256 ** 3,
