@@ -118,6 +118,8 @@ yz_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx) {
         // ---- z stage: row pairs of this CTA's rows
         const int t = tid % TZ, g = tid / TZ;
         const ZCol zc{g * G::PS, t, G::KS};
+        float2 twz[EZ];                      // z-stage twiddles of this thread (lanes differ in t)
+        fwd_twiddles<EZ, TZ>(twz, t);
 #pragma unroll 1
         for (int rnd = 0; rnd < G::ZROUNDS; ++rnd) {
             const int pair = rnd * G::GZ + g;
@@ -129,7 +131,7 @@ yz_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx) {
                 const int z = TZ * e + t;
                 v[e] = live ? make_float2(__ldg(plane + ya * NZ + z), __ldg(plane + yb * NZ + z)) : make_float2(0.f, 0.f);
             }
-            fwd_stage1<EZ, TZ, true>(v, Z, zc);   // a row pair's TZ threads share a warp
+            fwd_stage1_tw<EZ, TZ, true>(v, Z, zc, twz);   // a row pair's TZ threads share a warp
             fwd_stage2<EZ, TZ>(v);
             // v[q*TZ + k2] = C(k1 + EZ*k2), k1 = t*QZ + q.  Partner C(NZ - k): for
             // k1 != 0 it is k1' = EZ - k1, k2' = TZ-1-k2 (lane TZ-t for q = 0, TZ-1-t
@@ -260,6 +262,8 @@ yz_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx) {
         float* plane = out + (size_t)x * NY * NZ;
         const int t = tid % TZ, g = tid / TZ;
         const ZCol zc{g * G::PS, t, G::KS};
+        float2 twz[EZ];                      // z-stage twiddles of this thread (lanes differ in t)
+        inv_twiddles<EZ, TZ>(twz, t);
         const float2* s0 = cl.map_shared_rank(S, 0);
 #pragma unroll 1
         for (int rnd = 0; rnd < G::ZROUNDS; ++rnd) {
@@ -288,7 +292,7 @@ yz_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx) {
                     }
                     v[q * TZ + k2] = c;
                 }
-            inv_stage2<EZ, TZ>(v, Z, zc);
+            inv_stage2_tw<EZ, TZ>(v, Z, zc, twz);
             inv_stage1<EZ, TZ, true>(v, Z, zc);   // a row pair's TZ threads share a warp
             if (live) {
 #pragma unroll

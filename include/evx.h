@@ -187,8 +187,8 @@ int evx_ch_plan_create(evx_ch_plan** plan, const evx_grid* g, int flags);
 int evx_ch_plan_create_bc(evx_ch_plan** plan, const evx_grid* g, const evx_bc* bc, int flags);
 /* flags bit 2: with the x-pass and ny, nz in {64, 128, 256}, use the fused
  * (y, z) kernels (evx_fft_yz_r2c/c2r) instead of cuFFT's (y, z) plans.  Off by
- * default: on GB300 at 256^3 they take 73/68 us per transform against cuFFT's
- * 65/62 us (latency-bound; one HBM pass instead of two does not pay yet).
+ * default: on GB300 at 256^3 they take 55/68 us per transform against cuFFT's
+ * 64/61 us (the C2R is latency-bound on its distributed-shared-memory gathers).
  * By default an x-pass plan with nz = 256 keeps the half spectrum y-contiguous,
  * (nx, nz/2+1, ny): the z pass is evx_fft_z_r2c/c2r and the y transform one
  * contiguous batched cuFFT C2C (56/61 us per transform at 256^3 against
