@@ -91,6 +91,9 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) {
     return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
 }
+// A two-lane product for the places where nothing can be fused into it: its
+// result feeds only further products, or it is exact (a power of two times x).
+__device__ __forceinline__ float2 mul2_nofuse(float2 a, float2 b) { return __fmul2_rn(a, b); }
 }  // namespace exact
 
 // Per-thread load plan for one shared field plane (precomputed once per tile).

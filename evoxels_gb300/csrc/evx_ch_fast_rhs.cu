@@ -20,6 +20,7 @@ using namespace fast;
 using exact::add2;
 using exact::mul2;
 using exact::sub2;
+using exact::mul2_nofuse;
 
 // Two z-adjacent points at a time (two-lane sums, scalar products); every lane
 // performs exactly the scalar operations of lap7 / mu_hom / face_flux
@@ -32,21 +33,21 @@ __device__ __forceinline__ float2 lap7x2(const RhsK& K, float2 c, float2 xm, flo
     float2 t = mul2(add2(xp, xm), K.ih2x);
     t = add2(t, mul2(add2(yp, ym), K.ih2y));
     t = add2(t, mul2(add2(zp, zm), K.ih2z));
-    return sub2(t, mul2(mul2(f2s(2.f), c), K.ih2sum));
+    return sub2(t, mul2(mul2_nofuse(f2s(2.f), c), K.ih2sum));
 }
 // mu = w*c*(1-c)*(1-2c) - kappa*lap(c)
 __device__ __forceinline__ float2 mu_x2(const RhsK& K, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
                                         float2 zm, float2 zp) {
-    float2 h = mul2(K.w, c);
-    h = mul2(h, sub2(f2s(1.f), c));
-    h = mul2(h, sub2(f2s(1.f), mul2(f2s(2.f), c)));
+    float2 h = mul2_nofuse(K.w, c);                       // feeds a product
+    h = mul2_nofuse(h, sub2(f2s(1.f), c));                // feeds a product
+    h = mul2(h, sub2(f2s(1.f), mul2_nofuse(f2s(2.f), c)));   // 2c exact
     return sub2(h, mul2(K.kappa, lap7x2(K, c, xm, xp, ym, yp, zm, zp)));
 }
 // (cf*(1-cf)) * ((mu_hi - mu_lo)*ih), cf = 0.5*(c_hi + c_lo)
 __device__ __forceinline__ float2 flux_x2(float2 clo, float2 chi, float2 mlo, float2 mhi, float2 ih) {
-    const float2 cf = mul2(f2s(0.5f), add2(chi, clo));
-    const float2 m = mul2(cf, sub2(f2s(1.f), cf));
-    return mul2(m, mul2(sub2(mhi, mlo), ih));
+    const float2 cf = mul2_nofuse(f2s(0.5f), add2(chi, clo));   // exact
+    const float2 m = mul2_nofuse(cf, sub2(f2s(1.f), cf));        // feeds a product
+    return mul2(m, mul2_nofuse(sub2(mhi, mlo), ih));             // the inner one feeds a product
 }
 
 template <class T, bool FUSED>
@@ -150,7 +151,7 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
             float2 d = mul2(sub2(fxp_, fxm_), K.ihx);
             d = add2(d, mul2(sub2(fyp, fym), K.ihy));
             d = add2(d, mul2(sub2(fzp, fzm), K.ihz));
-            return mul2(K.D, d);
+            return mul2_nofuse(K.D, d);   // the result is stored
         };
         const float2 rA = divr(fxp[0], fxm[0], y1, y0, zhA, zlA);
         const float2 rB = divr(fxp[1], fxm[1], y2, y1, zhB, zlB);
