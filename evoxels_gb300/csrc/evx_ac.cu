@@ -46,6 +46,7 @@ using fast::f2s;
 using fast::exact::add2;
 using fast::exact::mul2;
 using fast::exact::sub2;
+using fast::exact::mul2_nofuse;   // products whose result only feeds products, or exact ones
 
 constexpr int AZ = 64, AY = 8;                // output tile
 constexpr int PW = AZ + 4;                    // shared row: z in [k0-2, k0+AZ+2), cell z at z-k0+2
@@ -71,7 +72,7 @@ __device__ __forceinline__ float bc_map(const Geo& G, int a, int side, float v) 
 
 // ((R - 2C) + L), two lanes
 __device__ __forceinline__ float2 d2x2(float2 R, float2 C, float2 L) {
-    return add2(sub2(R, mul2(f2s(2.f), C)), L);
+    return add2(sub2(R, mul2_nofuse(f2s(2.f), C)), L);
 }
 // ((pp + mm) - mp) - pm
 __device__ __forceinline__ float2 mixed2(float2 pp, float2 mm, float2 mp, float2 pm) {
@@ -79,7 +80,7 @@ __device__ __forceinline__ float2 mixed2(float2 pp, float2 mm, float2 mp, float2
 }
 // ((((0.5*ga)*gb)*m)*ia)*ib
 __device__ __forceinline__ float2 cross2(float2 ga, float2 gb, float2 m, float2 ia, float2 ib) {
-    return mul2(mul2(mul2(mul2(mul2(f2s(0.5f), ga), gb), m), ia), ib);
+    return mul2(mul2_nofuse(mul2_nofuse(mul2_nofuse(mul2_nofuse(f2s(0.5f), ga), gb), m), ia), ib);
 }
 
 __global__ void __launch_bounds__(AC_THREADS)
@@ -172,13 +173,13 @@ ac_rhs_kernel(const float* __restrict__ u, float* __restrict__ r, Geo G, AcP P, 
             const float2 B = *reinterpret_cast<const float2*>(o + c - PW);
             const float2 T = *reinterpret_cast<const float2*>(o + c + PW);
             const float2 Bk = make_float2(o[c - 1], C.x), F = make_float2(C.y, o[c + 2]);
-            const float2 gx = mul2(mul2(f2s(0.5f), sub2(R, L)), dx0);
-            const float2 gy = mul2(mul2(f2s(0.5f), sub2(T, B)), dx1);
-            const float2 gz = mul2(mul2(f2s(0.5f), sub2(F, Bk)), dx2);
+            const float2 gx = mul2_nofuse(mul2_nofuse(f2s(0.5f), sub2(R, L)), dx0);
+            const float2 gy = mul2_nofuse(mul2_nofuse(f2s(0.5f), sub2(T, B)), dx1);
+            const float2 gz = mul2_nofuse(mul2_nofuse(f2s(0.5f), sub2(F, Bk)), dx2);
             const float2 gx2 = mul2(gx, gx), gy2 = mul2(gy, gy), gz2 = mul2(gz, gz);
-            float2 n = mul2(mul2(gx2, d2x2(R, C, L)), q0);
-            n = add2(n, mul2(mul2(gy2, d2x2(T, C, B)), q1));
-            n = add2(n, mul2(mul2(gz2, d2x2(F, C, Bk)), q2));
+            float2 n = mul2(mul2_nofuse(gx2, d2x2(R, C, L)), q0);
+            n = add2(n, mul2(mul2_nofuse(gy2, d2x2(T, C, B)), q1));
+            n = add2(n, mul2(mul2_nofuse(gz2, d2x2(F, C, Bk)), q2));
             {   // xy: f(x+1,y+1) + f(x-1,y-1) - f(x-1,y+1) - f(x+1,y-1)
                 const float2 pp = *reinterpret_cast<const float2*>(p + c + PW);
                 const float2 mm = *reinterpret_cast<const float2*>(m + c - PW);
@@ -204,14 +205,16 @@ ac_rhs_kernel(const float* __restrict__ u, float* __restrict__ r, Geo G, AcP P, 
             float2 t = mul2(add2(R, L), q0);
             t = add2(t, mul2(add2(T, B), q1));
             t = add2(t, mul2(add2(F, Bk), q2));
-            const float2 lap = mul2(curv, sub2(t, mul2(mul2(f2s(2.f), C), qs)));
+            const float2 lap = mul2(curv, sub2(t, mul2(mul2_nofuse(f2s(2.f), C), qs)));
             // w*c*(1-c)*(1-2c); pot/2 as pot*0.5 (the same correctly rounded value)
             const float2 omC = sub2(f2s(1.f), C);
-            const float2 pot = mul2(mul2(mul2(w2, C), omC), sub2(f2s(1.f), mul2(f2s(2.f), C)));
-            const float2 ph = mul2(pot, f2s(0.5f));
+            const float2 pot = mul2_nofuse(mul2_nofuse(mul2_nofuse(w2, C), omC),
+                                           sub2(f2s(1.f), mul2_nofuse(f2s(2.f), C)));   // feeds *0.5
+            const float2 ph = mul2_nofuse(pot, f2s(0.5f));                               // feeds a division
             const float2 pot2 = make_float2(__fdiv_rn(ph.x, P.eps), __fdiv_rn(ph.y, P.eps));
-            const float2 df = add2(mul2(gab, sub2(add2(lap, nlap), pot2)), mul2(mul2(mul2(toe, C), omC), force));
-            const float2 res = mul2(M, df);
+            const float2 df = add2(mul2(gab, sub2(add2(lap, nlap), pot2)),
+                                   mul2(mul2_nofuse(mul2_nofuse(toe, C), omC), force));
+            const float2 res = mul2_nofuse(M, df);   // stored
             float* dst = r + ((size_t)i * ny + j) * nz + k;
             if (vec) {
                 *reinterpret_cast<float2*>(dst) = res;
