@@ -88,6 +88,8 @@ _SIGS = {
     "evx_ch_spectrum_floats": (C.c_size_t, [_P]),
     "evx_device_status": (C.c_int, [C.c_int]),
     "evx_ac_rhs": (C.c_int, [_P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.POINTER(EvxAcParams), _P]),
+    "evx_ac_rhs_stage": (C.c_int, [_P, _P, C.c_float, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC),
+                                   C.POINTER(EvxAcParams), _P]),
     "evx_rk4_combine": (C.c_int, [_P, _P, _P, _P, _P, C.c_float, _P, C.c_size_t, _P]),
     "evx_rkc_stage": (C.c_int, [_P, _P, _P, _P, _P, C.POINTER(EvxRkcCoeffs), _P, C.c_size_t, _P]),
     "evx_fft_yz_r2c": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P]),

@@ -84,7 +84,8 @@ __device__ __forceinline__ float2 cross2(float2 ga, float2 gb, float2 m, float2 
 }
 
 __global__ void __launch_bounds__(AC_THREADS)
-ac_rhs_kernel(const float* __restrict__ u, float* __restrict__ r, Geo G, AcP P, int LX) {
+ac_rhs_kernel(const float* __restrict__ u, const float* __restrict__ kst, float cst, float* __restrict__ r, Geo G,
+              AcP P, int LX) {
     __shared__ __align__(16) float ring[4][PLANE];
     const int tid = threadIdx.x;
     const int tx = tid & 31, ty = tid >> 5;
@@ -125,8 +126,16 @@ ac_rhs_kernel(const float* __restrict__ u, float* __restrict__ r, Geo G, AcP P, 
     auto fetch = [&](int x) {   // raw values of plane x into registers
         const int xi = x < 0 ? (perx ? x + nx : 0) : (x >= nx ? (perx ? x - nx : nx - 1) : x);
         const float* src = u + (size_t)xi * plane;
+        if (kst) {   // a Runge-Kutta stage input u + c*k, rounded as evx_fe_update rounds it
+            const float* ks = kst + (size_t)xi * plane;
 #pragma unroll
-        for (int s = 0; s < CPT; ++s) pre[s] = cell[s].off >= 0 ? __ldg(src + cell[s].off) : 0.f;
+            for (int s = 0; s < CPT; ++s)
+                pre[s] = cell[s].off >= 0 ? __fadd_rn(__ldg(src + cell[s].off), __fmul_rn(cst, __ldg(ks + cell[s].off)))
+                                          : 0.f;
+        } else {
+#pragma unroll
+            for (int s = 0; s < CPT; ++s) pre[s] = cell[s].off >= 0 ? __ldg(src + cell[s].off) : 0.f;
+        }
     };
     auto stash = [&](int x) {   // clip, boundary maps in x, y, z order, into the ring
         float* dst = ring[x & 3];
@@ -263,14 +272,15 @@ using namespace evx;
 
 extern "C" {
 
-int evx_ac_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc, const evx_ac_params* p,
-               void* stream) {
+namespace {
+int ac_rhs_launch(const float* u, const float* k, float c, float* r, const evx_grid* g, const evx_bc* bc,
+                  const evx_ac_params* p, void* stream) {
     int rc = validate_grid(g);
     if (rc) return rc;
     if ((rc = validate_bc(bc))) return rc;
     if (!p) return fail(EVX_ERR_BAD_ARG, "params are NULL");
     if (!u || !r) return fail(EVX_ERR_BAD_ARG, "NULL field pointer");
-    if (u == r) return fail(EVX_ERR_BAD_ARG, "input and output must not alias");
+    if (u == r || k == r) return fail(EVX_ERR_BAD_ARG, "input and output must not alias");
     if (!(p->eps != 0.f) || !std::isfinite(p->eps)) return fail(EVX_ERR_BAD_ARG, "eps must be finite and non-zero");
     const AcP P{p->w, p->eps, p->gab, p->M, p->force, p->three_over_eps, p->curvature, p->one_minus_curvature};
     const Geo G = make_geo(g, bc);
@@ -290,9 +300,21 @@ int evx_ac_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc, co
     lx = std::min(lx, g->nx);
     const dim3 grid(tz, ty, (g->nx + lx - 1) / lx);
     cudaStream_t st = as_stream(stream);
-    EVX_TIMED("ac_rhs", st, ac_rhs_kernel<<<grid, AC_THREADS, 0, st>>>(u, r, G, P, lx));
+    EVX_TIMED("ac_rhs", st, ac_rhs_kernel<<<grid, AC_THREADS, 0, st>>>(u, k, c, r, G, P, lx));
     count_launch();
     return check_launch("ac_rhs_kernel");
+}
+}  // namespace
+
+int evx_ac_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc, const evx_ac_params* p,
+               void* stream) {
+    return ac_rhs_launch(u, nullptr, 0.f, r, g, bc, p, stream);
+}
+
+int evx_ac_rhs_stage(const float* u, const float* k, float c, float* r, const evx_grid* g, const evx_bc* bc,
+                     const evx_ac_params* p, void* stream) {
+    if (!k) return fail(EVX_ERR_BAD_ARG, "NULL stage field");
+    return ac_rhs_launch(u, k, c, r, g, bc, p, stream);
 }
 
 int evx_rk4_combine(const float* u, const float* k1, const float* k2, const float* k3, const float* k4, float dt6,

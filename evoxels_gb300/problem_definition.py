@@ -262,3 +262,17 @@ class TwoPhaseAllenCahn(_BCMixin):
             _lib.check(L.evx_ac_rhs(phi[ch].data_ptr(), out[ch].data_ptr(), g, self._evx_bc, self._params,
                                     cuda_stream()), "evx_ac_rhs")
         return out
+
+    def rhs_stage(self, t, phi, k, c):
+        """``rhs(t, phi + c*k)`` with the stage input formed inside the kernel, bit for bit as
+        ``phi + float32(c)*k`` (the Runge-Kutta stages of evoxels/timesteppers.py:57-59)."""
+        phi = self.vg.check_field(phi)
+        k = self.vg.check_field(k)
+        out = torch.empty_like(phi)
+        g = self.vg.evx_grid()
+        L = _lib.lib()
+        cf = float(np.float32(c))
+        for ch in range(phi.shape[0]):
+            _lib.check(L.evx_ac_rhs_stage(phi[ch].data_ptr(), k[ch].data_ptr(), cf, out[ch].data_ptr(), g,
+                                          self._evx_bc, self._params, cuda_stream()), "evx_ac_rhs_stage")
+        return out

@@ -216,9 +216,15 @@ class RungeKutta4(TimeStepper):
         u = self.problem.vg.check_field(u)
         dt = self.dt
         k1 = self.problem.rhs(t, u)
-        k2 = self.problem.rhs(t + 0.5 * dt, self._stage(u, k1, 0.5 * dt))
-        k3 = self.problem.rhs(t + 0.5 * dt, self._stage(u, k2, 0.5 * dt))
-        k4 = self.problem.rhs(t + dt, self._stage(u, k3, dt))
+        fused = getattr(self.problem, "rhs_stage", None)   # the stage input formed inside the rhs kernel
+        if fused is not None:
+            k2 = fused(t + 0.5 * dt, u, k1, 0.5 * dt)
+            k3 = fused(t + 0.5 * dt, u, k2, 0.5 * dt)
+            k4 = fused(t + dt, u, k3, dt)
+        else:
+            k2 = self.problem.rhs(t + 0.5 * dt, self._stage(u, k1, 0.5 * dt))
+            k3 = self.problem.rhs(t + 0.5 * dt, self._stage(u, k2, 0.5 * dt))
+            k4 = self.problem.rhs(t + dt, self._stage(u, k3, dt))
         out = torch.empty_like(u)
         _lib.check(_lib.lib().evx_rk4_combine(u.data_ptr(), k1.data_ptr(), k2.data_ptr(), k3.data_ptr(),
                                               k4.data_ptr(), float(np.float32(dt / 6)), out.data_ptr(),

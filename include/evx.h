@@ -138,6 +138,12 @@ int evx_fe_update(const float* u, const float* r, float dt, float* out, size_t n
  * the reference's float32 arithmetic.  u and r: (nx, ny, nz) float32. */
 int evx_ac_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc,
                const evx_ac_params* p, void* stream);
+/* The same rhs of a Runge-Kutta stage input, r = rhs(u + c*k), the stage field
+ * formed on the fly as evx_fe_update forms it (float32(c), one rounding per
+ * operation), so RungeKutta4's k2..k4 equal rhs(evx_fe_update(u, k, c)) bit for
+ * bit without the stage field in HBM. */
+int evx_ac_rhs_stage(const float* u, const float* k, float c, float* r, const evx_grid* g,
+                     const evx_bc* bc, const evx_ac_params* p, void* stream);
 
 /* RungeKutta4.step's combination (evoxels/timesteppers.py:61):
  * out = u + dt6*(((k1 + 2*k2) + 2*k3) + k4), dt6 = float32(dt/6); the stage

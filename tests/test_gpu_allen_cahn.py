@@ -90,3 +90,23 @@ def test_ac_potential_forms(cuda_lib):
     # default Neumann BCs: the symbol lives on the x-mirrored grid, as the reference's k_squared
     assert tuple(TwoPhaseAllenCahn(vg).fourier_symbol.shape) == (16, 8, 5)
     assert tuple(TwoPhaseAllenCahn(vg, bc=("periodic",) * 3).fourier_symbol.shape) == (8, 8, 5)
+
+
+@pytest.mark.parametrize("bc", [None, ("periodic", "periodic", "periodic"),
+                                (("dirichlet", (0.2, 0.9)), "neumann", "periodic")])
+def test_ac_rhs_stage_equals_rhs_of_stage_field(cuda_lib, bc):
+    """rhs(u + c*k) with the stage input formed inside the kernel equals rhs(evx_fe_update(u, k, c))
+    bit for bit (RungeKutta4 takes the fused form)."""
+    from evoxels_gb300 import _lib
+    from evoxels_gb300.problem_definition import TwoPhaseAllenCahn
+    from evoxels_gb300.voxelgrid import cuda_stream
+    shape = (20, 18, 70)
+    kw = {} if bc is None else {"bc": bc}
+    prob = TwoPhaseAllenCahn(vg_for(shape), eps=2.5, curvature=0.1, **kw)
+    u = gpu(1.4 * oracle.seeded_unit_field(shape, 81) - 0.2)
+    k = gpu(oracle.seeded_unit_field(shape, 82) - 0.5)
+    for c in (0.25, 0.5 * 0.37, 0.37):
+        stage = torch.empty_like(u)
+        _lib.check(cuda_lib.evx_fe_update(u.data_ptr(), k.data_ptr(), float(np.float32(c)), stage.data_ptr(),
+                                          u.numel(), cuda_stream()), "fe")
+        torch.testing.assert_close(prob.rhs_stage(0.0, u, k, c), prob.rhs(0.0, stage), rtol=0, atol=0)
