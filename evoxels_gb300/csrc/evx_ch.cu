@@ -596,8 +596,27 @@ int evx_ch_forward(evx_ch_plan* plan, const float* u_in, float* u_out, int nstep
     return evx_ch_forward_spectra(plan, u_in, u_out, nsteps, traj, nullptr, prm, nonfinite, workspace, stream);
 }
 
+namespace {
+// The forward loop of evx_ch_forward_spectra; mult != NULL replaces the IMEX
+// multiplier by a table (the ExponentialEuler step of evx_ch_forward_mult).
+int ch_forward_impl(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps, float* traj, float* spectra,
+                    const float* mult, const evx_ch_params* prm, int* nonfinite, void* workspace, void* stream);
+}  // namespace
+
 int evx_ch_forward_spectra(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps, float* traj,
                            float* spectra, const evx_ch_params* prm, int* nonfinite, void* workspace, void* stream) {
+    return ch_forward_impl(plan, u_in, u_out, nsteps, traj, spectra, nullptr, prm, nonfinite, workspace, stream);
+}
+
+int evx_ch_forward_mult(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps, const float* mult,
+                        const evx_ch_params* prm, int* nonfinite, void* workspace, void* stream) {
+    if (!mult) return fail(EVX_ERR_BAD_ARG, "NULL multiplier table");
+    return ch_forward_impl(plan, u_in, u_out, nsteps, nullptr, nullptr, mult, prm, nonfinite, workspace, stream);
+}
+
+namespace {
+int ch_forward_impl(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps, float* traj, float* spectra,
+                    const float* mult, const evx_ch_params* prm, int* nonfinite, void* workspace, void* stream) {
     if (!plan) return fail(EVX_ERR_BAD_ARG, "plan is NULL");
     int rc = ch_validate_params(prm);
     if (rc) return rc;
@@ -638,8 +657,22 @@ int evx_ch_forward_spectra(evx_ch_plan* plan, const float* u_in, float* u_out, i
             if ((rc = check_launch("ch_mirror_x_kernel"))) return rc;
         }
         if ((rc = ch_r2c(plan, r, spec, st))) return rc;
-        float2* ds = spectra ? reinterpret_cast<float2*>(spectra + (size_t)s * plan->spec_floats) : nullptr;
-        if ((rc = ch_kspace_forward(plan, spec, P, st, ds))) return rc;
+        if (mult) {   // table multiplier (exponential Euler)
+            if (plan->xmode) {
+                XpassArgs a = xpass_args(plan, 4, spec, P);
+                a.mult = mult;
+                if ((rc = xpass_launch(a, st))) return rc;
+            } else {
+                const float invN = (float)(1.0 / ((double)plan->nxe * g->ny * g->nz));
+                EVX_TIMED("spec_mult", st, spec_mult_kernel<<<elementwise_grid(plan->nspec), 256, 0, st>>>(
+                    spec, mult, invN, plan->nspec));
+                count_launch();
+                if ((rc = check_launch("spec_mult_kernel"))) return rc;
+            }
+        } else {
+            float2* ds = spectra ? reinterpret_cast<float2*>(spectra + (size_t)s * plan->spec_floats) : nullptr;
+            if ((rc = ch_kspace_forward(plan, spec, P, st, ds))) return rc;
+        }
         if ((rc = ch_c2r(plan, spec, upd, false, st))) return rc;
     }
     EVX_TIMED("ch_axpy", st, ch_axpy_kernel<<<elementwise_grid(N / 4 + 1), 256, 0, st>>>(
@@ -647,6 +680,7 @@ int evx_ch_forward_spectra(evx_ch_plan* plan, const float* u_in, float* u_out, i
     count_launch();
     return check_launch("ch_axpy_kernel");
 }
+}  // namespace
 
 int evx_ch_step(evx_ch_plan* plan, const float* u_in, float* u_out, const evx_ch_params* p, void* workspace,
                 void* stream) {

@@ -289,6 +289,26 @@ class ExponentialEuler(TimeStepper):
                    "evx_spectral_update")
         return out
 
+    def advance(self, u, nsteps, nonfinite=None):
+        """``nsteps`` steps from ``u``.  For CahnHilliard one library call
+        (``evx_ch_forward_mult``: each step's update is fused into the next
+        step's rhs pass), bit-identical to ``nsteps`` calls of ``step``; other
+        problems step one at a time."""
+        if not isinstance(self.problem, CahnHilliard):
+            for _ in range(nsteps):
+                u = self.step(0.0, u)
+            return u
+        u = self.problem.vg.check_field(u)
+        if u.shape[0] != 1:
+            raise NotImplementedError("ExponentialEuler in evoxels_gb300 steps one field (C == 1)")
+        out = torch.empty_like(u)
+        p = self._plan
+        nf = nonfinite.data_ptr() if nonfinite is not None else None
+        _lib.check(_lib.lib().evx_ch_forward_mult(p.handle, u.data_ptr(), out.data_ptr(), int(nsteps),
+                                                  self._mult.data_ptr(), self.problem.evx_params(self.dt), nf,
+                                                  p.workspace.data_ptr(), cuda_stream()), "evx_ch_forward_mult")
+        return out
+
 
 def _rkc_chebyshev(polygrad, damping):
     """``w0``, ``s`` and the Chebyshev values ``T_s(w0)``, ``T_s'(w0)`` for the

@@ -214,6 +214,14 @@ size_t evx_ch_workspace_bytes(const evx_ch_plan* plan);
 int evx_spectral_update(evx_ch_plan* plan, const float* u, const float* r, const float* mult, float* out,
                         void* workspace, void* stream);
 
+/* nsteps ExponentialEuler steps of CahnHilliard in one call, the update fused
+ * into the next step's rhs pass as in evx_ch_forward: each step is
+ * u + irfftn(mult * rfftn(pad_fft(rhs(u))))[:nx] with the CahnHilliard rhs of
+ * prm (prm->dt is not used), bit-identical to nsteps evx_ch_rhs +
+ * evx_spectral_update calls.  nonfinite as in evx_ch_forward. */
+int evx_ch_forward_mult(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps, const float* mult,
+                        const evx_ch_params* prm, int* nonfinite, void* workspace, void* stream);
+
 /* One PseudoSpectralIMEX step of CahnHilliard (evoxels/timesteppers.py:85-89):
  * u_out = u_in + irfftn(prefac * rfftn(rhs(u_in))).  u_in is read only. */
 int evx_ch_step(evx_ch_plan* plan, const float* u_in, float* u_out,
