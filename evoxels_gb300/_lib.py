@@ -83,6 +83,7 @@ _SIGS = {
     "evx_ch_workspace_bytes": (C.c_size_t, [_P]),
     "evx_spectral_update": (C.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "evx_ch_forward_mult": (C.c_int, [_P, _P, _P, C.c_int, _P, C.POINTER(EvxChParams), _P, _P, _P]),
+    "evx_ch_mult_layout": (C.c_int, [_P]),
     "evx_ch_step": (C.c_int, [_P, _P, _P, C.POINTER(EvxChParams), _P, _P]),
     "evx_ch_forward": (C.c_int, [_P, _P, _P, C.c_int, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),

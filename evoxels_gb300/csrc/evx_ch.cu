@@ -591,6 +591,8 @@ int evx_spectral_update(evx_ch_plan* plan, const float* u, const float* r, const
 
 size_t evx_ch_spectrum_floats(const evx_ch_plan* p) { return p ? p->spec_floats : 0; }
 
+int evx_ch_mult_layout(const evx_ch_plan* p) { return p ? (p->ztmode ? 1 : 0) : -1; }
+
 int evx_ch_forward(evx_ch_plan* plan, const float* u_in, float* u_out, int nsteps, float* traj,
                    const evx_ch_params* prm, int* nonfinite, void* workspace, void* stream) {
     return evx_ch_forward_spectra(plan, u_in, u_out, nsteps, traj, nullptr, prm, nonfinite, workspace, stream);

@@ -63,7 +63,8 @@ __device__ int g_dev_status;       // bit 0: an x-pass barrier wait gave up
 // twiddle into xs[k1][j] (N2 > 1) or back into v (N2 == 1).  MODE 0 forward
 // (optional store of the product to dsp), 1 adjoint g, 2 adjoint g and h (into
 // hv), 3 adjoint g with the Parseval sums against dsp, 4 multiplier table
-// (mult[kx*M + ky*nzh + kz], mrow = mult + ky*nzh + kz).  dsp points at the tile's stored
+// (mult[kx*M + m] in the spectrum's own pencil order, mrow = mult + m: a warp's
+// reads are consecutive whichever of y or z is contiguous).  dsp points at the tile's stored
 // spectrum ([element][thread], thread offset included).
 // PRE (mode 3): the stored spectrum values come preloaded in dpre[q*N2 + k2].
 template <int N1, int N2, int MODE, bool PRE = false>
@@ -199,7 +200,7 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
     fwd_stage1<N1, N2>(v, xs, c);
     float2 hv[MODE == 2 ? N1 : 1];
     mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2,
-                            mult + (ky * nzh + kz), M);
+                            mult + mc, M);
     auto store = [&](float2* dst) {
         if (live) {
 #pragma unroll
@@ -345,7 +346,7 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         fwd_stage1<N1, N2>(v, xs, c);
         float2 hv[1];
         mid_stage<N1, N2, MODE, PRE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1,
-                                     t2, mult + (ky * nzh + kz), M, &dpre);
+                                     t2, mult + mc, M, &dpre);
         inv_stage1<N1, N2>(v, xs, c);
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) xs[(N2 * n1 + c.n2) * P + c.p] = v[n1];

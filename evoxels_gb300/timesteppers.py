@@ -85,6 +85,19 @@ def clear_plans():
         _plans.clear()
 
 
+def mult_table(plan, table):
+    """A real multiplier table over the (extended) rfft grid, shaped like the
+    reference's ``phi_1_k_squared`` ([Nx_ext, Ny, Nz//2+1]), as the contiguous
+    float32 device table of ``evx_spectral_update`` on ``plan``: the plan's
+    spectrum order (``evx_ch_mult_layout``; 1 is [Nx_ext, Nz//2+1, Ny])."""
+    t = table.to(torch.float32)
+    t = t.reshape(t.shape[-3:])
+    layout = int(_lib.lib().evx_ch_mult_layout(plan.handle))
+    if layout not in (0, 1):
+        raise RuntimeError(f"evx_ch_mult_layout returned {layout}")
+    return (t.transpose(1, 2) if layout == 1 else t).contiguous()
+
+
 class TimeStepper:
     """Interface of evoxels/timesteppers.py:9-29."""
 
@@ -249,8 +262,8 @@ class ExponentialEuler(TimeStepper):
         self.problem.verify_fft_bc_config()
         self.pad = self.problem.pad_fft_bc
         self.phi_1_k_squared = self.phi1(self.dt * self.problem.fourier_symbol)
-        self._mult = (self.dt * self.phi_1_k_squared).to(torch.float32).contiguous()
         self._plan = get_plan(self.problem.vg, bc=self.problem.bc)
+        self._mult = mult_table(self._plan, self.dt * self.phi_1_k_squared)
 
     def phi1(self, z):
         """``(exp(z) - 1)/z`` with the degree-6 Pade form where |z| < 0.5

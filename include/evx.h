@@ -210,9 +210,16 @@ size_t evx_ch_workspace_bytes(const evx_ch_plan* plan);
  * for any rhs on the plan's grid: out = u + irfftn(mult * rfftn(pad_fft(r)))[:nx],
  * pad_fft the plan's x extension (evoxels/boundary_conditions.py:61-71).  mult is
  * the real multiplier table dt*phi1(dt*symbol) over the (extended) rfft grid,
- * [nxe][ny][nz/2+1] float32 on the device.  r and u are read only. */
+ * float32 on the device, in the plan's spectrum order (evx_ch_mult_layout):
+ * [nxe][ny][nz/2+1], or [nxe][nz/2+1][ny] for the plans whose z pass keeps y
+ * contiguous.  r and u are read only. */
 int evx_spectral_update(evx_ch_plan* plan, const float* u, const float* r, const float* mult, float* out,
                         void* workspace, void* stream);
+
+/* Layout of the multiplier tables of evx_spectral_update and
+ * evx_ch_forward_mult on this plan: 0 [nxe][ny][nz/2+1] (the rfftn order),
+ * 1 [nxe][nz/2+1][ny]; -1 for a NULL plan. */
+int evx_ch_mult_layout(const evx_ch_plan* plan);
 
 /* nsteps ExponentialEuler steps of CahnHilliard in one call, the update fused
  * into the next step's rhs pass as in evx_ch_forward: each step is

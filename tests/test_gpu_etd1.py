@@ -131,7 +131,7 @@ def test_etd1_allen_cahn_driver_and_errors(cuda_lib):
                                                 plan.workspace.data_ptr(), None), "evx_spectral_update")
 
 
-@pytest.mark.parametrize("shape", [(32, 20, 36), (24, 16, 20), (64, 64, 64), (16, 8, 256)])
+@pytest.mark.parametrize("shape", [(32, 20, 36), (24, 16, 20), (64, 64, 64), (16, 8, 256), (8, 24, 256)])
 @pytest.mark.parametrize("b", range(3))
 def test_etd1_fused_advance_bitexact(cuda_lib, shape, b):
     """ExponentialEuler.advance for CahnHilliard (one evx_ch_forward_mult call, each update fused into the
@@ -143,6 +143,19 @@ def test_etd1_fused_advance_bitexact(cuda_lib, shape, b):
     v = u0
     for _ in range(4):
         v = st.step(0.0, v)
+    if shape[2] == 256:   # the z pass's plan: the table is kept in its [kx][kz][ky] order
+        assert torch.equal(st._mult, (st.dt * st.phi_1_k_squared).float().transpose(1, 2).contiguous())
+        # against the cuFFT (y, z) plan with the rfftn-ordered table
+        from evoxels_gb300 import _lib
+        from evoxels_gb300.timesteppers import get_plan, mult_table
+        from evoxels_gb300.voxelgrid import cuda_stream
+        plan = get_plan(st.problem.vg, bc=st.problem.bc, cufft_yz=True)
+        m = mult_table(plan, st.dt * st.phi_1_k_squared)
+        r = st.problem.rhs(0.0, u0)
+        out = torch.empty_like(u0)
+        _lib.check(cuda_lib.evx_spectral_update(plan.handle, u0.data_ptr(), r.data_ptr(), m.data_ptr(),
+                                                out.data_ptr(), plan.workspace.data_ptr(), cuda_stream()), "etd1")
+        assert oracle.rel_to_max(out.cpu().numpy(), st.step(0.0, u0).cpu().numpy()) < 1e-6
     nf = torch.zeros((1,), dtype=torch.int32, device=DEV)   # OR-ed into by the final update
     w = st.advance(u0, 4, nonfinite=nf)
     assert torch.equal(w, v)

@@ -119,7 +119,7 @@ def test_adjoint_matches_cufft_yz_plan(cuda_lib, shape, spectral):
 def test_etd1_matches_cufft_yz_plan(cuda_lib):
     from evoxels_gb300 import _lib
     from evoxels_gb300.problem_definition import CahnHilliard
-    from evoxels_gb300.timesteppers import ExponentialEuler, get_plan
+    from evoxels_gb300.timesteppers import ExponentialEuler, get_plan, mult_table
     from evoxels_gb300.voxelgrid import cuda_stream
     shape = (32, 24, 64)
     for bc in (("periodic",) * 3, ("neumann", "periodic", "periodic")):
@@ -131,8 +131,10 @@ def test_etd1_matches_cufft_yz_plan(cuda_lib):
         outs = []
         for cufft_yz in (False, True):
             plan = get_plan(vg, bc=prob.bc, cufft_yz=cufft_yz, z_pass=not cufft_yz)
+            assert cuda_lib.evx_ch_mult_layout(plan.handle) == (0 if cufft_yz else 1)
+            m = mult_table(plan, st.dt * st.phi_1_k_squared)   # the z pass's table is [kx][kz][ky]
             out = torch.empty_like(u0)
-            _lib.check(cuda_lib.evx_spectral_update(plan.handle, u0.data_ptr(), r.data_ptr(), st._mult.data_ptr(),
+            _lib.check(cuda_lib.evx_spectral_update(plan.handle, u0.data_ptr(), r.data_ptr(), m.data_ptr(),
                                                     out.data_ptr(), plan.workspace.data_ptr(), cuda_stream()), "etd1")
             outs.append(out.cpu().numpy())
         assert oracle.rel_to_max(outs[0], outs[1]) < 1e-6
