@@ -118,6 +118,8 @@ _SIGS = {
     "evx_prof_reset": (None, []),
     "evx_prof_query": (C.c_int, [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "evx_launch_count": (C.c_ulonglong, []),
+    "evx_set_graphs": (None, [C.c_int]),
+    "evx_graphs_enabled": (C.c_int, []),
 }
 
 _lock = threading.Lock()

@@ -290,11 +290,15 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
         if (!plan->spec_floats) return fail(EVX_ERR_UNSUPPORTED, "stored spectra need an x-pass plan (power-of-two nx)");
         if (reinterpret_cast<uintptr_t>(spectra) & 15) return fail(EVX_ERR_BAD_ARG, "spectra must be 16-byte aligned");
     }
-    cudaStream_t st = as_stream(stream);
     const size_t N = plan->n;
     if (nsteps == 0)
-        return check_cuda(cudaMemcpyAsync(lam_out, lam_in, N * sizeof(float), cudaMemcpyDeviceToDevice, st),
-                          "evx_ch_adjoint copy");
+        return check_cuda(cudaMemcpyAsync(lam_out, lam_in, N * sizeof(float), cudaMemcpyDeviceToDevice,
+                                          as_stream(stream)), "evx_ch_adjoint copy");
+    const GraphKey key{2, key_p(states), key_p(spectra), (uint64_t)nsteps, key_p(lam_in), key_p(lam_out),
+                       key_p(grads), key_p(workspace), key_f(prm->D), key_f(prm->kappa), key_f(prm->w),
+                       key_f(prm->A), key_f(prm->sym_coef), key_f(prm->dt)};
+    return plan->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
+    int rc;
     if ((rc = ch_plan_bind(plan, workspace, st, want && !spectral))) return rc;
     const evx_grid* g = &plan->g;
     const Geo G = make_geo(g, nullptr);
@@ -375,6 +379,7 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
         lam = dst;
     }
     return EVX_OK;
+    });
 }
 
 }  // extern "C"

@@ -170,7 +170,9 @@ struct evx_batch {
     cudaGraphExec_t gexec = nullptr;
     const void* gexec_ws = nullptr;
     int gexec_steps = 0;
+    unsigned long long gexec_launches = 0;
     int kspace_blocks = 0;
+    evx::GraphCache graphs;                // replays of repeated forward / adjoint calls
 };
 
 namespace {
@@ -307,11 +309,14 @@ int capture_chunk(evx_batch* b, void* ws, int steps) {
     if ((rc = bind_plans(b, ws, b->cap))) return rc;
     const Bufs B = bufs(b, ws);
     if ((rc = check_cuda(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal), "begin capture"))) return rc;
+    const unsigned long long c0 = launch_counter();
     int rc2 = EVX_OK;
     for (int s = 0; s < steps && !rc2; ++s)
         rc2 = (s % 2 == 0) ? fused_step(b, B, B.ua, B.ub, b->cap) : fused_step(b, B, B.ub, B.ua, b->cap);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(b->cap, &graph);
+    b->gexec_launches = launch_counter() - c0;   // counted per replay instead
+    uncount_launch(b->gexec_launches);
     if (rc2) {
         if (graph) cudaGraphDestroy(graph);
         return rc2;
@@ -577,10 +582,12 @@ int evx_batch_forward(evx_batch* b, const float* u_in, float* u_out, int nsteps,
          15) || (reinterpret_cast<uintptr_t>(ws) & 255))
         return fail(EVX_ERR_BAD_ARG, "buffers must be 16-byte aligned (workspace 256-byte)");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
-    cudaStream_t st = as_stream(stream);
     const size_t T = b->total;
     if (nsteps == 0)
-        return check_cuda(cudaMemcpyAsync(u_out, u_in, T * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
+        return check_cuda(cudaMemcpyAsync(u_out, u_in, T * sizeof(float), cudaMemcpyDeviceToDevice, as_stream(stream)),
+                          "copy");
+    const GraphKey key{3, key_p(u_in), key_p(u_out), (uint64_t)nsteps, key_p(traj), key_p(nonfinite), key_p(ws)};
+    return b->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
     int rc;
     if ((rc = bind_plans(b, ws, st))) return rc;
     const Bufs B = bufs(b, ws);
@@ -604,7 +611,9 @@ int evx_batch_forward(evx_batch* b, const float* u_in, float* u_out, int nsteps,
             ++s;
         }
         const int chunk = (b->tune.graph_steps / 2) * 2;
-        if (chunk >= 2 && nsteps - s >= chunk) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;   // inside a capture of the whole call: no chunk graph
+        if ((rc = check_cuda(cudaStreamIsCapturing(st, &cs), "cudaStreamIsCapturing"))) return rc;
+        if (chunk >= 2 && nsteps - s >= chunk && cs == cudaStreamCaptureStatusNone) {
             if (!b->gexec || b->gexec_ws != ws || b->gexec_steps != chunk) {
                 if ((rc = capture_chunk(b, ws, chunk))) return rc;
                 if ((rc = bind_plans(b, ws, st))) return rc;
@@ -612,6 +621,7 @@ int evx_batch_forward(evx_batch* b, const float* u_in, float* u_out, int nsteps,
             while (nsteps - s >= chunk) {
                 EVX_TIMED("batch_graph_chunk", st, rc = check_cuda(cudaGraphLaunch(b->gexec, st), "cudaGraphLaunch"));
                 if (rc) return rc;
+                count_launch((unsigned)b->gexec_launches);
                 s += chunk;
             }
         }
@@ -627,6 +637,7 @@ int evx_batch_forward(evx_batch* b, const float* u_in, float* u_out, int nsteps,
         src, B.upd, u_out, traj ? traj + (size_t)(nsteps - 1) * T : nullptr, n4, nonfinite));
     count_launch();
     return check_launch("batch_axpy_kernel");
+    });
 }
 
 int evx_batch_adjoint(evx_batch* b, const float* states, int nsteps, const float* lam_in, float* lam_out,
@@ -638,10 +649,12 @@ int evx_batch_adjoint(evx_batch* b, const float* states, int nsteps, const float
           reinterpret_cast<uintptr_t>(states)) & 15) || (reinterpret_cast<uintptr_t>(ws) & 255))
         return fail(EVX_ERR_BAD_ARG, "buffers must be 16-byte aligned (workspace 256-byte)");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
-    cudaStream_t st = as_stream(stream);
     const size_t T = b->total;
     if (nsteps == 0)
-        return check_cuda(cudaMemcpyAsync(lam_out, lam_in, T * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
+        return check_cuda(cudaMemcpyAsync(lam_out, lam_in, T * sizeof(float), cudaMemcpyDeviceToDevice,
+                                          as_stream(stream)), "copy");
+    const GraphKey key{4, key_p(states), (uint64_t)nsteps, key_p(lam_in), key_p(lam_out), key_p(grads), key_p(ws)};
+    return b->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
     int rc;
     if ((rc = bind_plans(b, ws, st))) return rc;
     const Bufs B = bufs(b, ws);
@@ -675,6 +688,7 @@ int evx_batch_adjoint(evx_batch* b, const float* states, int nsteps, const float
         lam = dst;
     }
     return EVX_OK;
+    });
 }
 
 }  // extern "C"

@@ -629,11 +629,15 @@ int ch_forward_impl(evx_ch_plan* plan, const float* u_in, float* u_out, int nste
         if (!plan->spec_floats) return fail(EVX_ERR_UNSUPPORTED, "stored spectra need an x-pass plan (power-of-two nx)");
         if (reinterpret_cast<uintptr_t>(spectra) & 15) return fail(EVX_ERR_BAD_ARG, "spectra must be 16-byte aligned");
     }
-    cudaStream_t st = as_stream(stream);
     const size_t N = plan->n;
     if (nsteps == 0)
-        return check_cuda(cudaMemcpyAsync(u_out, u_in, N * sizeof(float), cudaMemcpyDeviceToDevice, st),
+        return check_cuda(cudaMemcpyAsync(u_out, u_in, N * sizeof(float), cudaMemcpyDeviceToDevice, as_stream(stream)),
                           "evx_ch_forward copy");
+    const GraphKey key{1, key_p(u_in), key_p(u_out), (uint64_t)nsteps, key_p(traj), key_p(spectra), key_p(mult),
+                       key_p(nonfinite), key_p(workspace), key_f(prm->D), key_f(prm->kappa), key_f(prm->w),
+                       key_f(prm->A), key_f(prm->sym_coef), key_f(prm->dt)};
+    return plan->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
+    int rc;
     if ((rc = ch_plan_bind(plan, workspace, st, false))) return rc;
     const evx_grid* g = &plan->g;
     const Geo G = make_geo(g, &plan->bc);
@@ -681,6 +685,7 @@ int ch_forward_impl(evx_ch_plan* plan, const float* u_in, float* u_out, int nste
         src, upd, u_out, traj ? traj + (size_t)(nsteps - 1) * N : nullptr, N, nonfinite));
     count_launch();
     return check_launch("ch_axpy_kernel");
+    });
 }
 }  // namespace
 

@@ -4,6 +4,7 @@
 #include <cufft.h>
 
 #include "evx_common.cuh"
+#include "evx_graph.cuh"
 #include "evx_prof.cuh"
 
 struct evx_ch_plan {
@@ -29,6 +30,7 @@ struct evx_ch_plan {
     int n_part;              // capacity of the partial-sum array (blocks)
     size_t n_xpart;          // x-pass blocks (Parseval partial sums, 2 doubles each); 0 without x-pass
     size_t spec_floats;      // floats per stored increment spectrum; 0 without x-pass
+    evx::GraphCache graphs;  // replays of repeated forward / adjoint calls
 };
 
 namespace evx {

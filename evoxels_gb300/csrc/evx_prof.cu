@@ -6,6 +6,7 @@
 // the elapsed time per named slot.  The launch counter counts this library's
 // own kernel launches (not cuFFT's) and is always on.
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -77,6 +78,29 @@ void prof_end(const ProfTok& t, cudaStream_t st) {
 
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+unsigned long long launch_counter() { return g_launches.load(std::memory_order_relaxed); }
+
+void uncount_launch(unsigned long long n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
+
+namespace {
+// -1: not yet read from the environment (EVX_GRAPHS=0 turns graph replay off)
+std::atomic<int> g_graphs{-1};
+}  // namespace
+
+bool graphs_enabled() {
+    int v = g_graphs.load(std::memory_order_relaxed);
+    if (v < 0) {
+        const char* e = std::getenv("EVX_GRAPHS");
+        v = (e && std::strcmp(e, "0") == 0) ? 0 : 1;
+        int expect = -1;
+        g_graphs.compare_exchange_strong(expect, v);
+        v = g_graphs.load(std::memory_order_relaxed);
+    }
+    if (!v) return false;
+    std::lock_guard<std::mutex> lk(g_mu);
+    return !g_on;
+}
+
 }  // namespace evx
 
 using namespace evx;
@@ -122,5 +146,9 @@ int evx_prof_query(int index, char* name, int name_cap, double* total_ms, long l
 }
 
 unsigned long long evx_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+void evx_set_graphs(int on) { g_graphs.store(on ? 1 : 0, std::memory_order_relaxed); }
+
+int evx_graphs_enabled(void) { return graphs_enabled() ? 1 : 0; }
 
 }  // extern "C"

@@ -372,8 +372,20 @@ int evx_prof_collect(void);
 void evx_prof_reset(void);
 int evx_prof_query(int index, char* name, int name_cap, double* total_ms, long long* count);
 
-/* Number of this library's own kernel launches since load (cuFFT's excluded). */
+/* Number of this library's own kernel launches since load (cuFFT's excluded;
+ * a replayed graph counts its kernels once per replay). */
 unsigned long long evx_launch_count(void);
+
+/* CUDA graph replay of repeated multi-step calls (evx_ch_forward*,
+ * evx_ch_adjoint*, evx_batch_forward/adjoint): a plan runs the first call
+ * with a given set of pointers, step count and parameters eagerly, captures
+ * the second into a graph and replays that graph for later identical calls
+ * (bit-identical results; at most 4 graphs kept per plan).  Calls made while
+ * the stream is being captured by the caller, or with kernel timing on, run
+ * eagerly.  On by default; EVX_GRAPHS=0 in the environment or
+ * evx_set_graphs(0) turns it off. */
+void evx_set_graphs(int on);
+int evx_graphs_enabled(void);
 
 #ifdef __cplusplus
 }
