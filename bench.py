@@ -713,6 +713,12 @@ def main():
                     help="override the IMEX/FE steps per bench step (profiling runs)")
     ap.add_argument("--fd-steps-per-pass", type=int, default=0, choices=[0, 1, 2, 4],
                     help="temporal blocking of the finite-difference workload (0: autotuned)")
+    ap.add_argument("--ref-device", default="cpu", choices=["cpu", "cuda"],
+                    help="reference arm: the oracle port of the reference's torch path on the host cores (the "
+                         "default) or on the GPU (the same-box GPU baseline of the reference's torch path)")
+    ap.add_argument("--ref-compile", action="store_true",
+                    help="reference arm on the GPU: the Cahn-Hilliard step under torch.compile, as the "
+                         "reference's jit=True")
     ap.add_argument("--grid", default=None,
                     help="NX,NY,NZ: run a Cahn-Hilliard workload on another grid (profiling runs; "
                          "the metric then names the grid)")
@@ -897,11 +903,18 @@ def main():
 
 
 def run_reference(args, torch, warmup):
-    """Reference arm: the oracle port of the reference's torch path on host cores."""
+    """Reference arm: the oracle port of the reference's torch path on host cores, or with
+    ``--ref-device cuda`` the same torch ops on the GPU (the reference selects its device with
+    ``torch.set_default_device``, evoxels/voxelgrid.py:156-189), eager or under torch.compile."""
     import oracle
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
     wl = args.workload
+    on_gpu = args.ref_device == "cuda"
+    if args.ref_compile and not on_gpu:
+        raise SystemExit("--ref-compile needs --ref-device cuda")
+    if on_gpu:
+        torch.set_default_device("cuda")
     if wl.startswith("batched"):
         rng = np.random.default_rng(4)
         sides = rng.choice([32, 48, 64, 96, 128], 64)
@@ -968,11 +981,16 @@ def run_reference(args, torch, warmup):
         def one():
             return oracle.rd_fe_run(u0, 1, 0.1 / 6, 1.0, (("dirichlet", (0, 0)), "neumann", "neumann"))
         sample = f"{n}^3: 1 forward-Euler step per bench step, fp32"
+    if args.ref_compile:
+        one, sample = _compiled_reference_step(torch, oracle, wl, shape, sample)
+    sync = torch.cuda.synchronize if on_gpu else (lambda: None)
     for _ in range(warmup):
         one()
+    sync()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         one()
+    sync()
     el = time.perf_counter() - t0
     units_ref = units if wl.startswith("batched") else n ** 3
     value = units_ref * args.steps / el
@@ -995,8 +1013,49 @@ def run_reference(args, torch, warmup):
                          "sample": sample},
         "e2e": {"value": round(value, 1), "unit": "voxel-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if on_gpu:
+        out["cpu_baseline"] = None
+        out["ref_device"] = "cuda"
+        out["gpu_torch_baseline"] = {"value": round(value, 1), "unit": "voxel-steps/s",
+                                     "mode": "torch.compile" if args.ref_compile else "eager",
+                                     "device": torch.cuda.get_device_name(0), "sample": sample}
     print(json.dumps(out))
     return 0
+
+
+def _compiled_reference_step(torch, oracle, wl, shape, sample):
+    """The Cahn-Hilliard IMEX step of the reference's torch path under torch.compile (its jit=True):
+    forward workloads step with it, forward + adjoint workloads add the VJP through it (dL/du, dL/dD,
+    dL/deps) as the eager arm's ch_imex_vjp does."""
+    fwd_only = wl in ("ch100_fwd", "ch512_fwd", "driver256")
+    if not fwd_only and wl not in ("ch256_fwd_adj", "ch128_inversion", "ch512_fwd_adj"):
+        raise SystemExit(f"--ref-compile covers the Cahn-Hilliard IMEX workloads, not {wl}")
+    k2 = oracle.rfft_k_squared(shape)
+    seed_u, seed_l = (1, None) if fwd_only else (6, 7)
+
+    def step_fn(u, Dt, et):
+        prefac = 0.1 / (1 - 0.1 * (-2 * et * Dt * 0.25 * k2 ** 2))
+        mh = lambda c, lib=None: 18 / et * c * (1 - c) * (1 - 2 * c)  # noqa: E731
+        return oracle.imex_step(u, prefac, lambda v: oracle.ch_rhs(v, et, Dt, None, (1.0, 1.0, 1.0), mh))
+    cstep = torch.compile(step_fn)
+    u0 = torch.tensor(oracle.seeded_ch_field(shape, seed_u), dtype=torch.float32).unsqueeze(0)
+    d0, e0 = torch.tensor(1.0), torch.tensor(3.0)
+    if fwd_only:
+        def one():
+            with torch.no_grad():
+                return cstep(u0, d0, e0)
+        return one, sample + " (torch.compile)"
+    lam = torch.tensor(oracle.seeded_unit_field(shape, seed_l) - 0.5, dtype=torch.float32).unsqueeze(0)
+
+    def one():
+        with torch.no_grad():
+            u1 = cstep(u0, d0, e0)
+        u = u0.detach().clone().requires_grad_(True)
+        Dt = torch.tensor(1.0, requires_grad=True)
+        et = torch.tensor(3.0, requires_grad=True)
+        torch.autograd.grad(cstep(u, Dt, et), (u, Dt, et), grad_outputs=lam)
+        return u1
+    return one, sample + " (torch.compile)"
 
 
 if __name__ == "__main__":
