@@ -542,23 +542,44 @@ class Batched:
         return 4 * self.b.total, 4 * self.b.total
 
     def plain(self, steps):
-        """Same work through the single-grid path, one instance at a time (ms per bench step)."""
+        """Same work through the single-grid path, one instance at a time (ms per bench step):
+        PseudoSpectralIMEX.advance, or for the adjoint workload CahnHilliardAdjoint's forward with
+        the trajectory (and the increment spectra where the grid has the x-pass) and its adjoint
+        with the parameter gradients."""
+        from evoxels_gb300.adjoint import CahnHilliardAdjoint
         from evoxels_gb300.problem_definition import CahnHilliard
         from evoxels_gb300.timesteppers import PseudoSpectralIMEX
         from evoxels_gb300.voxelfields import VoxelFields
         from evoxels_gb300.voxelgrid import VoxelGridGB300
         torch = self.torch
+        dev = self.u0.device
         runs = []
         for i, s in enumerate(self.shapes):
-            vg = VoxelGridGB300(VoxelFields(s, domain_size=s).grid_info(), device=self.u0.device)
-            st = PseudoSpectralIMEX(CahnHilliard(vg, eps=float(self.eps[i]), D=float(self.M[i]), mu_hom=self.pin), 0.1)
-            u = torch.tensor(self.fields[i], dtype=torch.float32, device=self.u0.device).unsqueeze(0)
-            runs.append((st, u))
+            vg = VoxelGridGB300(VoxelFields(s, domain_size=s).grid_info(), device=dev)
+            u = torch.tensor(self.fields[i], dtype=torch.float32, device=dev).unsqueeze(0)
+            if not self.adj:
+                st = PseudoSpectralIMEX(CahnHilliard(vg, eps=float(self.eps[i]), D=float(self.M[i]), mu_hom=self.pin),
+                                        0.1)
+                runs.append((st, u))
+                continue
+            r = CahnHilliardAdjoint(vg, 0.1, pinned_w=18 / 3.0)
+            traj = torch.empty((self.T + 1,) + s, dtype=torch.float32, device=dev)
+            traj[0] = u[0]
+            lam = torch.empty_like(u).uniform_(-1e-3, 1e-3)
+            runs.append((r, traj, r.new_spectra(self.T), lam, torch.zeros(3, dtype=torch.float64, device=dev),
+                         float(self.M[i]), float(self.eps[i])))
 
         def one():
-            for st, u in runs:
-                st.advance(u, self.T)
-        one()
+            if not self.adj:
+                for st, u in runs:
+                    st.advance(u, self.T)
+                return
+            for r, traj, spec, lam, g, d, e in runs:
+                r.forward(traj[0:1], self.T, d, e, traj=traj[1:], spectra=spec)
+                g.zero_()
+                r.adjoint(traj, self.T, lam, d, e, g, spec)
+        for _ in range(3):   # the third call replays the graphs the second one captured
+            one()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
@@ -859,11 +880,13 @@ def main():
                          "bytes_per_voxel_step": step_bytes // wl.units_per_step}
 
     vs_plain = None
-    if isinstance(wl, Batched) and not wl.adj:
+    if isinstance(wl, Batched):
         plain_ms = wl.plain(max(2, min(args.steps, 5)))
         vs_plain = {"plain_ms_per_step": round(plain_ms, 3), "plain_value": round(wl.units_per_step / (plain_ms / 1e3), 1),
                     "speedup": round(plain_ms / (ms / args.steps), 3),
-                    "plain_path": "single-grid PseudoSpectralIMEX.advance per instance, same GPU"}
+                    "plain_path": ("single-grid CahnHilliardAdjoint forward (trajectory, increment spectra) + "
+                                   "adjoint with parameter gradients per instance, same GPU" if wl.adj else
+                                   "single-grid PseudoSpectralIMEX.advance per instance, same GPU")}
     if isinstance(wl, Driver):
         t = wl.sync_reference()
         vs_plain = {"sync_output_s_per_solve": round(t[False], 4), "async_output_s_per_solve": round(t[True], 4),
