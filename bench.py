@@ -472,7 +472,8 @@ class FdForward:
 class Batched:
     """64 uneven periodic CH instances (sides from {32,48,64,96,128}, seed 4), per-instance
     mobility M ~ U[0.5,2] and kappa ~ U[0.5,3] (eps = kappa/2, bulk pinned to 18/3),
-    dt = 0.1; forward, or forward + adjoint with parameter gradients."""
+    dt = 0.1; forward, or forward (trajectory and increment spectra kept) + adjoint with
+    parameter gradients."""
 
     def __init__(self, torch, device, steps_per=50, adjoint=False, n_inst=64, autotune=True):
         from evoxels_gb300.batched import BatchedCahnHilliard, BatchTuning
@@ -510,6 +511,7 @@ class Batched:
                        "sides": sorted(set(int(a) for a in sides)), "total_voxels": self.n,
                        "steps_per_bench_step": self.T, "dt": 0.1, "M_range": [0.5, 2.0], "kappa_range": [0.5, 3.0],
                        "bulk": "pinned 18/3", "seed": 4, "tuning": tuned or "defaults",
+                       "stored_spectra": bool(adjoint),
                        "work_items": self.b.work_items,
                        "l2": "inputs larger than L2 (%.2f GB per packed field)" % (4 * self.b.total / 1e9)}
 
@@ -518,10 +520,13 @@ class Batched:
         if not self.adj:
             return b.forward(self.u0, self.T)
         t = b.total
+        spec = getattr(b, "_bench_spectra", None)
+        if spec is None:   # the stored increment spectra of the T steps (spectral parameter gradients)
+            spec = b._bench_spectra = b.new_spectra(self.T)
         self.states[:t].copy_(self.u0)
-        b.forward(self.states[:t], self.T, traj=self.states[t:])
+        b.forward(self.states[:t], self.T, traj=self.states[t:], spectra=spec)
         self.grads.zero_()
-        return b.adjoint(self.states, self.T, self.lam, self.grads)
+        return b.adjoint(self.states, self.T, self.lam, self.grads, spectra=spec)
 
     def prof_step(self):
         """The step without CUDA graphs, so every kernel gets its own timing events."""

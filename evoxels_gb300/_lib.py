@@ -110,6 +110,9 @@ _SIGS = {
     "evx_batch_offsets": (C.c_int, [_P, _P]),
     "evx_batch_forward": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, _P, _P]),
     "evx_batch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, _P, _P, _P]),
+    "evx_batch_spectrum_floats": (C.c_size_t, [_P]),
+    "evx_batch_forward_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, _P, _P, _P]),
+    "evx_batch_adjoint_spectra": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, _P, _P, _P]),
     "evx_mse_scratch_bytes": (C.c_size_t, [C.c_size_t]),
     "evx_nan_flag": (C.c_int, [_P, C.c_size_t, _P, _P]),
     "evx_mse_grad": (C.c_int, [_P, _P, C.c_size_t, _P, _P, _P, C.c_size_t, _P]),

@@ -119,26 +119,48 @@ class BatchedCahnHilliard:
         return [packed[o:o + n].view((1,) + s) for o, n, s in zip(self.offsets, self.sizes, self.shapes)]
 
     # ---- stepping --------------------------------------------------------------
-    def forward(self, u, nsteps, traj=None, nonfinite=None):
-        """``nsteps`` IMEX steps of every instance; ``traj`` (nsteps x total) receives u_1..u_n."""
+    def new_spectra(self, nsteps):
+        """Buffer for ``nsteps`` steps of stored increment spectra (every instance)."""
+        n = int(_lib.lib().evx_batch_spectrum_floats(self.handle))
+        return torch.empty(max(1, int(nsteps) * n), dtype=torch.float32, device=self.device)
+
+    def _check_spectra(self, spectra, nsteps):
+        n = int(_lib.lib().evx_batch_spectrum_floats(self.handle))
+        if spectra.dtype != torch.float32 or not spectra.is_contiguous() or spectra.numel() < int(nsteps) * n:
+            raise ValueError("spectra must be a contiguous float32 tensor from new_spectra(nsteps)")
+
+    def forward(self, u, nsteps, traj=None, nonfinite=None, spectra=None):
+        """``nsteps`` IMEX steps of every instance; ``traj`` (nsteps x total) receives u_1..u_n,
+        ``spectra`` (optional, from ``new_spectra``; needs ``traj``) each step's increment spectra."""
         self._check(u)
         out = torch.empty_like(u)
         if traj is not None:
             self._check(traj, nsteps)
-        _lib.check(_lib.lib().evx_batch_forward(self.handle, u.data_ptr(), out.data_ptr(), int(nsteps),
-                                                traj.data_ptr() if traj is not None else None,
-                                                nonfinite.data_ptr() if nonfinite is not None else None,
-                                                self.workspace.data_ptr(), cuda_stream()), "evx_batch_forward")
+        if spectra is not None:
+            self._check_spectra(spectra, nsteps)
+        _lib.check(_lib.lib().evx_batch_forward_spectra(self.handle, u.data_ptr(), out.data_ptr(), int(nsteps),
+                                                        traj.data_ptr() if traj is not None else None,
+                                                        spectra.data_ptr() if spectra is not None else None,
+                                                        nonfinite.data_ptr() if nonfinite is not None else None,
+                                                        self.workspace.data_ptr(), cuda_stream()),
+                   "evx_batch_forward_spectra")
         return out
 
-    def adjoint(self, states, nsteps, lam, grads=None):
-        """Adjoint through ``states`` ((nsteps+1) x total); ``grads`` (n x 3 float64) accumulates."""
+    def adjoint(self, states, nsteps, lam, grads=None, spectra=None):
+        """Adjoint through ``states`` ((nsteps+1) x total); ``grads`` (n x 3 float64) accumulates.
+        ``spectra``: the forward's stored spectra of the same steps (the mobility gradient sums then
+        come from k-space by Parseval)."""
         self._check(states, nsteps + 1)
         self._check(lam)
+        if spectra is not None:
+            self._check_spectra(spectra, nsteps)
         out = torch.empty_like(lam)
-        _lib.check(_lib.lib().evx_batch_adjoint(self.handle, states.data_ptr(), int(nsteps), lam.data_ptr(),
-                                                out.data_ptr(), grads.data_ptr() if grads is not None else None,
-                                                self.workspace.data_ptr(), cuda_stream()), "evx_batch_adjoint")
+        _lib.check(_lib.lib().evx_batch_adjoint_spectra(self.handle, states.data_ptr(),
+                                                        spectra.data_ptr() if spectra is not None else None,
+                                                        int(nsteps), lam.data_ptr(), out.data_ptr(),
+                                                        grads.data_ptr() if grads is not None else None,
+                                                        self.workspace.data_ptr(), cuda_stream()),
+                   "evx_batch_adjoint_spectra")
         return out
 
     def param_grads(self, grads):

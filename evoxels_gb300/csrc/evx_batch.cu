@@ -32,23 +32,28 @@ namespace {
 
 struct KInst {          // k-space descriptor of one instance
     long long soff;     // spectrum offset (complex values)
-    int nx, ny, nzh;
+    long long doff;     // stored increment spectrum offset (complex values)
+    int nx, ny, nzh, nz;
     int kx, ky, kz;     // offsets of the k^2 tables
     float sym_coef, dt, invN;
     int xmode;          // 1: its group's multiply is done by the x-pass
+    int xoff;           // first partial-sum slot of the spectral adjoint's blocks
 };
 
 struct RInst {          // gradient-reduction descriptor of one instance
-    int part0, nparts, orig, pad;
-    double kA, DA;      // kappa*A and D*A
+    int part0, nparts, orig, xpart0, nxpart, pad;
+    double kA, DA, invD;   // kappa*A, D*A, 1/D
 };
 
+// With dspec the multiplied spectrum (the step's increment spectrum) is also
+// stored there, at the instance's doff.
 __global__ void batch_kspace_fwd_kernel(float2* __restrict__ spec, const KInst* __restrict__ ki,
-                                        const float* __restrict__ k2) {
+                                        const float* __restrict__ k2, float2* __restrict__ dspec) {
     const KInst K = ki[blockIdx.y];
     if (K.xmode) return;   // uniform in the block
     const size_t total = (size_t)K.nx * K.ny * K.nzh;
     float2* s = spec + K.soff;
+    float2* ds = dspec ? dspec + K.doff : nullptr;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
         const int k = (int)(e % K.nzh);
@@ -60,6 +65,54 @@ __global__ void batch_kspace_fwd_kernel(float2* __restrict__ spec, const KInst* 
         v.x = __fmul_rn(__fmul_rn(v.x, pre), K.invN);
         v.y = __fmul_rn(__fmul_rn(v.y, pre), K.invN);
         s[e] = v;
+        if (ds) ds[e] = v;
+    }
+}
+
+// Spectral adjoint of the k-space groups: g-hat = prefac/N * lam-hat, and the
+// Parseval sums t1 = sum wz Re(lam-hat conj dU), t2 = sum wz prefac k^4 Re(...)
+// against the stored increment spectrum dU (wz = 1 on the kz = 0 and nz/2
+// planes, 2 elsewhere), per block in double into xpart[2*(xoff + block)].
+__global__ void batch_kspace_adj_spec_kernel(float2* __restrict__ spec, const float2* __restrict__ dspec,
+                                             double* __restrict__ xpart, const KInst* __restrict__ ki,
+                                             const float* __restrict__ k2) {
+    __shared__ double red[2][8];
+    const KInst K = ki[blockIdx.y];
+    if (K.xmode) return;   // uniform in the block
+    const size_t total = (size_t)K.nx * K.ny * K.nzh;
+    float2* s = spec + K.soff;
+    const float2* ds = dspec + K.doff;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    float t1 = 0.f, t2 = 0.f;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
+        const int k = (int)(e % K.nzh);
+        const size_t t = e / K.nzh;
+        const int j = (int)(t % K.ny), i = (int)(t / K.ny);
+        const float kk = (__ldg(k2 + K.kx + i) + __ldg(k2 + K.ky + j)) + __ldg(k2 + K.kz + k);
+        const float k4 = kk * kk;
+        const float pre = K.dt / (1.f - K.dt * (K.sym_coef * k4));
+        const float sg = pre * K.invN;
+        const float2 v = s[e], d = __ldg(ds + e);
+        const float wz = (k == 0 || 2 * k == K.nz) ? 1.f : 2.f;
+        const float re = wz * (v.x * d.x + v.y * d.y);
+        t1 += re;
+        t2 += re * (pre * k4);
+        s[e] = make_float2(v.x * sg, v.y * sg);
+    }
+    double a = t1, b = t2;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { red[0][w] = a; red[1][w] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sa = 0.0, sb = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { sa += red[0][q]; sb += red[1][q]; }
+        double* o = xpart + (size_t)(K.xoff + blockIdx.x) * 2;
+        o[0] = sa;
+        o[1] = sb;
     }
 }
 
@@ -124,6 +177,38 @@ __global__ void batch_grad_reduce_kernel(const double* __restrict__ part, const 
     }
 }
 
+// Spectral variant: the pullback's two real-space sums (slots 1, 2 of each
+// work item) and the Parseval sums t1, t2 of the instance's x-pass or k-space
+// blocks: dL/dD += t1/D - kappa*A*t2, dL/dkappa += sK - D*A*t2, dL/dw += sW.
+__global__ void batch_grad_reduce_spec_kernel(const double* __restrict__ part, const double* __restrict__ xpart,
+                                              const RInst* __restrict__ ri, double* __restrict__ grads) {
+    __shared__ double s[4][256];
+    const RInst R = ri[blockIdx.x];
+    const int t = threadIdx.x;
+    double a[4] = {0.0, 0.0, 0.0, 0.0};   // sK, sW, t1, t2
+    for (int b = t; b < R.nparts; b += 256) {
+        a[0] += part[(size_t)(R.part0 + b) * 4 + 1];
+        a[1] += part[(size_t)(R.part0 + b) * 4 + 2];
+    }
+    for (int b = t; b < R.nxpart; b += 256) {
+        a[2] += xpart[(size_t)(R.xpart0 + b) * 2];
+        a[3] += xpart[(size_t)(R.xpart0 + b) * 2 + 1];
+    }
+    for (int q = 0; q < 4; ++q) s[q][t] = a[q];
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o)
+            for (int q = 0; q < 4; ++q) s[q][t] += s[q][t + o];
+        __syncthreads();
+    }
+    if (t == 0) {
+        double* g = grads + (size_t)R.orig * 3;
+        g[0] += s[2][0] * R.invD - R.kA * s[3][0];
+        g[1] += s[0][0] - R.DA * s[3][0];
+        g[2] += s[1][0];
+    }
+}
+
 size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 }  // namespace
@@ -164,8 +249,10 @@ struct evx_batch {
     float* d_k2 = nullptr;
     size_t ws_fft = 0;
     size_t off_fft = 0, off_r = 0, off_upd = 0, off_spec = 0, off_ua = 0, off_ub = 0, off_lam = 0, off_part = 0,
-           off_cnt = 0, total_ws = 0;
-    int grid_rhs = 0, grid_pb[2] = {0, 0};
+           off_xpart = 0, off_cnt = 0, total_ws = 0;
+    int grid_rhs = 0, grid_pb[3] = {0, 0, 0};
+    size_t spec_floats = 0;                // floats of one step's stored increment spectra (all instances)
+    size_t n_xpart = 0;                    // Parseval partial-sum slots of the spectral adjoint
     cudaStream_t cap = nullptr;
     cudaGraphExec_t gexec = nullptr;
     const void* gexec_ws = nullptr;
@@ -246,35 +333,40 @@ int batch_c2r(evx_batch* b, float2* in, float* out, cudaStream_t st) {
     return EVX_OK;
 }
 
-// x-pass of every power-of-two group: mode 0 forward, 1 adjoint g, 2 adjoint g and h
-int batch_xpass(evx_batch* b, int mode, float2* spec, float2* spec_h, cudaStream_t st) {
+// x-pass of every power-of-two group: mode 0 forward (dspec: store the increment
+// spectra), 1 adjoint g, 2 adjoint g and h, 3 adjoint g with the Parseval sums
+int batch_xpass(evx_batch* b, int mode, float2* spec, float2* spec_h, cudaStream_t st, float2* dspec = nullptr,
+                double* xpart = nullptr) {
     for (auto& g : b->groups) {
         if (!g.xmode) continue;
         int rc = xpass_batch_launch(mode, g.nx, spec, spec_h, b->d_xb + g.first, g.count, g.ny * g.nzh, g.nzh, g.nz,
-                                    b->d_k2 + g.k2x, b->d_k2 + g.k2y, b->d_k2 + g.k2z, st, g.zt ? g.ny : 0);
+                                    b->d_k2 + g.k2x, b->d_k2 + g.k2y, b->d_k2 + g.k2z, st, g.zt ? g.ny : 0, dspec,
+                                    xpart);
         if (rc) return rc;
     }
     return EVX_OK;
 }
 
-// One IMEX step's spectral part: r -> upd
-int batch_spectral(evx_batch* b, float* r, float2* spec, float* upd, cudaStream_t st) {
+// One IMEX step's spectral part: r -> upd; dspec (optional) receives the step's
+// increment spectra
+int batch_spectral(evx_batch* b, float* r, float2* spec, float* upd, cudaStream_t st, float2* dspec = nullptr) {
     int rc;
     if ((rc = batch_r2c(b, r, spec, st))) return rc;
     if (b->any_kspace) {
         EVX_TIMED("batch_kspace_fwd", st,
-                  batch_kspace_fwd_kernel<<<dim3(b->kspace_blocks, b->n), 256, 0, st>>>(spec, b->d_kinst, b->d_k2));
+                  batch_kspace_fwd_kernel<<<dim3(b->kspace_blocks, b->n), 256, 0, st>>>(spec, b->d_kinst, b->d_k2,
+                                                                                      dspec));
         count_launch();
         if ((rc = check_launch("batch_kspace_fwd_kernel"))) return rc;
     }
-    if ((rc = batch_xpass(b, 0, spec, nullptr, st))) return rc;
+    if ((rc = batch_xpass(b, 0, spec, nullptr, st, dspec))) return rc;
     return batch_c2r(b, spec, upd, st);
 }
 
 struct Bufs {
     float *r, *upd, *ua, *ub, *lam;
     float2* spec;
-    double* part;
+    double *part, *xpart;
     int* cnt;
 };
 
@@ -287,14 +379,15 @@ Bufs bufs(evx_batch* b, void* ws) {
     o.ub = reinterpret_cast<float*>(ws_at(ws, b->off_ub));
     o.lam = reinterpret_cast<float*>(ws_at(ws, b->off_lam));
     o.part = reinterpret_cast<double*>(ws_at(ws, b->off_part));
+    o.xpart = reinterpret_cast<double*>(ws_at(ws, b->off_xpart));
     o.cnt = reinterpret_cast<int*>(ws_at(ws, b->off_cnt));
     return o;
 }
 
-int fused_step(evx_batch* b, const Bufs& B, const float* src, float* dst, cudaStream_t st) {
+int fused_step(evx_batch* b, const Bufs& B, const float* src, float* dst, cudaStream_t st, float2* dspec = nullptr) {
     int rc = batch_rhs_launch(true, src, B.upd, dst, B.r, b->d_inst, b->d_items, b->n_items, B.cnt, b->grid_rhs, st);
     if (rc) return rc;
-    return batch_spectral(b, B.r, B.spec, B.upd, st);
+    return batch_spectral(b, B.r, B.spec, B.upd, st, dspec);
 }
 
 // Capture `steps` (even) fused steps A->B->A... on the internal stream.
@@ -437,6 +530,9 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
         }
     }
     b->ws_fft = wmax;
+    size_t maxspec = 0;
+    for (auto& g : b->groups) maxspec = std::max(maxspec, g.nspec);
+    b->kspace_blocks = (int)std::max<size_t>(1, std::min<size_t>(256, (maxspec + 2047) / 2048));
     // work items, k-space and reduction descriptors, k^2 tables
     std::vector<BatchInst> hinst(n);
     std::vector<KInst> hk(n);
@@ -447,6 +543,7 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
         for (int k = 0; k < b->groups[gi].count; ++k) group_of[b->groups[gi].first + k] = (int)gi;
     std::vector<BatchItem> items;
     std::vector<float> k2;
+    size_t doff = 0, xoff = 0;   // stored-spectrum offsets (complex) and partial-sum slots, internal order
     std::map<std::tuple<int, int, int, double, double, double>, int> k2pos;
     for (int ii = 0; ii < n; ++ii) {
         const int i = b->order[ii];
@@ -475,6 +572,8 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
         hr[ii].orig = i;
         hr[ii].kA = (double)s.params.kappa * s.params.A;
         hr[ii].DA = (double)s.params.D * s.params.A;
+        hr[ii].invD = 1.0 / (double)s.params.D;
+        hr[ii].pad = 0;
         const auto kk = std::make_tuple(s.nx, s.ny, s.nz, s.h[0], s.h[1], s.h[2]);
         if (!k2pos.count(kk)) {
             k2pos[kk] = (int)k2.size();
@@ -493,13 +592,25 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
         hk[ii].invN = (float)(1.0 / ((double)s.nx * s.ny * s.nz));
         evx_batch::Group& grp = b->groups[group_of[ii]];
         hk[ii].xmode = grp.xmode ? 1 : 0;
+        hk[ii].nz = s.nz;
         grp.k2x = hk[ii].kx; grp.k2y = hk[ii].ky; grp.k2z = hk[ii].kz;
         hxb[ii].soff = soff_of[ii];
         hxb[ii].sym = s.params.sym_coef;
         hxb[ii].dt = s.params.dt;
         hxb[ii].invN = hk[ii].invN;
-        hxb[ii].pad = 0;
+        // the stored spectrum: the x-pass tile layout ([tile][element][thread]) or the k-space layout
+        const int Mx = s.ny * (s.nz / 2 + 1);
+        const size_t dsz = grp.xmode ? xpass_spectrum_floats(s.nx, Mx) / 2 : (size_t)s.nx * s.ny * (s.nz / 2 + 1);
+        const size_t xsl = grp.xmode ? xpass_blocks(s.nx, Mx) : (size_t)b->kspace_blocks;
+        hxb[ii].doff = hk[ii].doff = (long long)doff;
+        hxb[ii].xoff = hk[ii].xoff = (int)xoff;
+        hr[ii].xpart0 = (int)xoff;
+        hr[ii].nxpart = (int)xsl;
+        doff += (dsz + 1) & ~(size_t)1;   // 16-byte aligned starts
+        xoff += xsl;
     }
+    b->spec_floats = 2 * doff;
+    b->n_xpart = xoff;
     // largest work items first (longest-processing-time order for the persistent blocks)
     std::stable_sort(items.begin(), items.end(), [&](const BatchItem& a, const BatchItem& c) {
         auto cost = [&](const BatchItem& x) {
@@ -537,11 +648,7 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     auto bps = [&](int occ) { return b->tune.blocks_per_sm > 0 ? std::min(b->tune.blocks_per_sm, occ) : occ; };
     b->grid_rhs = bps(batch_rhs_blocks_per_sm()) * sms;
-    b->grid_pb[0] = bps(batch_pullback_blocks_per_sm(false)) * sms;
-    b->grid_pb[1] = bps(batch_pullback_blocks_per_sm(true)) * sms;
-    size_t maxspec = 0;
-    for (auto& g : b->groups) maxspec = std::max(maxspec, g.nspec);
-    b->kspace_blocks = (int)std::max<size_t>(1, std::min<size_t>(256, (maxspec + 2047) / 2048));
+    for (int gr = 0; gr < 3; ++gr) b->grid_pb[gr] = bps(batch_pullback_blocks_per_sm(gr)) * sms;
     // workspace layout
     size_t o = 0;
     b->off_fft = o;  o += al256(b->ws_fft);
@@ -552,6 +659,7 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
     b->off_ub = o;   o += al256(b->total * sizeof(float));
     b->off_lam = o;  o += al256(b->total * sizeof(float));
     b->off_part = o; o += al256((size_t)b->n_items * 4 * sizeof(double));
+    b->off_xpart = o; o += al256(std::max<size_t>(1, b->n_xpart) * 2 * sizeof(double));
     b->off_cnt = o;  o += 256;
     b->total_ws = o;
     *out = b;
@@ -573,35 +681,47 @@ int evx_batch_offsets(const evx_batch* b, int64_t* offsets) {
     return EVX_OK;
 }
 
+size_t evx_batch_spectrum_floats(const evx_batch* b) { return b ? b->spec_floats : 0; }
+
 int evx_batch_forward(evx_batch* b, const float* u_in, float* u_out, int nsteps, float* traj, int* nonfinite,
                       void* ws, void* stream) {
+    return evx_batch_forward_spectra(b, u_in, u_out, nsteps, traj, nullptr, nonfinite, ws, stream);
+}
+
+int evx_batch_forward_spectra(evx_batch* b, const float* u_in, float* u_out, int nsteps, float* traj, float* spectra,
+                              int* nonfinite, void* ws, void* stream) {
     if (!b) return fail(EVX_ERR_BAD_ARG, "batch is NULL");
     if (!u_in || !u_out || !ws) return fail(EVX_ERR_BAD_ARG, "NULL buffer");
     if (u_in == u_out) return fail(EVX_ERR_BAD_ARG, "input and output must not alias");
-    if (((reinterpret_cast<uintptr_t>(u_in) | reinterpret_cast<uintptr_t>(u_out) | reinterpret_cast<uintptr_t>(traj)) &
-         15) || (reinterpret_cast<uintptr_t>(ws) & 255))
+    if (((reinterpret_cast<uintptr_t>(u_in) | reinterpret_cast<uintptr_t>(u_out) | reinterpret_cast<uintptr_t>(traj) |
+          reinterpret_cast<uintptr_t>(spectra)) & 15) || (reinterpret_cast<uintptr_t>(ws) & 255))
         return fail(EVX_ERR_BAD_ARG, "buffers must be 16-byte aligned (workspace 256-byte)");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
+    if (spectra && !traj) return fail(EVX_ERR_BAD_ARG, "stored spectra are kept with the trajectory only");
     const size_t T = b->total;
     if (nsteps == 0)
         return check_cuda(cudaMemcpyAsync(u_out, u_in, T * sizeof(float), cudaMemcpyDeviceToDevice, as_stream(stream)),
                           "copy");
-    const GraphKey key{3, key_p(u_in), key_p(u_out), (uint64_t)nsteps, key_p(traj), key_p(nonfinite), key_p(ws)};
+    const GraphKey key{3, key_p(u_in), key_p(u_out), (uint64_t)nsteps, key_p(traj), key_p(spectra), key_p(nonfinite),
+                       key_p(ws)};
     return b->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
     int rc;
     if ((rc = bind_plans(b, ws, st))) return rc;
     const Bufs B = bufs(b, ws);
     const float* src = u_in;
+    auto dspec = [&](int s) {
+        return spectra ? reinterpret_cast<float2*>(spectra + (size_t)s * b->spec_floats) : nullptr;
+    };
     // step 0 from the input
     if ((rc = batch_rhs_launch(false, u_in, nullptr, nullptr, B.r, b->d_inst, b->d_items, b->n_items, B.cnt,
                                b->grid_rhs, st)))
         return rc;
-    if ((rc = batch_spectral(b, B.r, B.spec, B.upd, st))) return rc;
+    if ((rc = batch_spectral(b, B.r, B.spec, B.upd, st, dspec(0)))) return rc;
     int s = 1;
     if (traj) {
         for (; s < nsteps; ++s) {
             float* dst = traj + (size_t)(s - 1) * T;
-            if ((rc = fused_step(b, B, src, dst, st))) return rc;
+            if ((rc = fused_step(b, B, src, dst, st, dspec(s)))) return rc;
             src = dst;
         }
     } else {
@@ -642,18 +762,25 @@ int evx_batch_forward(evx_batch* b, const float* u_in, float* u_out, int nsteps,
 
 int evx_batch_adjoint(evx_batch* b, const float* states, int nsteps, const float* lam_in, float* lam_out,
                       double* grads, void* ws, void* stream) {
+    return evx_batch_adjoint_spectra(b, states, nullptr, nsteps, lam_in, lam_out, grads, ws, stream);
+}
+
+int evx_batch_adjoint_spectra(evx_batch* b, const float* states, const float* spectra, int nsteps,
+                              const float* lam_in, float* lam_out, double* grads, void* ws, void* stream) {
     if (!b) return fail(EVX_ERR_BAD_ARG, "batch is NULL");
     if (!lam_in || !lam_out || !ws || (!states && nsteps > 0)) return fail(EVX_ERR_BAD_ARG, "NULL buffer");
     if (lam_in == lam_out) return fail(EVX_ERR_BAD_ARG, "lam_in and lam_out must not alias");
     if (((reinterpret_cast<uintptr_t>(lam_in) | reinterpret_cast<uintptr_t>(lam_out) |
-          reinterpret_cast<uintptr_t>(states)) & 15) || (reinterpret_cast<uintptr_t>(ws) & 255))
+          reinterpret_cast<uintptr_t>(states) | reinterpret_cast<uintptr_t>(spectra)) & 15) ||
+        (reinterpret_cast<uintptr_t>(ws) & 255))
         return fail(EVX_ERR_BAD_ARG, "buffers must be 16-byte aligned (workspace 256-byte)");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
     const size_t T = b->total;
     if (nsteps == 0)
         return check_cuda(cudaMemcpyAsync(lam_out, lam_in, T * sizeof(float), cudaMemcpyDeviceToDevice,
                                           as_stream(stream)), "copy");
-    const GraphKey key{4, key_p(states), (uint64_t)nsteps, key_p(lam_in), key_p(lam_out), key_p(grads), key_p(ws)};
+    const GraphKey key{4, key_p(states), key_p(spectra), (uint64_t)nsteps, key_p(lam_in), key_p(lam_out),
+                       key_p(grads), key_p(ws)};
     return b->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
     int rc;
     if ((rc = bind_plans(b, ws, st))) return rc;
@@ -662,10 +789,33 @@ int evx_batch_adjoint(evx_batch* b, const float* states, int nsteps, const float
     float* hbuf = B.r + T;
     float2* spec_h = B.spec + b->total_spec;
     const bool want = grads != nullptr;
+    const bool spectral = want && spectra != nullptr;   // gradient sums by Parseval against the stored spectra
     const float* lam = lam_in;
     for (int s = nsteps - 1; s >= 0; --s) {
         float* dst = (s % 2 == 0) ? lam_out : B.lam;
         if ((rc = batch_r2c(b, lam, B.spec, st))) return rc;
+        if (spectral) {
+            float2* ds = reinterpret_cast<float2*>(const_cast<float*>(spectra) + (size_t)s * b->spec_floats);
+            if (b->any_kspace) {
+                EVX_TIMED("batch_kspace_adj_spec", st,
+                          batch_kspace_adj_spec_kernel<<<dim3(b->kspace_blocks, b->n), 256, 0, st>>>(
+                              B.spec, ds, B.xpart, b->d_kinst, b->d_k2));
+                count_launch();
+                if ((rc = check_launch("batch_kspace_adj_spec_kernel"))) return rc;
+            }
+            if ((rc = batch_xpass(b, 3, B.spec, nullptr, st, ds, B.xpart))) return rc;
+            if ((rc = batch_c2r(b, B.spec, gbuf, st))) return rc;
+            const float* us = states + (size_t)s * T;
+            if ((rc = batch_pullback_launch(2, us, gbuf, lam, nullptr, nullptr, dst, B.part, b->d_inst, b->d_items,
+                                            b->n_items, B.cnt + 1, b->grid_pb[2], st)))
+                return rc;
+            EVX_TIMED("batch_grad_reduce", st, batch_grad_reduce_spec_kernel<<<b->n, 256, 0, st>>>(
+                                                   B.part, B.xpart, b->d_rinst, grads));
+            count_launch();
+            if ((rc = check_launch("batch_grad_reduce_spec_kernel"))) return rc;
+            lam = dst;
+            continue;
+        }
         if (b->any_kspace) {
             EVX_TIMED("batch_kspace_adj", st,
                       batch_kspace_adj_kernel<<<dim3(b->kspace_blocks, b->n), 256, 0, st>>>(
@@ -677,7 +827,7 @@ int evx_batch_adjoint(evx_batch* b, const float* states, int nsteps, const float
         if ((rc = batch_c2r(b, B.spec, gbuf, st))) return rc;
         if (want && (rc = batch_c2r(b, spec_h, hbuf, st))) return rc;
         const float* us = states + (size_t)s * T;
-        if ((rc = batch_pullback_launch(want, us, gbuf, lam, hbuf, us + T, dst, B.part, b->d_inst, b->d_items,
+        if ((rc = batch_pullback_launch(want ? 1 : 0, us, gbuf, lam, hbuf, us + T, dst, B.part, b->d_inst, b->d_items,
                                         b->n_items, B.cnt + 1, b->grid_pb[want ? 1 : 0], st)))
             return rc;
         if (want) {

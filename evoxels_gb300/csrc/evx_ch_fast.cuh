@@ -191,10 +191,12 @@ struct BatchItem {
 };
 int batch_rhs_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const BatchInst* insts,
                      const BatchItem* items, int n_items, int* counter, int grid, cudaStream_t st);
-int batch_pullback_launch(bool grads, const float* u, const float* g, const float* lam, const float* h,
+// grads: 0 none, 1 the four real-space gradient sums (h and u1 read), 2 the two
+// real-space sums of the spectral-gradient path
+int batch_pullback_launch(int grads, const float* u, const float* g, const float* lam, const float* h,
                           const float* u1, float* lam_out, double* part, const BatchInst* insts,
                           const BatchItem* items, int n_items, int* counter, int grid, cudaStream_t st);
 int batch_rhs_blocks_per_sm();
-int batch_pullback_blocks_per_sm(bool grads);
+int batch_pullback_blocks_per_sm(int grads);
 
 }  // namespace evx

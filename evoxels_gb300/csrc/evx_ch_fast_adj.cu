@@ -454,7 +454,9 @@ __device__ __forceinline__ Geo batch_geo(const BatchInst& B) {
 
 // Persistent batched pullback; with GRADS each work item writes its partial sums
 // to part[item*4 .. item*4+3].
-template <bool GRADS>
+// GR as pullback_tile: 0 none, 1 all four gradient sums (reads h and u1), 2 the
+// two real-space sums of the spectral-gradient path
+template <int GR>
 __global__ void __launch_bounds__(THREADS, 2)
 ch_pullback_batch_kernel(const float* __restrict__ u, const float* __restrict__ gfield, const float* __restrict__ lam,
                          const float* __restrict__ hfield, const float* __restrict__ u1, float* __restrict__ lam_out,
@@ -478,20 +480,20 @@ ch_pullback_batch_kernel(const float* __restrict__ u, const float* __restrict__ 
         const size_t o = (size_t)B.off;
         float sD = 0.f, sK = 0.f, sW = 0.f, sH = 0.f;
         if (B.tile == 0)
-            pullback_tile<TileWide, GRADS ? 1 : 0, false>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
-                                           GRADS ? u1 + o : nullptr, lam_out + o, G, B.P, I.k0, I.j0, I.x0, I.x1, cs,
-                                           gs, ms, bs, sD, sK, sW, sH);
+            pullback_tile<TileWide, GR, false>(u + o, gfield + o, lam + o, GR == 1 ? hfield + o : nullptr,
+                                               GR == 1 ? u1 + o : nullptr, lam_out + o, G, B.P, I.k0, I.j0, I.x0, I.x1,
+                                               cs, gs, ms, bs, sD, sK, sW, sH);
         else
-            pullback_tile<TileSquare, GRADS ? 1 : 0, false>(u + o, gfield + o, lam + o, GRADS ? hfield + o : nullptr,
-                                             GRADS ? u1 + o : nullptr, lam_out + o, G, B.P, I.k0, I.j0, I.x0, I.x1,
-                                             cs, gs, ms, bs, sD, sK, sW, sH);
-        if (GRADS) block_reduce4(sD, sK, sW, sH, red, part + (size_t)I.part * 4);
+            pullback_tile<TileSquare, GR, false>(u + o, gfield + o, lam + o, GR == 1 ? hfield + o : nullptr,
+                                                 GR == 1 ? u1 + o : nullptr, lam_out + o, G, B.P, I.k0, I.j0, I.x0,
+                                                 I.x1, cs, gs, ms, bs, sD, sK, sW, sH);
+        if (GR) block_reduce4(sD, sK, sW, sH, red, part + (size_t)I.part * 4);
         __syncthreads();   // shared memory and s_item are reused by the next item
     }
 }
 
 int g_bps[2][3] = {{0, 0, 0}, {0, 0, 0}};   // [tile variant][gradient mode]
-int g_batch_bps[2] = {0, 0};
+int g_batch_bps[3] = {0, 0, 0};
 int g_sms = 0;
 
 void init_occupancy() {
@@ -510,8 +512,9 @@ void init_occupancy() {
     setup(ch_pullback_fast_kernel<TileSquare, 0>, &g_bps[1][0]);
     setup(ch_pullback_fast_kernel<TileSquare, 1>, &g_bps[1][1]);
     setup(ch_pullback_fast_kernel<TileSquare, 2>, &g_bps[1][2]);
-    setup(ch_pullback_batch_kernel<false>, &g_batch_bps[0]);
-    setup(ch_pullback_batch_kernel<true>, &g_batch_bps[1]);
+    setup(ch_pullback_batch_kernel<0>, &g_batch_bps[0]);
+    setup(ch_pullback_batch_kernel<1>, &g_batch_bps[1]);
+    setup(ch_pullback_batch_kernel<2>, &g_batch_bps[2]);
 }
 
 // One wave of blocks over equal segments of the tile-major (tile, x) plane
@@ -577,25 +580,29 @@ int ch_pullback_fast_launch(int grads, const float* u, const float* g, const flo
                                  sink);
 }
 
-int batch_pullback_blocks_per_sm(bool grads) {
+int batch_pullback_blocks_per_sm(int grads) {
     init_occupancy();
-    return g_batch_bps[grads ? 1 : 0];
+    return g_batch_bps[grads < 0 ? 0 : (grads > 2 ? 2 : grads)];
 }
 
-int batch_pullback_launch(bool grads, const float* u, const float* g, const float* lam, const float* h,
+int batch_pullback_launch(int grads, const float* u, const float* g, const float* lam, const float* h,
                           const float* u1, float* lam_out, double* part, const BatchInst* insts,
                           const BatchItem* items, int n_items, int* counter, int grid, cudaStream_t st) {
     init_occupancy();
     int rc = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), st), "batch pullback counter reset");
     if (rc) return rc;
-    if (grads)
+    if (grads == 1)
         EVX_TIMED("batch_pullback_grads", st,
-                  ch_pullback_batch_kernel<true><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, insts,
-                                                                                  items, n_items, counter));
+                  ch_pullback_batch_kernel<1><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, insts,
+                                                                               items, n_items, counter));
+    else if (grads == 2)
+        EVX_TIMED("batch_pullback_grads_spec", st,
+                  ch_pullback_batch_kernel<2><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
+                                                                               part, insts, items, n_items, counter));
     else
         EVX_TIMED("batch_pullback", st,
-                  ch_pullback_batch_kernel<false><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
-                                                                                   nullptr, insts, items, n_items, counter));
+                  ch_pullback_batch_kernel<0><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
+                                                                               nullptr, insts, items, n_items, counter));
     count_launch();
     return check_launch("ch_pullback_batch_kernel");
 }

@@ -89,13 +89,16 @@ struct XpassArgs {
 struct XBatchInst {
     long long soff;    // complex values
     float sym, dt, invN;
-    int pad;
+    int xoff;          // first partial-sum slot (pairs of doubles) of the instance's blocks
+    long long doff;    // stored increment spectrum offset (complex values)
 };
 bool xpass_supported(int nx);
-// mode 0 forward, 1 adjoint g, 2 adjoint g and h (spec_h, same offsets); per-tile kernel
+// mode 0 forward (optional store of the increment spectra to dspec), 1 adjoint g,
+// 2 adjoint g and h (spec_h, same offsets), 3 adjoint g with the Parseval sums
+// against dspec into xpart; per-tile kernel, per-instance offsets from xb
 int xpass_batch_launch(int mode, int nx, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M,
                        int nzh, int nz, const float* kx2, const float* ky2, const float* kz2, cudaStream_t st,
-                       int nyk = 0);
+                       int nyk = 0, float2* dspec = nullptr, double* xpart = nullptr);
 size_t xpass_blocks(int nx, int M);
 size_t xpass_spectrum_floats(int nx, int M);
 int xpass_launch(const XpassArgs& a, cudaStream_t st);

@@ -167,6 +167,8 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
         const XBatchInst X = xb[blockIdx.y];
         spec += X.soff;
         if (spec_h) spec_h += X.soff;
+        if (dspec) dspec += X.doff;
+        if (xpart) xpart += (size_t)X.xoff * 2;
         sym_coef = X.sym;
         dt = X.dt;
         invN = X.invN;
@@ -520,11 +522,12 @@ size_t xpass_spectrum_floats(int nx, int M) {
 
 template <int N1, int N2>
 int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M, int nzh, int nz,
-                  const float* kx2, const float* ky2, const float* kz2, cudaStream_t st, int nyk) {
+                  const float* kx2, const float* ky2, const float* kz2, cudaStream_t st, int nyk, float2* dspec,
+                  double* xpart) {
     constexpr int P = 256 / N2;
     const size_t smem = (size_t)N1 * N2 * P * sizeof(float2);
     const dim3 grid((M + P - 1) / P, count);
-    static bool attr[3] = {false, false, false};   // per mode of this (N1, N2)
+    static bool attr[4] = {false, false, false, false};   // per mode of this (N1, N2)
     auto go = [&](auto kern, const char* slot) {
         if (!attr[mode]) {
             const int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -532,34 +535,38 @@ int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, 
             if (rc) return rc;
             attr[mode] = true;
         }
-        EVX_TIMED(slot, st, (kern<<<grid, 256, smem, st>>>(spec, spec_h, nullptr, nullptr, M, nzh, nz, kx2, ky2, kz2,
+        EVX_TIMED(slot, st, (kern<<<grid, 256, smem, st>>>(spec, spec_h, dspec, xpart, M, nzh, nz, kx2, ky2, kz2,
                                                            0.f, 0.f, 0.f, xb, nullptr, nyk)));
         count_launch();
         return check_launch("xpass_kernel (batched)");
     };
     switch (mode) {
-        case 0: return go(xpass_kernel<N1, N2, 0>, "batch_xpass_fwd");
+        case 0: return go(xpass_kernel<N1, N2, 0>, dspec ? "batch_xpass_fwd_store" : "batch_xpass_fwd");
         case 1: return go(xpass_kernel<N1, N2, 1>, "batch_xpass_adj");
-        default: return go(xpass_kernel<N1, N2, 2>, "batch_xpass_adj");
+        case 2: return go(xpass_kernel<N1, N2, 2>, "batch_xpass_adj");
+        default: return go(xpass_kernel<N1, N2, 3>, "batch_xpass_adj_spec");
     }
 }
 
 int xpass_batch_launch(int mode, int nx, float2* spec, float2* spec_h, const XBatchInst* xb, int count, int M,
                        int nzh, int nz, const float* kx2, const float* ky2, const float* kz2, cudaStream_t st,
-                       int nyk) {
+                       int nyk, float2* dspec, double* xpart) {
     int rc = xpass_init();
     if (rc) return rc;
     if (count < 1 || count > 65535) return fail(EVX_ERR_BAD_ARG, "batched x-pass: %d instances", count);
-    if (mode < 0 || mode > 2) return fail(EVX_ERR_BAD_ARG, "batched x-pass mode %d", mode);
-    if (mode == 2 && !spec_h) return fail(EVX_ERR_BAD_ARG, "x-pass mode 2 is missing a buffer");
+    if (mode < 0 || mode > 3) return fail(EVX_ERR_BAD_ARG, "batched x-pass mode %d", mode);
+    if ((mode == 2 && !spec_h) || (mode == 3 && (!dspec || !xpart)))
+        return fail(EVX_ERR_BAD_ARG, "x-pass mode %d is missing a buffer", mode);
+    if (mode != 0 && mode != 3) dspec = nullptr;
+    if (mode != 3) xpart = nullptr;
     switch (nx) {
-        case 8: return xpass_batch_t<8, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
-        case 16: return xpass_batch_t<16, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
-        case 32: return xpass_batch_t<16, 2>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
-        case 64: return xpass_batch_t<16, 4>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
-        case 128: return xpass_batch_t<16, 8>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
-        case 256: return xpass_batch_t<16, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
-        case 512: return xpass_batch_t<32, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk);
+        case 8: return xpass_batch_t<8, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk, dspec, xpart);
+        case 16: return xpass_batch_t<16, 1>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk, dspec, xpart);
+        case 32: return xpass_batch_t<16, 2>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk, dspec, xpart);
+        case 64: return xpass_batch_t<16, 4>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk, dspec, xpart);
+        case 128: return xpass_batch_t<16, 8>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk, dspec, xpart);
+        case 256: return xpass_batch_t<16, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk, dspec, xpart);
+        case 512: return xpass_batch_t<32, 16>(mode, spec, spec_h, xb, count, M, nzh, nz, kx2, ky2, kz2, st, nyk, dspec, xpart);
         default: return fail(EVX_ERR_UNSUPPORTED, "x-pass needs a power-of-two nx in [8, 512]");
     }
 }

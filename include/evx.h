@@ -347,6 +347,24 @@ int evx_batch_adjoint(evx_batch* batch, const float* states, int nsteps,
                       const float* lam_in, float* lam_out, double* grads,
                       void* workspace, void* stream);
 
+/* Floats of one step's stored increment spectra for all instances (the
+ * x-pass layout for power-of-two groups, the rfftn layout for the others). */
+size_t evx_batch_spectrum_floats(const evx_batch* batch);
+
+/* evx_batch_forward with the trajectory and, in spectra (16-byte aligned,
+ * nsteps * evx_batch_spectrum_floats floats), each step's increment spectra. */
+int evx_batch_forward_spectra(evx_batch* batch, const float* u_in, float* u_out, int nsteps,
+                              float* traj, float* spectra, int* nonfinite, void* workspace,
+                              void* stream);
+
+/* evx_batch_adjoint with the stored spectra of the same steps: the mobility
+ * gradient sums by Parseval in k-space (no inverse transform of the second
+ * adjoint field, no h or u_{s+1} reads in the pullback).  lam_out equals
+ * evx_batch_adjoint's bit for bit; the gradients agree to float32 rounding. */
+int evx_batch_adjoint_spectra(evx_batch* batch, const float* states, const float* spectra,
+                              int nsteps, const float* lam_in, float* lam_out, double* grads,
+                              void* workspace, void* stream);
+
 /* ---- inversion loss ---------------------------------------------------------- */
 
 /* loss = mean((u - target)^2) (device double) and, if lam != NULL, its gradient
