@@ -186,6 +186,14 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
     const float ky2v = __ldg(ky2 + ky), kz2v = __ldg(kz2 + kz);
     float2* dsp = dspec ? dspec + (size_t)blockIdx.x * N1 * 256 + tid : nullptr;
     float t1 = 0.f, t2 = 0.f;
+    // mode 3: the tile's stored spectrum into registers first, in flight with the tile's own loads
+    // (nx <= 128: at 256 the registers would spill)
+    constexpr bool PRE = MODE == 3 && N1 <= 16 && N1 * N2 <= 128;
+    float2 dpre[PRE ? N1 : 1];
+    if constexpr (PRE) {
+#pragma unroll
+        for (int e = 0; e < N1; ++e) dpre[e] = __ldcs(dsp + e * 256);
+    }
 
     constexpr int NH = (N1 * N2) / 2;   // physical rows with EXT
     float2 v[N1];
@@ -201,8 +209,8 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
     }
     fwd_stage1<N1, N2>(v, xs, c);
     float2 hv[MODE == 2 ? N1 : 1];
-    mid_stage<N1, N2, MODE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2,
-                            mult + mc, M);
+    mid_stage<N1, N2, MODE, PRE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2,
+                                 mult + mc, M, &dpre);
     auto store = [&](float2* dst) {
         if (live) {
 #pragma unroll
