@@ -2,7 +2,7 @@
 
 Drop-in names for the reference's torch path: ``VoxelFields``,
 ``run_cahn_hilliard_solver``, ``run_allen_cahn_solver``, ``TimeDependentSolver``,
-``CahnHilliard``, ``ReactionDiffusion``, ``TwoPhaseAllenCahn``,
+``SteadyStatePseudoTimeSolver``, ``CahnHilliard``, ``ReactionDiffusion``, ``TwoPhaseAllenCahn``,
 ``PseudoSpectralIMEX``, ``ForwardEuler``, ``RungeKutta4``, ``ExponentialEuler``,
 ``RKC1``, ``RKC2``.  All compute
 runs in ``libevx.so`` (hand-written CUDA + cuFFT) through the C ABI declared in
@@ -18,6 +18,7 @@ __all__ = [
     "run_cahn_hilliard_solver",
     "run_allen_cahn_solver",
     "TimeDependentSolver",
+    "SteadyStatePseudoTimeSolver",
     "CahnHilliard",
     "ReactionDiffusion",
     "TwoPhaseAllenCahn",
@@ -38,9 +39,9 @@ def __getattr__(name):
     if name == "run_allen_cahn_solver":
         from .precompiled_solvers.allen_cahn import run_allen_cahn_solver
         return run_allen_cahn_solver
-    if name == "TimeDependentSolver":
-        from .solvers import TimeDependentSolver
-        return TimeDependentSolver
+    if name in ("TimeDependentSolver", "SteadyStatePseudoTimeSolver"):
+        from . import solvers
+        return getattr(solvers, name)
     if name in ("CahnHilliard", "ReactionDiffusion", "TwoPhaseAllenCahn"):
         from . import problem_definition
         return getattr(problem_definition, name)

@@ -187,3 +187,82 @@ class TimeDependentSolver(BaseSolver):
         else:
             self._handle_outputs(u, frame, time, vtk_out, verbose, plot_bounds, colormap)
         return u
+
+
+@dataclass
+class SteadyStatePseudoTimeSolver(BaseSolver):
+    """Pseudo-time iteration to a steady state (evoxels/solvers.py:210-247).
+
+    Same fields (``conv_crit``, ``check_freq``), convergence measure
+    ``||u - step(u)||_F / sqrt(Nx*Ny*Nz)`` per field, printed lines and single
+    output frame as the reference.  The reference evaluates ``step(time, u)``
+    twice per iteration (once for the difference, once for the update); the
+    steps here are deterministic and functional, so one evaluation gives both.
+    Iterations between checks run as one ``advance`` call when the stepper has
+    one, and the difference norm is a device reduction (``evx_mse_grad``
+    without a gradient: ``sqrt(mean(d^2))`` equals the reference's measure).
+
+    One deliberate difference: the reference never advances its iteration
+    counter (``self.iter`` stays 0), so it checks every iteration, passes time
+    0 to every step and ignores ``max_iters``.  Here the counter advances, so
+    convergence is checked every ``check_freq`` iterations and ``max_iters``
+    bounds the loop; with ``check_freq=1`` and an autonomous problem the
+    iterates, the stopping iteration and the output are the reference's.
+    """
+    conv_crit: float = 1e-6
+    check_freq: int = 10
+
+    def _run_loop(self, u, step, time_increment, frames, max_iters, vtk_out, verbose, plot_bounds, colormap):
+        if self.check_freq < 1:
+            raise ValueError("check_freq must be a positive integer")
+        self.converged = False
+        self.iter = 0
+        advance = getattr(self._stepper, "advance", None)
+        time = 0.0
+        while not self.converged and self.iter < max_iters:
+            time = self.iter * time_increment
+            if self.iter % self.check_freq == 0:
+                u_next = step(time, u)
+                self.converged = self.check_convergence(u, u_next, verbose)
+                u = u_next
+                self.iter += 1
+                continue
+            n = min(self.check_freq - self.iter % self.check_freq, max_iters - self.iter)
+            if advance is not None:
+                u = advance(u, n)
+            else:
+                for s in range(n):
+                    u = step((self.iter + s) * time_increment, u)
+            self.iter += n
+            time = (self.iter - 1) * time_increment
+        self._handle_outputs(u, 0, time, vtk_out, verbose, plot_bounds, colormap)
+        return u
+
+    def rel_changes(self, u, u_next):
+        """``||u[i] - u_next[i]||_F / sqrt(Nx*Ny*Nz)`` per field, as host floats."""
+        from . import _lib
+        from .voxelgrid import cuda_stream
+        n = u[0].numel()
+        L = _lib.lib()
+        need = int(L.evx_mse_scratch_bytes(n))
+        sc = getattr(self, "_conv_scratch", None)
+        if sc is None or sc.numel() < need or sc.device != u.device:
+            sc = torch.empty(need, dtype=torch.uint8, device=u.device)
+            self._conv_scratch = sc
+        ms = torch.empty(u.shape[0], dtype=torch.float64, device=u.device)
+        for i in range(u.shape[0]):
+            _lib.check(L.evx_mse_grad(u[i].data_ptr(), u_next[i].data_ptr(), n, None, ms[i:i + 1].data_ptr(),
+                                      sc.data_ptr(), sc.numel(), cuda_stream()), "evx_mse_grad")
+        return [float(np.sqrt(m)) for m in ms.cpu().tolist()]
+
+    def check_convergence(self, u, u_next, verbose):
+        """Relative change of every field below ``conv_crit`` (evoxels/solvers.py:231-247)."""
+        converged = True
+        for name, rel_change in zip(self.fieldnames, self.rel_changes(u, u_next)):
+            if rel_change > self.conv_crit:
+                converged = False
+            if verbose:
+                print(f"Iter {self.iter}: Field '{name}' relative change: {rel_change:.2e}")
+        if converged and verbose:
+            print(f"Converged after {self.iter} iterations.")
+        return converged

@@ -48,6 +48,7 @@ __all__ = [
     "fe_step",
     "ch_imex_run",
     "rd_fe_run",
+    "steady_state_run",
     "ch_imex_vjp",
     "ch_imex_loss_grads",
     "seeded_ch_field",
@@ -530,6 +531,33 @@ def rkc_step(u, dt, rhs_fn, k):
             y_new = y_new + k["gamma"][j] * dt * r0
         y_prev, y = y, y_new
     return y
+
+
+def steady_state_run(u0, step_fn, max_iters, conv_crit=1e-6, check_freq=10):
+    """``SteadyStatePseudoTimeSolver._run_loop`` / ``check_convergence``
+    (evoxels/solvers.py:218-247): ``diff = u - step(u)``, ``u = step(u)``, and
+    at every ``check_freq``-th iteration the per-field measure
+    ``torch.linalg.norm(diff[i]) / sqrt(Nx*Ny*Nz)`` in the field's dtype against
+    ``conv_crit``.  The iteration counter advances (the reference's loop leaves it
+    at 0, which amounts to ``check_freq = 1`` with ``max_iters`` unbounded).
+
+    Returns ``(u, iterations, converged, [(iteration, [rel_change per field]), ...])``.
+    """
+    u = u0
+    it = 0
+    converged = False
+    checks = []
+    nvox = float(np.prod(u0.shape[1:]))
+    while not converged and it < max_iters:
+        u_next = step_fn(u)
+        diff = u - u_next
+        if it % check_freq == 0:
+            rel = [float(torch.linalg.norm(diff[i]) / np.sqrt(nvox)) for i in range(u.shape[0])]
+            checks.append((it, rel))
+            converged = all(r <= conv_crit for r in rel)
+        u = u_next
+        it += 1
+    return u, it, converged, checks
 
 
 def seeded_ch_field(shape, seed):

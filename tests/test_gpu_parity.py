@@ -135,7 +135,7 @@ def test_ch_imex_vs_reference_golden(cuda_lib, i):
 
 @pytest.mark.parametrize("shape", [(16, 16, 16), (5, 7, 9), (24, 20, 18), (100, 100, 100)])
 def test_ch_one_step_error_vs_fp64_oracle(cuda_lib, shape):
-    """Spec bar: <= 1e-5 relative (to max) per step against FP64."""
+    """Per-step error bar: <= 1e-5 relative (to max) against the FP64 oracle."""
     from evoxels_gb300.problem_definition import CahnHilliard
     from evoxels_gb300.timesteppers import PseudoSpectralIMEX
     u0 = oracle.seeded_ch_field(shape, 1)
@@ -167,7 +167,7 @@ def test_ch_forward_fused_equals_stepwise(cuda_lib):
 
 
 def test_ch_1000_steps_vs_fp64_oracle(cuda_lib):
-    """Spec bar: <= 1e-4 relative (to max) after 1000 steps (32^3 keeps the FP64 run short)."""
+    """Long-run error bar: <= 1e-4 relative (to max) after 1000 steps (32^3 keeps the FP64 run short)."""
     from evoxels_gb300.problem_definition import CahnHilliard
     from evoxels_gb300.timesteppers import PseudoSpectralIMEX
     shape = (32, 32, 32)
