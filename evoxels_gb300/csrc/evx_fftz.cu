@@ -139,14 +139,26 @@ zt_r2c_kernel(const float* __restrict__ in, float2* __restrict__ out, int nx, in
     }
 }
 
-template <int NZ>
+// 16-byte asynchronous global -> shared copy (zero-filled when !full) and its groups.
+__device__ __forceinline__ void cp_async16(float2* dst, const float2* src, bool full) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(s), "l"(src), "r"(full ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// DB: the staging area T is double-buffered and, on the vectorised path, the
+// next item's spectrum runs are copied into the idle buffer by cp.async while
+// the current item is transformed (the R2C's one-item-ahead prefetch, without
+// the registers); otherwise the thread's staging loads go through registers.
+template <int NZ, bool DB = false>
 __global__ void __launch_bounds__(256)
 zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, int ny, bool vec) {
     using G = ZT<NZ>;
     constexpr int EZ = G::EZ, TZ = G::TZ, QZ = G::QZ, NH = G::NH, NH1 = G::NH1, YG = G::YG, TP = G::TP;
     extern __shared__ __align__(16) float2 sm[];
     float2* Z = sm;
-    float2* T = sm + G::PAIRS * G::PS;
+    float2* T = sm + G::PAIRS * G::PS;           // [DB ? 2 : 1][NH1][TP]
     const int tid = threadIdx.x;
     const int t = tid % TZ, g = tid / TZ;
     const ZCol zc{g * G::PS, t, G::KS};
@@ -154,33 +166,61 @@ zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, in
     inv_twiddles<EZ, TZ>(tw, t);
     const int groups = (ny + YG - 1) / YG;
     const long items = (long)nx * groups;
-    for (long it = blockIdx.x; it < items; it += gridDim.x) {
-        const int x = (int)(it / groups), y0 = (int)(it - (long)x * groups) * YG;
-        const int rows = min(YG, ny - y0);
-        const float2* irow = in + (size_t)x * NH1 * ny + y0;
-        // all of the thread's loads in flight at once (two y values each; vec: even ny,
-        // 16-byte aligned input), then into T
-        constexpr int HY = YG / 2, PER = (NH1 * HY + 255) / 256;
-        float4 w[PER];
-#pragma unroll
-        for (int p = 0; p < PER; ++p) {
-            const int e = tid + 256 * p, kz = e / HY, yl = 2 * (e - kz * HY);
-            const float2* src = irow + (size_t)kz * ny + yl;
-            float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (e < NH1 * HY) {
-                if (vec && yl + 1 < rows) {
-                    v4 = __ldg(reinterpret_cast<const float4*>(src));
-                } else {
-                    if (yl < rows) { const float2 q = __ldg(src); v4.x = q.x; v4.y = q.y; }
-                    if (yl + 1 < rows) { const float2 q = __ldg(src + 1); v4.z = q.x; v4.w = q.y; }
-                }
-            }
-            w[p] = v4;
-        }
+    constexpr int HY = YG / 2, NST = NH1 * HY, PER = (NST + 255) / 256;
+    const bool db = DB && vec;
+    // queue the copies of item it2's half spectrum (two y values per copy) into Tb
+    auto issue = [&](long it2, float2* Tb) {
+        const int x2 = (int)(it2 / groups), y2 = (int)(it2 - (long)x2 * groups) * YG;
+        const int rows2 = min(YG, ny - y2);
+        const float2* irow2 = in + (size_t)x2 * NH1 * ny + y2;
 #pragma unroll
         for (int p = 0; p < PER; ++p) {
             const int e = tid + 256 * p;
-            if (e < NH1 * HY) *reinterpret_cast<float4*>(T + (e / HY) * TP + 2 * (e % HY)) = w[p];
+            if (e < NST) {
+                const int kz = e / HY, yl = 2 * (e - kz * HY);
+                const bool full = yl < rows2;    // vec: rows2 is even, so yl + 1 < rows2 too
+                cp_async16(Tb + kz * TP + yl, full ? irow2 + (size_t)kz * ny + yl : irow2, full);
+            }
+        }
+        cp_async_commit();
+    };
+    if (db && blockIdx.x < items) issue(blockIdx.x, T);
+    int buf = 0;
+    for (long it = blockIdx.x; it < items; it += gridDim.x, buf ^= 1) {
+        const int x = (int)(it / groups), y0 = (int)(it - (long)x * groups) * YG;
+        const int rows = min(YG, ny - y0);
+        const float2* irow = in + (size_t)x * NH1 * ny + y0;
+        const float2* Tc = T;
+        if (db) {
+            // the idle buffer was last read before the previous item's closing barrier
+            Tc = T + buf * (NH1 * TP);
+            if (it + gridDim.x < items) issue(it + gridDim.x, T + (buf ^ 1) * (NH1 * TP));
+            else cp_async_commit();              // empty group: the wait below stays uniform
+            cp_async_wait_prev();                // this item's copies have landed
+        } else {
+            // all of the thread's loads in flight at once (two y values each; vec: even ny,
+            // 16-byte aligned input), then into T
+            float4 w[PER];
+#pragma unroll
+            for (int p = 0; p < PER; ++p) {
+                const int e = tid + 256 * p, kz = e / HY, yl = 2 * (e - kz * HY);
+                const float2* src = irow + (size_t)kz * ny + yl;
+                float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (e < NH1 * HY) {
+                    if (vec && yl + 1 < rows) {
+                        v4 = __ldg(reinterpret_cast<const float4*>(src));
+                    } else {
+                        if (yl < rows) { const float2 q = __ldg(src); v4.x = q.x; v4.y = q.y; }
+                        if (yl + 1 < rows) { const float2 q = __ldg(src + 1); v4.z = q.x; v4.w = q.y; }
+                    }
+                }
+                w[p] = v4;
+            }
+#pragma unroll
+            for (int p = 0; p < PER; ++p) {
+                const int e = tid + 256 * p;
+                if (e < NH1 * HY) *reinterpret_cast<float4*>(T + (e / HY) * TP + 2 * (e % HY)) = w[p];
+            }
         }
         __syncthreads();
         const int a = 2 * g, b = a + 1;
@@ -191,7 +231,7 @@ zt_c2r_kernel(const float2* __restrict__ in, float* __restrict__ out, int nx, in
             for (int k2 = 0; k2 < TZ; ++k2) {
                 const int k = t * QZ + q + EZ * k2;
                 const int kk = k <= NH ? k : NZ - k;
-                const float4 AB = *reinterpret_cast<const float4*>(T + kk * TP + a);   // (A, B) of the pair
+                const float4 AB = *reinterpret_cast<const float4*>(Tc + kk * TP + a);  // (A, B) of the pair
                 float2 c;
                 if (k == 0 || k == NH) c = make_float2(AB.x, AB.z);                    // real parts only
                 else if (k < NH) c = make_float2(AB.x - AB.w, AB.y + AB.z);            // A + iB
@@ -268,7 +308,12 @@ int zt_launch_t(bool fwd, int nx, int ny, const void* in, void* out, cudaStream_
         constexpr bool S = NZ == 256;
         return zt_go(zt_r2c_kernel<NZ, S ? 2 : 1, S, true>, true, items, nx, ny, in, out, G::SMEM, st);
     }
-    return zt_go(zt_c2r_kernel<NZ>, false, items, nx, ny, in, out, G::SMEM, st);
+    // C2R for nz = 256: double-buffered staging (2 x 34 KB more shared memory, still 2 blocks per SM)
+    if constexpr (NZ == 256)
+        return zt_go(zt_c2r_kernel<NZ, true>, false, items, nx, ny, in, out,
+                     G::SMEM + (size_t)G::NH1 * G::TP * sizeof(float2), st);
+    else
+        return zt_go(zt_c2r_kernel<NZ>, false, items, nx, ny, in, out, G::SMEM, st);
 }
 
 int zt_launch(bool fwd, int nx, int ny, int nz, const void* in, void* out, cudaStream_t st) {
