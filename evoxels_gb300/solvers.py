@@ -202,12 +202,15 @@ class SteadyStatePseudoTimeSolver(BaseSolver):
     one, and the difference norm is a device reduction (``evx_mse_grad``
     without a gradient: ``sqrt(mean(d^2))`` equals the reference's measure).
 
-    One deliberate difference: the reference never advances its iteration
+    Two deliberate differences.  The reference never advances its iteration
     counter (``self.iter`` stays 0), so it checks every iteration, passes time
     0 to every step and ignores ``max_iters``.  Here the counter advances, so
     convergence is checked every ``check_freq`` iterations and ``max_iters``
     bounds the loop; with ``check_freq=1`` and an autonomous problem the
-    iterates, the stopping iteration and the output are the reference's.
+    iterates, the stopping iteration and the output are those of the
+    reference's loop.  And on the reference's torch backend the first check
+    raises ``TypeError`` (``torch.sqrt`` of the Python int ``Nx*Ny*Nz``,
+    evoxels/solvers.py:238-239); here the measure is computed as written.
     """
     conv_crit: float = 1e-6
     check_freq: int = 10
