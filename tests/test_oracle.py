@@ -213,3 +213,29 @@ def test_normalize_bc_errors_match_reference_messages():
         oracle.normalize_bc((("dirichlet", (1.0,)), "periodic", "periodic"))
     with pytest.raises(ValueError, match="do not accept boundary values"):
         oracle.normalize_bc((("neumann", (1.0, 2.0)), "periodic", "periodic"))
+
+
+def test_steady_state_loop_semantics():
+    """The steady-state loop (evoxels/solvers.py:218-247): with check_freq = 1 it stops at the first
+    iteration whose relative change ||u - step(u)||_F / sqrt(Nx Ny Nz) is <= conv_crit, having applied
+    the step that many times plus one; a larger check_freq checks only multiples of it; max_iters
+    bounds a run that does not converge."""
+    shape = (8, 6, 5)
+    bc = (("dirichlet", (0.0, 0.0)), "neumann", "neumann")
+    u0 = torch.tensor(oracle.seeded_unit_field(shape, 7), dtype=torch.float32).unsqueeze(0)
+
+    def step(v):
+        return oracle.fe_step(v, 0.15, lambda w: oracle.rd_rhs(w, 1.0, bc))
+    crit = 1e-4
+    u, it, conv, checks = oracle.steady_state_run(u0, step, 5000, crit, 1)
+    assert conv and [c[0] for c in checks] == list(range(it))
+    rel = [c[1][0] for c in checks]
+    assert rel[-1] <= crit and all(r > crit for r in rel[:-1])
+    ref = u0
+    for _ in range(it):
+        ref = step(ref)
+    assert torch.equal(u, ref)
+    _, it7, conv7, checks7 = oracle.steady_state_run(u0, step, 5000, crit, 7)
+    assert conv7 and it7 >= it and (it7 - 1) % 7 == 0 and all(c[0] % 7 == 0 for c in checks7)
+    _, itn, convn, _ = oracle.steady_state_run(u0, step, 23, 0.0, 5)
+    assert not convn and itn == 23
