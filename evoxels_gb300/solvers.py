@@ -216,7 +216,8 @@ class SteadyStatePseudoTimeSolver(BaseSolver):
     check_freq: int = 10
 
     def _run_loop(self, u, step, time_increment, frames, max_iters, vtk_out, verbose, plot_bounds, colormap):
-        if self.check_freq < 1:
+        cf = int(self.check_freq)
+        if cf != self.check_freq or cf < 1:
             raise ValueError("check_freq must be a positive integer")
         self.converged = False
         self.iter = 0
@@ -224,13 +225,13 @@ class SteadyStatePseudoTimeSolver(BaseSolver):
         time = 0.0
         while not self.converged and self.iter < max_iters:
             time = self.iter * time_increment
-            if self.iter % self.check_freq == 0:
+            if self.iter % cf == 0:
                 u_next = step(time, u)
                 self.converged = self.check_convergence(u, u_next, verbose)
                 u = u_next
                 self.iter += 1
                 continue
-            n = min(self.check_freq - self.iter % self.check_freq, max_iters - self.iter)
+            n = min(cf - self.iter % cf, max_iters - self.iter)
             if advance is not None:
                 u = advance(u, n)
             else:
