@@ -64,3 +64,22 @@ def test_voxel_sphere_is_symmetric():
     vf.set_voxel_sphere("s", (8.0, 8.0, 8.0), 4.0)
     s = vf.fields["s"]
     assert s.sum() > 0 and np.array_equal(s, s[::-1]) and np.array_equal(s, s.transpose(1, 0, 2))
+
+
+def test_checkpoint_interval_is_the_largest_that_fits():
+    """``(K+1)`` segment states + ``K`` stored spectra + ``ceil(n/K)`` checkpoints within the budget."""
+    import math
+    from evoxels_gb300.adjoint import default_checkpoint_interval
+
+    class VG:
+        shape = (512, 512, 512)
+    field = 4 * 512 ** 3
+    spec = 4 * 512 * 512 * 257 * 2
+    for n, budget in [(100, 16 * 2 ** 30), (100, 200 * 2 ** 30), (1000, 40 * 2 ** 30), (7, 1)]:
+        K = default_checkpoint_interval(VG(), n, budget_bytes=budget, spectrum_bytes=spec)
+        need = lambda k: (k + 1) * field + k * spec + math.ceil(n / k) * field  # noqa: E731
+        assert 1 <= K <= n
+        assert K == 1 or need(K) <= budget
+        assert all(need(k) > budget for k in range(K + 1, n + 1))
+    # everything fits: the whole trajectory is kept
+    assert default_checkpoint_interval(VG(), 100, budget_bytes=2 ** 40, spectrum_bytes=spec) == 100
