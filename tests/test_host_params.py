@@ -83,3 +83,15 @@ def test_checkpoint_interval_is_the_largest_that_fits():
         assert all(need(k) > budget for k in range(K + 1, n + 1))
     # everything fits: the whole trajectory is kept
     assert default_checkpoint_interval(VG(), 100, budget_bytes=2 ** 40, spectrum_bytes=spec) == 100
+
+
+def test_ac_params_are_float32_roundings():
+    """The two-phase Allen-Cahn constants (evoxels/problem_definition.py:420-447: ``potential/2/eps``
+    with the default ``18/eps`` well, ``3/eps`` forcing, ``curvature`` and ``1 - curvature``)."""
+    from evoxels_gb300.problem_definition import ac_params
+    f = lambda x: float(np.float32(x))  # noqa: E731
+    eps, gab, M, force, curv = 2.5, 0.8, 1.3, 0.2, 0.03
+    p = ac_params(eps, gab, M, force, curv)
+    assert (p.w, p.eps, p.gab, p.M, p.force) == (f(18 / eps), f(eps), f(gab), f(M), f(force))
+    assert (p.three_over_eps, p.curvature, p.one_minus_curvature) == (f(3 / eps), f(curv), f(1 - curv))
+    assert ac_params(eps, gab, M, force, curv, w=4.0).w == 4.0
