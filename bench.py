@@ -76,6 +76,10 @@ def algorithmic_bytes(slot, n, nspec):
         "cufft_c2r_x2": 16 * nspec + 8 * n,
         "fft_yz_r2c": 4 * n + 8 * nspec,   # read the field, write the (y,z) half spectrum
         "fft_yz_c2r": 8 * nspec + 4 * n,
+        "fft_z_r2c": 4 * n + 8 * nspec,    # read the field, write the z-transformed half spectrum
+        "fft_z_c2r": 8 * nspec + 4 * n,    # read the half spectrum, write the field
+        "cufft_c2c_y": 16 * nspec,         # read + write the half spectrum (library)
+        "batch_cufft_c2c_y": 16 * nspec,
         "batch_rhs_fused": 16 * n,
         "batch_rhs": 8 * n,
         "batch_kspace_fwd": 16 * nspec,
@@ -241,6 +245,40 @@ class ChFwdAdj:
 
     def e2e_bytes(self):
         return 2 * 4 * self.n, 4 * self.n + 8 * 4
+
+    def fp64_errors(self):
+        """Error of this workload's GPU results against the FP64 oracle on the host, from the same
+        float64 inputs: the state after the bench step's forward steps, and one adjoint step
+        (dL/du and the step's dL/dD, dL/deps) against torch autograd through the FP64 oracle.
+        ``max|gpu - fp64| / max|fp64|`` for fields, relative error for the scalars."""
+        import oracle
+        torch = self.torch
+        torch.set_num_threads(os.cpu_count() or 1)
+        dev = self.c0.device
+        c0_64 = torch.tensor(0.5 + 0.1 * np.random.default_rng(self.config["seed_c0"]).random(self.shape)).unsqueeze(0)
+        traj = torch.empty((self.T + 1,) + self.shape, dtype=torch.float32, device=dev)
+        traj[0:1].copy_(c0_64)
+        self.runner.forward(traj[0:1], self.T, 1.0, 3.0, traj=traj[1:])
+        t0 = time.perf_counter()
+        u64 = oracle.ch_imex_run(c0_64, self.T, 0.1)
+        fwd = oracle.rel_to_max(traj[self.T].cpu().numpy(), u64[0].numpy())
+        one = oracle.rel_to_max(traj[1].cpu().numpy(), oracle.ch_imex_run(c0_64, 1, 0.1)[0].numpy())
+        lam64 = torch.tensor(np.random.default_rng(7).random(self.shape) - 0.5).unsqueeze(0)
+        g64, dD, deps = oracle.ch_imex_vjp(c0_64, lam64, 0.1, 3.0, 1.0)
+        lam = lam64.float().to(dev)
+        grads = torch.zeros(3, dtype=torch.float64, device=dev)
+        g = self.runner.adjoint(traj[0:2], 1, lam, 1.0, 3.0, grads)
+        adj = oracle.rel_to_max(g.cpu().numpy(), g64.numpy())
+        gD, geps = self.runner.param_grads(grads, 3.0)
+        host_s = time.perf_counter() - t0
+        del traj
+        return {"forward_1_step": float("%.3g" % one), "forward_%d_steps" % self.T: float("%.3g" % fwd),
+                "adjoint_1_step_dL_du": float("%.3g" % adj),
+                "adjoint_1_step_dL_dD": float("%.3g" % (abs(gD - dD) / abs(dD))),
+                "adjoint_1_step_dL_deps": float("%.3g" % (abs(geps - deps) / abs(deps))),
+                "bar": "1e-5 per step (fields, max|err|/max|ref|)",
+                "reference": "FP64 oracle (torch CPU restatement of the reference, float64) from the same "
+                             "float64 c0, %.0f s on the host" % host_s}
 
 
 class ChForward:
@@ -595,6 +633,42 @@ class Batched:
         return a.elapsed_time(b) / steps
 
 
+def batched_summary(torch, device, steps, warmup):
+    """The batched forward + adjoint workload (64 uneven instances) timed as the headline one (CUDA
+    events, device-resident inputs larger than L2), its plain per-grid counterpart on the same GPU, and
+    the forward error of a sample of instances against the FP64 oracle."""
+    import oracle
+    wl = Batched(torch, device, 20, adjoint=True)
+    for _ in range(warmup):
+        wl.step()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        wl.step()
+    b.record()
+    b.synchronize()
+    ms = a.elapsed_time(b) / steps
+    plain_ms = wl.plain(max(2, min(steps, 5)))
+    # one forward step of a sample of instances (every side length once) against FP64
+    out = wl.b.unpack(wl.b.forward(wl.u0, 1))
+    errs = {}
+    for side in sorted(set(s[0] for s in wl.shapes)):
+        i = next(k for k, s in enumerate(wl.shapes) if s[0] == side)
+        r64 = oracle.ch_imex_run(torch.tensor(wl.fields[i]).unsqueeze(0), 1, 0.1, float(wl.eps[i]), float(wl.M[i]),
+                                 mu_hom=wl.pin)
+        errs["instance %d (%d^3)" % (i, side)] = float("%.3g" % oracle.rel_to_max(out[i].cpu().numpy(), r64.numpy()))
+    return {"workload": "batched64_fwd_adj", "value": round(wl.units_per_step / (ms / 1e3), 1),
+            "unit": "voxel-steps/s", "ms_per_step": round(ms, 3), "steps": steps,
+            "plain_value": round(wl.units_per_step / (plain_ms / 1e3), 1), "plain_ms_per_step": round(plain_ms, 3),
+            "vs_plain": round(plain_ms / ms, 3),
+            "plain_path": "single-grid CahnHilliardAdjoint forward (trajectory, increment spectra) + adjoint with "
+                          "parameter gradients, one instance at a time, same GPU",
+            "config": {k: wl.config[k] for k in ("instances", "sides", "total_voxels", "steps_per_bench_step",
+                                                 "tuning", "l2")},
+            "err_vs_fp64_forward_1_step": errs}
+
+
 def make_workload(name, torch, device, inner=None, spp=0, shape=None):
     if name == "batched64_fwd":
         return Batched(torch, device, inner or 50, adjoint=False)
@@ -735,6 +809,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ch256_fwd_adj")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline workload only: skip the FP64 error statement and the batched line")
     ap.add_argument("--inner-steps", type=int, default=None,
                     help="override the IMEX/FE steps per bench step (profiling runs)")
     ap.add_argument("--fd-steps-per-pass", type=int, default=0, choices=[0, 1, 2, 4],
@@ -920,6 +996,13 @@ def main():
         "vs_plain": vs_plain,
         "clocks": clocks,
     }
+    if world == 1 and args.workload == "ch256_fwd_adj" and not args.shape and not args.no_extras:
+        # the metric's second half (batched uneven grids against the plain per-grid path, same GPU)
+        # and the error statement of the headline run
+        out["err_vs_fp64"] = wl.fp64_errors()
+        del wl
+        torch.cuda.empty_cache()
+        out["batched"] = batched_summary(torch, device, args.steps, warmup)
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.shape:
         cb, _, _ = cpu_sample(args.workload, torch)
         out["cpu_baseline"] = cb

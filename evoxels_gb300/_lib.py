@@ -37,9 +37,13 @@ class EvxGrid(C.Structure):
                 ("inv_h2_sum", C.c_float)]
 
 
+EVX_BULK_DOUBLE_WELL = 0
+EVX_BULK_REGULAR_SOLUTION = 1
+
+
 class EvxChParams(C.Structure):
     _fields_ = [("D", C.c_float), ("kappa", C.c_float), ("w", C.c_float), ("A", C.c_float),
-                ("sym_coef", C.c_float), ("dt", C.c_float)]
+                ("sym_coef", C.c_float), ("dt", C.c_float), ("bulk", C.c_int32)]
 
 
 class EvxAcParams(C.Structure):
@@ -89,6 +93,8 @@ _SIGS = {
     "evx_ch_adjoint": (C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(EvxChParams), _P, _P, _P]),
     "evx_ch_spectrum_floats": (C.c_size_t, [_P]),
     "evx_device_status": (C.c_int, [C.c_int]),
+    "evx_device_status_async": (C.c_int, [_P, _P]),
+    "evx_set_wait_polls": (C.c_int, [C.c_int]),
     "evx_ac_rhs": (C.c_int, [_P, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC), C.POINTER(EvxAcParams), _P]),
     "evx_ac_rhs_stage": (C.c_int, [_P, _P, C.c_float, _P, C.POINTER(EvxGrid), C.POINTER(EvxBC),
                                    C.POINTER(EvxAcParams), _P]),
@@ -177,6 +183,32 @@ def prof_read():
         out[name.value.decode()] = (ms.value, cnt.value)
         i += 1
     return out
+
+
+EVX_STATUS_WAIT_GAVE_UP = 1
+
+
+class DeviceWaitError(RuntimeError):
+    """A bounded wait inside a kernel gave up: the results of the calls since the last check are invalid."""
+
+
+def raise_device_status(status, where=""):
+    """Raise ``DeviceWaitError`` for a non-zero device status word (and clear it on the device)."""
+    if not status:
+        return
+    lib().evx_device_status(1)
+    what = "a bounded wait of the x-pass on its tile loads gave up" if status & EVX_STATUS_WAIT_GAVE_UP else \
+        "device status %#x" % status
+    raise DeviceWaitError(f"{where + ': ' if where else ''}{what}; the results computed since the last check "
+                          "are invalid")
+
+
+def check_device_status(where=""):
+    """Synchronous read of the device status word; raises ``DeviceWaitError`` if a kernel gave up."""
+    v = lib().evx_device_status(0)
+    if v < 0:
+        check(EVX_ERR_CUDA, where or "evx_device_status")
+    raise_device_status(v, where)
 
 
 def check(code, what=""):

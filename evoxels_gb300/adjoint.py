@@ -142,6 +142,7 @@ class CahnHilliardAdjoint:
     def param_grads(self, grads, eps):
         """Map (dL/dD, dL/dkappa, dL/dw) to (dL/dD, dL/deps)."""
         gD, gK, gW = (float(x) for x in grads.tolist())
+        _lib.check_device_status("CahnHilliardAdjoint gradients")
         geps = 2.0 * gK
         if self.pinned_w is None:
             geps += -18.0 / float(eps) ** 2 * gW
@@ -154,7 +155,7 @@ class CahnHilliardAdjoint:
         lam = torch.empty_like(uT)
         loss = self.mse(uT, target, lam)
         g0, grads = self.backward_checkpointed(saved, nsteps, lam, D, eps, K)
-        gD, geps = self.param_grads(grads, eps)
+        gD, geps = self.param_grads(grads, eps)     # reads the device status word
         return float(loss), g0, gD, geps
 
 

@@ -166,6 +166,7 @@ class BatchedCahnHilliard:
     def param_grads(self, grads):
         """(dL/dD, dL/dkappa, dL/dw) per instance -> (dL/dD, dL/deps)."""
         g = grads.detach().cpu().numpy()
+        _lib.check_device_status("BatchedCahnHilliard gradients")
         geps = 2.0 * g[:, 1]
         if self.pinned_w is None:
             geps = geps - 18.0 / self.eps ** 2 * g[:, 2]

@@ -284,6 +284,8 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
         return fail(EVX_ERR_BAD_ARG, "lam_in and lam_out must be 16-byte aligned");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
     if (plan->xext) return fail(EVX_ERR_UNSUPPORTED, "the adjoint of the mirrored-x spectral step is not built");
+    if (prm->bulk != EVX_BULK_DOUBLE_WELL)
+        return fail(EVX_ERR_UNSUPPORTED, "the adjoint is built for the double-well bulk term w*c(1-c)(1-2c)");
     const bool want = grads != nullptr;
     const bool spectral = want && spectra != nullptr;
     if (spectral) {
@@ -296,7 +298,7 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
                                           as_stream(stream)), "evx_ch_adjoint copy");
     const GraphKey key{2, key_p(states), key_p(spectra), (uint64_t)nsteps, key_p(lam_in), key_p(lam_out),
                        key_p(grads), key_p(workspace), key_f(prm->D), key_f(prm->kappa), key_f(prm->w),
-                       key_f(prm->A), key_f(prm->sym_coef), key_f(prm->dt)};
+                       key_f(prm->A), key_f(prm->sym_coef), key_f(prm->dt), (uint64_t)prm->bulk};
     return plan->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
     int rc;
     if ((rc = ch_plan_bind(plan, workspace, st, want && !spectral))) return rc;

@@ -440,6 +440,8 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
         if (rc) return rc;
         if (inst[i].nz % 4) return fail(EVX_ERR_UNSUPPORTED, "batched instances need nz %% 4 == 0 (instance %d)", i);
         if ((rc = ch_validate_params(&inst[i].params))) return rc;
+        if (inst[i].params.bulk != EVX_BULK_DOUBLE_WELL)
+            return fail(EVX_ERR_UNSUPPORTED, "batched instances take the double-well bulk term only");
     }
     evx_batch* b = new evx_batch();
     b->n = n;

@@ -91,7 +91,7 @@ ch_rhs_kernel(const float* __restrict__ u, const float* __restrict__ upd, float*
             const float zm = (!pz && gk == 0) ? ghost_lo(G, 2, c) : cs[s0][jj][kk - 1];
             const float zp = (!pz && gk == G.nz - 1) ? ghost_hi(G, 2, c) : cs[s0][jj][kk + 1];
             const float lap = lap7(G, c, xm, xp, ym, yp, zm, zp);
-            ms[ms_sl][a][b] = __fsub_rn(mu_hom(P.w, c), __fmul_rn(P.kappa, lap));
+            ms[ms_sl][a][b] = __fsub_rn(mu_bulk(P.bulk, P.w, c), __fmul_rn(P.kappa, lap));
         }
     };
 
@@ -266,6 +266,8 @@ int ch_validate_params(const evx_ch_params* p) {
     const float v[6] = {p->D, p->kappa, p->w, p->A, p->sym_coef, p->dt};
     for (float x : v)
         if (!std::isfinite(x)) return fail(EVX_ERR_BAD_ARG, "Cahn-Hilliard parameters must be finite");
+    if (p->bulk != EVX_BULK_DOUBLE_WELL && p->bulk != EVX_BULK_REGULAR_SOLUTION)
+        return fail(EVX_ERR_BAD_ARG, "unknown bulk potential form %d", (int)p->bulk);
     return EVX_OK;
 }
 
@@ -358,10 +360,12 @@ bool all_periodic(const Geo& G) {
     return G.kind[0] == EVX_BC_PERIODIC && G.kind[1] == EVX_BC_PERIODIC && G.kind[2] == EVX_BC_PERIODIC;
 }
 
-int ch_rhs_launch(bool fused, const float* u, const float* upd, float* u_new, float* r,
+// exact: the reference's float32 operations (evx_ch_rhs); the spectral loops pass
+// false, which lets the periodic fast path fuse its products
+int ch_rhs_launch(bool fused, bool exact, const float* u, const float* upd, float* u_new, float* r,
                   const evx_grid* g, const Geo& G, const ChP& P, cudaStream_t st) {
     if (all_periodic(G) && fast_ok(g, {u, upd, u_new, r}))
-        return ch_rhs_fast_launch(fused, u, upd, u_new, r, g, G, P, st);
+        return ch_rhs_fast_launch(fused, exact, u, upd, u_new, r, g, G, P, st);
     dim3 grid; int lx;
     ch_stencil_grid(g, &grid, &lx);
     if (fused) EVX_TIMED("ch_rhs_fused", st, ch_rhs_kernel<true><<<grid, dim3(32, 8), 0, st>>>(u, upd, u_new, r, G, P, lx));
@@ -384,7 +388,7 @@ int evx_ch_rhs(const float* u, float* r, const evx_grid* g, const evx_bc* bc, co
     if ((rc = ch_validate_params(p))) return rc;
     if (!u || !r) return fail(EVX_ERR_BAD_ARG, "NULL field pointer");
     if (u == r) return fail(EVX_ERR_BAD_ARG, "input and output must not alias");
-    return ch_rhs_launch(false, u, nullptr, nullptr, r, g, make_geo(g, bc), make_chp(p), as_stream(stream));
+    return ch_rhs_launch(false, true, u, nullptr, nullptr, r, g, make_geo(g, bc), make_chp(p), as_stream(stream));
 }
 
 int evx_ch_plan_create(evx_ch_plan** out, const evx_grid* g, int flags) {
@@ -635,7 +639,7 @@ int ch_forward_impl(evx_ch_plan* plan, const float* u_in, float* u_out, int nste
                           "evx_ch_forward copy");
     const GraphKey key{1, key_p(u_in), key_p(u_out), (uint64_t)nsteps, key_p(traj), key_p(spectra), key_p(mult),
                        key_p(nonfinite), key_p(workspace), key_f(prm->D), key_f(prm->kappa), key_f(prm->w),
-                       key_f(prm->A), key_f(prm->sym_coef), key_f(prm->dt)};
+                       key_f(prm->A), key_f(prm->sym_coef), key_f(prm->dt), (uint64_t)prm->bulk};
     return plan->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
     int rc;
     if ((rc = ch_plan_bind(plan, workspace, st, false))) return rc;
@@ -649,10 +653,10 @@ int ch_forward_impl(evx_ch_plan* plan, const float* u_in, float* u_out, int nste
     const float* src = u_in;
     for (int s = 0; s < nsteps; ++s) {
         if (s == 0) {
-            rc = ch_rhs_launch(false, src, nullptr, nullptr, r, g, G, P, st);
+            rc = ch_rhs_launch(false, false, src, nullptr, nullptr, r, g, G, P, st);
         } else {
             float* dst = traj ? traj + (size_t)(s - 1) * N : (((nsteps - 1 - s) % 2 == 0) ? ubuf : u_out);
-            rc = ch_rhs_launch(true, src, upd, dst, r, g, G, P, st);
+            rc = ch_rhs_launch(true, false, src, upd, dst, r, g, G, P, st);
             src = dst;
         }
         if (rc) return rc;

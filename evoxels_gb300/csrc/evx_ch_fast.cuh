@@ -151,8 +151,10 @@ inline bool fast_ok(const evx_grid* g, std::initializer_list<const void*> ptrs) 
 inline int default_tile_variant(int nz) { return (nz % 64 != 0 && nz % 32 == 0) ? 1 : 0; }
 int ch_tile_variant(int nz);   // honours evx_set_tile_variant
 
-int ch_rhs_fast_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
-                       const Geo& G, const ChP& P, cudaStream_t st);
+// exact: the reference's float32 operations in its order (evx_ch_rhs); else the
+// fused-product arithmetic of the spectral loops (always for the fused pass)
+int ch_rhs_fast_launch(bool fused, bool exact, const float* u, const float* upd, float* u_new, float* r,
+                       const evx_grid* g, const Geo& G, const ChP& P, cudaStream_t st);
 // Final gradient reduction of the spectral-gradient pullback (grads == 2), done by
 // the block that finishes last: the blocks' partial sums (part) and the x-pass
 // Parseval partials (xpart: <lam', u'-u>, <K lam', u'-u> per block) in a fixed

@@ -27,34 +27,59 @@ constexpr int RING_C = NC * MAX_FIELD, RING_M = NM * MAX_POT;
 constexpr size_t ADJ_SMEM = (size_t)(2 * RING_C + 2 * RING_M) * sizeof(float) + 4 * 8 * sizeof(double);
 
 // Two points of a patch row (z-adjacent) are processed together with the
-// sm_100 two-lane fp32 instructions (FADD2 / FMUL2 / FFMA2).
+// sm_100 two-lane fp32 instructions (FADD2 / FMUL2 / FFMA2).  Constants are
+// folded into per-axis weights: with s = c_lo + c_hi on a face (cf = s/2),
+//   Gb''  = D*ih2 * cf(1-cf) * (g_lo - g_hi)          = s*(gq2 + gq1*s) * dg
+//   cfb'' = 0.5*D*ih2 * (g_lo - g_hi)(mu_hi - mu_lo)(1 - 2cf) = dg*dmu * (hw - hw*s)
+// so mub = sum_a (Gb''_minus - Gb''_plus) and the 0.5-weighted cbar face sum is a
+// plain sum of cfb''; -kappa is folded into the Laplacian weights.
+struct PbK {
+    float2 gq1[3], gq2[3];   // -D*ih2_a/4, D*ih2_a/2
+    float2 hw[3], nhw[3];    // 0.5*D*ih2_a and its negative
+    float2 lk[3], lkc;       // -kappa*ih2_a, 2*kappa*sum(ih2): -kappa*Laplacian
+    float2 l[3], lc;         // ih2_a, -2*sum(ih2): the Laplacian itself (gradient sums)
+    float2 w, w6, nw6;       // w, 6w, -6w
+};
+__device__ __forceinline__ PbK make_pbk(const Geo& G, const ChP& P) {
+    PbK K;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float dg = P.D * G.ih2[a];
+        K.gq1[a] = f2s(-0.25f * dg);
+        K.gq2[a] = f2s(0.5f * dg);
+        K.hw[a] = f2s(0.5f * dg);
+        K.nhw[a] = f2s(-0.5f * dg);
+        K.lk[a] = f2s(-P.kappa * G.ih2[a]);
+        K.l[a] = f2s(G.ih2[a]);
+    }
+    K.lkc = f2s(2.f * P.kappa * G.ih2sum);
+    K.lc = f2s(-2.f * G.ih2sum);
+    K.w = f2s(P.w);
+    K.w6 = f2s(6.f * P.w);
+    K.nw6 = f2s(-6.f * P.w);
+    return K;
+}
 __device__ __forceinline__ float2 phi2(float2 c) {    // c(1-c)(1-2c)
     return mul2(mul2(c, sub2(f2s(1.f), c)), fma2(c, f2s(-2.f), f2s(1.f)));
 }
-__device__ __forceinline__ float2 dphi2(float2 c) {   // 1 - 6c + 6c^2
-    return fma2(mul2(f2s(6.f), c), sub2(c, f2s(1.f)), f2s(1.f));
+// sum_a wa*(xp_a + xm_a) + c*wc
+__device__ __forceinline__ float2 lapw(const float2 (&wa)[3], float2 wc, float2 c, float2 xm, float2 xp, float2 ym,
+                                       float2 yp, float2 zm, float2 zp) {
+    float2 t = mul2(add2(xp, xm), wa[0]);
+    t = fma2(add2(yp, ym), wa[1], t);
+    t = fma2(add2(zp, zm), wa[2], t);
+    return fma2(c, wc, t);
 }
-struct LapK {   // broadcast Laplacian weights
-    float2 x, y, z, m2sum;   // ih2 per axis, -2*sum(ih2)
-};
-// ((xp+xm)*ih2x + (yp+ym)*ih2y) + (zp+zm)*ih2z - 2c*sum(ih2)
-__device__ __forceinline__ float2 lap2(const LapK& L, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
-                                       float2 zm, float2 zp) {
-    float2 t = mul2(add2(xp, xm), L.x);
-    t = fma2(add2(yp, ym), L.y, t);
-    t = fma2(add2(zp, zm), L.z, t);
-    return fma2(c, L.m2sum, t);
+template <int AX>
+__device__ __forceinline__ float2 gb2(const PbK& K, float2 clo, float2 chi, float2 glo, float2 ghi) {
+    const float2 sm = add2(clo, chi);
+    return mul2(mul2(sm, fma2(sm, K.gq1[AX], K.gq2[AX])), sub2(glo, ghi));
 }
-// Gbar on a face: (ihD*(g_lo - g_hi)) * m(cf), m(x) = x(1-x), cf = (c_lo + c_hi)/2
-__device__ __forceinline__ float2 gbar2(float2 clo, float2 chi, float2 glo, float2 ghi, float2 ihD) {
-    const float2 cf = mul2(f2s(0.5f), add2(clo, chi));
-    return mul2(mul2(ihD, sub2(glo, ghi)), mul2(cf, sub2(f2s(1.f), cf)));
-}
-// cbar on a face: (ihD*(g_lo - g_hi)) * ((mu_hi - mu_lo)*ih) * (1 - 2cf)
-__device__ __forceinline__ float2 cfb2(float2 clo, float2 chi, float2 mlo, float2 mhi, float2 glo, float2 ghi,
-                                       float2 ih, float2 ihD) {
-    const float2 cf = mul2(f2s(0.5f), add2(clo, chi));
-    return mul2(mul2(mul2(ihD, sub2(glo, ghi)), mul2(sub2(mhi, mlo), ih)), fma2(cf, f2s(-2.f), f2s(1.f)));
+template <int AX>
+__device__ __forceinline__ float2 cfb2(const PbK& K, float2 clo, float2 chi, float2 mlo, float2 mhi, float2 glo,
+                                       float2 ghi) {
+    const float2 sm = add2(clo, chi);
+    return mul2(mul2(sub2(glo, ghi), sub2(mhi, mlo)), fma2(sm, K.nhw[AX], K.hw[AX]));
 }
 __device__ __forceinline__ float2 sel2(bool px, bool py, float2 v) {
     return make_float2(px ? v.x : 0.f, py ? v.y : 0.f);
@@ -134,20 +159,16 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     const int W = T::W;
     const int nx = G.nx, ny = G.ny, nz = G.nz;
     const size_t plane = (size_t)ny * nz;
-    const float2 ihx = f2s(G.ih[0]), ihy = f2s(G.ih[1]), ihz = f2s(G.ih[2]);
-    const float2 ihDx = f2s(G.ih[0] * P.D), ihDy = f2s(G.ih[1] * P.D), ihDz = f2s(G.ih[2] * P.D);
-    const float2 w2 = f2s(P.w), mk2 = f2s(-P.kappa);
-    const LapK L{f2s(G.ih2[0]), f2s(G.ih2[1]), f2s(G.ih2[2]), f2s(-2.f * G.ih2sum)};
+    const PbK K = make_pbk(G, P);
     const LoadPlan LP = make_load_plan<T>(tid, j0, k0, ny, nz);
-    int mr[2], mc[2];
+    int mo_[2];   // field offsets of the potential patches (upper row, left column)
     bool mv[2];
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
         const int pidx = tid + m * THREADS;
         mv[m] = pidx < T::NMU;
         const int py = mv[m] ? pidx / T::MPZ : 0;
-        mr[m] = 1 + 2 * py;
-        mc[m] = 2 + 2 * (pidx - py * T::MPZ);
+        mo_[m] = (1 + 2 * py) * W + 2 + 2 * (pidx - py * T::MPZ);
     }
     const int ra = 2 + 2 * ty, rc = 4 + 2 * tx;
     const int gj = j0 + 2 * ty, gk = k0 + 2 * tx;
@@ -165,9 +186,9 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             pg[s] = ldg4(gfield + base + LP.goff[s]);
         }
     };
-    auto stash = [&](int p) {
-        float* dc = cs + cslt(p) * T::FIELD;
-        float* dg = gs + cslt(p) * T::FIELD;
+    auto stash = [&](int slot) {
+        float* dc = cs + slot * T::FIELD;
+        float* dg = gs + slot * T::FIELD;
 #pragma unroll
         for (int s = 0; s < 2; ++s)
             if (LP.valid[s]) {
@@ -176,87 +197,74 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             }
     };
 
-    float2 gxm[2][2];   // Gbar on the x face below the current potential plane, per patch row
-    auto gx_faces = [&](int plo, int m, float2 out[2]) {
-        const float* c0 = cs + cslt(plo) * T::FIELD;
-        const float* c1 = cs + cslt(plo + 1) * T::FIELD;
-        const float* g0 = gs + cslt(plo) * T::FIELD;
-        const float* g1 = gs + cslt(plo + 1) * T::FIELD;
-        const int a = mr[m] * W + mc[m], b = a + W;
-        out[0] = gbar2(lds2(c0 + a), lds2(c1 + a), lds2(g0 + a), lds2(g1 + a), ihDx);
-        out[1] = gbar2(lds2(c0 + b), lds2(c1 + b), lds2(g0 + b), lds2(g1 + b), ihDx);
+    float2 gxm[2][2];   // Gb'' on the x face below the current potential plane, per patch row
+    // x faces between field slots c0/g0 (plane p) and c1/g1 (plane p+1) of potential patch m
+    auto gx_faces = [&](const float* c0, const float* c1, const float* g0, const float* g1, int m, float2 out[2]) {
+        const int a = mo_[m], b = a + W;
+        out[0] = gb2<0>(K, lds2(c0 + a), lds2(c1 + a), lds2(g0 + a), lds2(g1 + a));
+        out[1] = gb2<0>(K, lds2(c0 + b), lds2(c1 + b), lds2(g0 + b), lds2(g1 + b));
     };
 
-    auto compute_mu = [&](int p) {
-        const float* cc = cs + cslt(p) * T::FIELD;
-        const float* cm = cs + cslt(p - 1) * T::FIELD;
-        const float* cp = cs + cslt(p + 1) * T::FIELD;
-        const float* gc = gs + cslt(p) * T::FIELD;
-        float* mo = ms + mslt(p) * T::POT;
-        float* bo = bs + mslt(p) * T::POT;
+    // mu and mub of plane p: field slots cm (p-1), cc (p), cp (p+1) and g slots gc (p), gp (p+1);
+    // writes potential slots mo / bo
+    auto compute_mu = [&](const float* cm, const float* cc, const float* cp, const float* gc, const float* gp,
+                          float* mo, float* bo) {
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
             if (!mv[m]) continue;
-            const int a = mr[m] * W + mc[m], b = a + W;
+            const int a = mo_[m], b = a + W;
             const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
             const float2 zmA = make_float2(cc[a - 1], A.x), zpA = make_float2(A.y, cc[a + 2]);
             const float2 zmB = make_float2(cc[b - 1], B.x), zpB = make_float2(B.y, cc[b + 2]);
             // chemical potential w*phi(c) - kappa*L(c) on the 2x2 patch
-            const float2 muA = fma2(w2, phi2(A), mul2(mk2, lap2(L, A, lds2(cm + a), lds2(cp + a), up, B, zmA, zpA)));
-            const float2 muB = fma2(w2, phi2(B), mul2(mk2, lap2(L, B, lds2(cm + b), lds2(cp + b), A, dn, zmB, zpB)));
+            const float2 muA = fma2(K.w, phi2(A), lapw(K.lk, K.lkc, A, lds2(cm + a), lds2(cp + a), up, B, zmA, zpA));
+            const float2 muB = fma2(K.w, phi2(B), lapw(K.lk, K.lkc, B, lds2(cm + b), lds2(cp + b), A, dn, zmB, zpB));
             *reinterpret_cast<float2*>(mo + a - W) = muA;
             *reinterpret_cast<float2*>(mo + b - W) = muB;
-            // mub = sum_faces ih*(Gb_minus - Gb_plus)
+            // mub = sum_faces (Gb''_minus - Gb''_plus)
             float2 gxp[2];
-            gx_faces(p, m, gxp);
-            float2 bA = mul2(sub2(gxm[m][0], gxp[0]), ihx);
-            float2 bB = mul2(sub2(gxm[m][1], gxp[1]), ihx);
+            gx_faces(cc, cp, gc, gp, m, gxp);
+            float2 bA = sub2(gxm[m][0], gxp[0]);
+            float2 bB = sub2(gxm[m][1], gxp[1]);
             gxm[m][0] = gxp[0];
             gxm[m][1] = gxp[1];
             const float2 gup = lds2(gc + a - W), gA = lds2(gc + a), gB = lds2(gc + b), gdn = lds2(gc + b + W);
             {   // z faces: (left, mid) and (mid, right) of each row
                 const float2 gzmA = make_float2(gc[a - 1], gA.x), gzpA = make_float2(gA.y, gc[a + 2]);
                 const float2 gzmB = make_float2(gc[b - 1], gB.x), gzpB = make_float2(gB.y, gc[b + 2]);
-                bA = fma2(sub2(gbar2(zmA, A, gzmA, gA, ihDz), gbar2(A, zpA, gA, gzpA, ihDz)), ihz, bA);
-                bB = fma2(sub2(gbar2(zmB, B, gzmB, gB, ihDz), gbar2(B, zpB, gB, gzpB, ihDz)), ihz, bB);
+                bA = add2(bA, sub2(gb2<2>(K, zmA, A, gzmA, gA), gb2<2>(K, A, zpA, gA, gzpA)));
+                bB = add2(bB, sub2(gb2<2>(K, zmB, B, gzmB, gB), gb2<2>(K, B, zpB, gB, gzpB)));
             }
             {   // y faces above, between and below the two rows
-                const float2 y0 = gbar2(up, A, gup, gA, ihDy), y1 = gbar2(A, B, gA, gB, ihDy);
-                const float2 y2 = gbar2(B, dn, gB, gdn, ihDy);
-                bA = fma2(sub2(y0, y1), ihy, bA);
-                bB = fma2(sub2(y1, y2), ihy, bB);
+                const float2 y0 = gb2<1>(K, up, A, gup, gA), y1 = gb2<1>(K, A, B, gA, gB);
+                const float2 y2 = gb2<1>(K, B, dn, gB, gdn);
+                bA = add2(bA, sub2(y0, y1));
+                bB = add2(bB, sub2(y1, y2));
             }
             *reinterpret_cast<float2*>(bo + a - W) = bA;
             *reinterpret_cast<float2*>(bo + b - W) = bB;
         }
     };
 
-    // x face cbar of the output patch between planes plo and plo+1
+    // x face cbar'' of the output patch between planes (c0, g0, m0) and (c1, g1, m1)
     float2 cfx_m[2], c_prev[2], b_prev[2];
-    auto x_faces_b = [&](int plo, float2 out[2]) {
-        const float* c0 = cs + cslt(plo) * T::FIELD;
-        const float* c1 = cs + cslt(plo + 1) * T::FIELD;
-        const float* g0 = gs + cslt(plo) * T::FIELD;
-        const float* g1 = gs + cslt(plo + 1) * T::FIELD;
-        const float* m0 = ms + mslt(plo) * T::POT;
-        const float* m1 = ms + mslt(plo + 1) * T::POT;
-        out[0] = cfb2(lds2(c0 + pa), lds2(c1 + pa), lds2(m0 + pa - W), lds2(m1 + pa - W), lds2(g0 + pa),
-                      lds2(g1 + pa), ihx, ihDx);
-        out[1] = cfb2(lds2(c0 + pb), lds2(c1 + pb), lds2(m0 + pb - W), lds2(m1 + pb - W), lds2(g0 + pb),
-                      lds2(g1 + pb), ihx, ihDx);
+    auto x_faces_b = [&](const float* c0, const float* c1, const float* g0, const float* g1, const float* m0,
+                         const float* m1, float2 out[2]) {
+        out[0] = cfb2<0>(K, lds2(c0 + pa), lds2(c1 + pa), lds2(m0 + pa - W), lds2(m1 + pa - W), lds2(g0 + pa),
+                         lds2(g1 + pa));
+        out[1] = cfb2<0>(K, lds2(c0 + pb), lds2(c1 + pb), lds2(m0 + pb - W), lds2(m1 + pb - W), lds2(g0 + pb),
+                         lds2(g1 + pb));
     };
 
-    auto compute_lam = [&](int i) {
-        const float* cc = cs + cslt(i) * T::FIELD;
-        const float* gc = gs + cslt(i) * T::FIELD;
-        const float* mm = ms + mslt(i) * T::POT;
-        const float* bb = bs + mslt(i) * T::POT;
-        const float* bp = bs + mslt(i + 1) * T::POT;
-        // acc: sum of cbar-face values around each point (times 0.5 at the end)
+    // lam on plane i: field slots cc (i), cx (i+1), g slots gc (i), gx (i+1), potential slots mm / bb (i)
+    // and mx / bx (i+1)
+    auto compute_lam = [&](int i, const float* cc, const float* cx, const float* gc, const float* gx,
+                           const float* mm, const float* mx, const float* bb, const float* bx) {
+        // acc: sum of the cbar'' face values around each point
         float2 accA, accB;
         {
             float2 cfx_p[2];
-            x_faces_b(i, cfx_p);
+            x_faces_b(cc, cx, gc, gx, mm, mx, cfx_p);
             accA = add2(cfx_m[0], cfx_p[0]);
             accB = add2(cfx_m[1], cfx_p[1]);
             cfx_m[0] = cfx_p[0];
@@ -272,41 +280,41 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             const float2 mzmB = make_float2(mm[pb - W - 1], MB.x), mzpB = make_float2(MB.y, mm[pb - W + 2]);
             const float2 gzmA = make_float2(gc[pa - 1], gA.x), gzpA = make_float2(gA.y, gc[pa + 2]);
             const float2 gzmB = make_float2(gc[pb - 1], gB.x), gzpB = make_float2(gB.y, gc[pb + 2]);
-            accA = add2(accA, add2(cfb2(zmA, A, mzmA, MA, gzmA, gA, ihz, ihDz), cfb2(A, zpA, MA, mzpA, gA, gzpA, ihz, ihDz)));
-            accB = add2(accB, add2(cfb2(zmB, B, mzmB, MB, gzmB, gB, ihz, ihDz), cfb2(B, zpB, MB, mzpB, gB, gzpB, ihz, ihDz)));
+            accA = add2(accA, add2(cfb2<2>(K, zmA, A, mzmA, MA, gzmA, gA), cfb2<2>(K, A, zpA, MA, mzpA, gA, gzpA)));
+            accB = add2(accB, add2(cfb2<2>(K, zmB, B, mzmB, MB, gzmB, gB), cfb2<2>(K, B, zpB, MB, mzpB, gB, gzpB)));
         }
         {   // y faces
             const float2 mup = lds2(mm + pa - 2 * W), mdn = lds2(mm + pb);
             const float2 gup = lds2(gc + pa - W), gdn = lds2(gc + pb + W);
-            const float2 y0 = cfb2(up, A, mup, MA, gup, gA, ihy, ihDy), y1 = cfb2(A, B, MA, MB, gA, gB, ihy, ihDy);
-            const float2 y2 = cfb2(B, dn, MB, mdn, gB, gdn, ihy, ihDy);
+            const float2 y0 = cfb2<1>(K, up, A, mup, MA, gup, gA), y1 = cfb2<1>(K, A, B, MA, MB, gA, gB);
+            const float2 y2 = cfb2<1>(K, B, dn, MB, mdn, gB, gdn);
             accA = add2(accA, add2(y0, y1));
             accB = add2(accB, add2(y1, y2));
         }
-        // Laplacian of mub
+        // -kappa*L(mub) + acc
         const float2 bA = lds2(bb + pa - W), bB = lds2(bb + pb - W);
-        const float2 LbA = lap2(L, bA, b_prev[0], lds2(bp + pa - W), lds2(bb + pa - 2 * W), bB,
-                                make_float2(bb[pa - W - 1], bA.x), make_float2(bA.y, bb[pa - W + 2]));
-        const float2 LbB = lap2(L, bB, b_prev[1], lds2(bp + pb - W), bA, lds2(bb + pb),
-                                make_float2(bb[pb - W - 1], bB.x), make_float2(bB.y, bb[pb - W + 2]));
+        const float2 tA = add2(accA, lapw(K.lk, K.lkc, bA, b_prev[0], lds2(bx + pa - W), lds2(bb + pa - 2 * W), bB,
+                                          make_float2(bb[pa - W - 1], bA.x), make_float2(bA.y, bb[pa - W + 2])));
+        const float2 tB = add2(accB, lapw(K.lk, K.lkc, bB, b_prev[1], lds2(bx + pb - W), bA, lds2(bb + pb),
+                                          make_float2(bb[pb - W - 1], bB.x), make_float2(bB.y, bb[pb - W + 2])));
         const size_t o = (size_t)i * plane + (size_t)gj * nz + gk;
         const float2 u0 = wj0 ? __ldg(reinterpret_cast<const float2*>(u + o)) : f2s(0.f);
         const float2 u1r = wj1 ? __ldg(reinterpret_cast<const float2*>(u + o + nz)) : f2s(0.f);
         const float2 l0 = wj0 ? __ldg(reinterpret_cast<const float2*>(lam + o)) : f2s(0.f);
         const float2 l1 = wj1 ? __ldg(reinterpret_cast<const float2*>(lam + o + nz)) : f2s(0.f);
         {
-            // cbar = w*phi'(c)*mub - kappa*L(mub) + 0.5*acc; lam_s = lam' + [0<=u<=1]*cbar
-            const float2 cbA = fma2(mul2(w2, dphi2(A)), bA, fma2(mk2, LbA, mul2(f2s(0.5f), accA)));
-            const float2 cbB = fma2(mul2(w2, dphi2(B)), bB, fma2(mk2, LbB, mul2(f2s(0.5f), accB)));
-            const float2 oA = add2(l0, sel2(u0.x >= 0.f && u0.x <= 1.f, u0.y >= 0.f && u0.y <= 1.f, cbA));
-            const float2 oB = add2(l1, sel2(u1r.x >= 0.f && u1r.x <= 1.f, u1r.y >= 0.f && u1r.y <= 1.f, cbB));
+            // cbar = w*phi'(c)*mub - kappa*L(mub) + acc, w*phi'(c) = w + c*(6w*c - 6w);
+            // lam_s = lam' + [0<=u<=1]*cbar, the mask being clip(u) == u
+            const float2 cbA = fma2(fma2(A, fma2(A, K.w6, K.nw6), K.w), bA, tA);
+            const float2 cbB = fma2(fma2(B, fma2(B, K.w6, K.nw6), K.w), bB, tB);
+            const float2 oA = add2(l0, sel2(A.x == u0.x, A.y == u0.y, cbA));
+            const float2 oB = add2(l1, sel2(B.x == u1r.x, B.y == u1r.y, cbB));
             if (wj0) *reinterpret_cast<float2*>(lam_out + o) = oA;
             if (wj1) *reinterpret_cast<float2*>(lam_out + o + nz) = oB;
         }
         if (GR) {
-            const float* cx = cs + cslt(i + 1) * T::FIELD;
-            const float2 lcA = lap2(L, A, c_prev[0], lds2(cx + pa), up, B, zmA, zpA);
-            const float2 lcB = lap2(L, B, c_prev[1], lds2(cx + pb), A, dn, zmB, zpB);
+            const float2 lcA = lapw(K.l, K.lc, A, c_prev[0], lds2(cx + pa), up, B, zmA, zpA);
+            const float2 lcB = lapw(K.l, K.lc, B, c_prev[1], lds2(cx + pb), A, dn, zmB, zpB);
             if (wj0) {
                 aK = fma2(mul2(f2s(-1.f), bA), lcA, aK);
                 aW = fma2(bA, phi2(A), aW);
@@ -334,69 +342,89 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         b_prev[1] = bB;
     };
 
+    const float* C = cs;
+    const float* Gf = gs;
+    auto cf = [&](int slot) { return C + slot * T::FIELD; };
+    auto gf = [&](int slot) { return Gf + slot * T::FIELD; };
+    auto mp = [&](int slot) { return ms + slot * T::POT; };
+    auto bp = [&](int slot) { return bs + slot * T::POT; };
+    // potential of plane p from the field slots of p-1, p, p+1
+    auto mu_of = [&](int p) {
+        const int s0 = cslt(p - 1), s1 = cslt(p), s2 = cslt(p + 1), t = mslt(p);
+        compute_mu(cf(s0), cf(s1), cf(s2), gf(s1), gf(s2), mp(t), bp(t));
+    };
+
     if (ONEBAR) {
         // prologue: planes x0-2 .. x0+2 staged; potentials x0-1 .. x0+1; plane
         // x0+3 staged into the slot of x0-2; carried x quantities.  Planes up to
         // x1+1 and potentials up to x1 are needed.
         for (int p = x0 - 2; p <= x0 + 2; ++p) {
             fetch(p);
-            stash(p);
+            stash(cslt(p));
         }
         fetch(x0 + 3);
         __syncthreads();
 #pragma unroll
         for (int m = 0; m < 2; ++m)
-            if (mv[m]) gx_faces(x0 - 2, m, gxm[m]);
-        compute_mu(x0 - 1);
-        compute_mu(x0);
-        compute_mu(x0 + 1);
+            if (mv[m]) gx_faces(cf(cslt(x0 - 2)), cf(cslt(x0 - 1)), gf(cslt(x0 - 2)), gf(cslt(x0 - 1)), m, gxm[m]);
+        mu_of(x0 - 1);
+        mu_of(x0);
+        mu_of(x0 + 1);
         __syncthreads();
-        if (x0 + 3 <= x1 + 1) stash(x0 + 3);
+        if (x0 + 3 <= x1 + 1) stash(cslt(x0 + 3));
         if (x0 + 4 <= x1 + 1) fetch(x0 + 4);
     } else {
         // prologue: planes x0-2 .. x0+1 staged; potentials x0-1, x0
         for (int p = x0 - 2; p <= x0 + 1; ++p) {
             fetch(p);
-            stash(p);
+            stash(cslt(p));
         }
         fetch(x0 + 2);
         __syncthreads();
 #pragma unroll
         for (int m = 0; m < 2; ++m)
-            if (mv[m]) gx_faces(x0 - 2, m, gxm[m]);
-        compute_mu(x0 - 1);
-        compute_mu(x0);
+            if (mv[m]) gx_faces(cf(cslt(x0 - 2)), cf(cslt(x0 - 1)), gf(cslt(x0 - 2)), gf(cslt(x0 - 1)), m, gxm[m]);
+        mu_of(x0 - 1);
+        mu_of(x0);
         __syncthreads();
     }
-    x_faces_b(x0 - 1, cfx_m);
     {
-        const float* cprev = cs + cslt(x0 - 1) * T::FIELD;
-        const float* bprev = bs + mslt(x0 - 1) * T::POT;
-        c_prev[0] = lds2(cprev + pa);
-        c_prev[1] = lds2(cprev + pb);
-        b_prev[0] = lds2(bprev + pa - W);
-        b_prev[1] = lds2(bprev + pb - W);
+        const int s0 = cslt(x0 - 1), s1 = cslt(x0), t0 = mslt(x0 - 1), t1 = mslt(x0);
+        x_faces_b(cf(s0), cf(s1), gf(s0), gf(s1), mp(t0), mp(t1), cfx_m);
+        c_prev[0] = lds2(cf(s0) + pa);
+        c_prev[1] = lds2(cf(s0) + pb);
+        b_prev[0] = lds2(bp(t0) + pa - W);
+        b_prev[1] = lds2(bp(t0) + pb - W);
     }
     if (ONEBAR) {
         __syncthreads();
         // plane i: lam(i) reads potentials i, i+1 and planes i, i+1; mu(i+2) reads
         // planes i+1 .. i+3 and writes the potential slot of i-1; the stash of
-        // plane i+4 overwrites the slot of plane i-1 - all last read before the barrier
+        // plane i+4 overwrites the slot of plane i-1 - all last read before the barrier.
+        // Slots of planes i .. i+4 (all five) and potentials i .. i+2 (all three),
+        // advanced by one per plane.
+        int c0 = cslot(x0), m0 = mslot(x0);
         for (int i = x0; i < x1; ++i) {
-            compute_lam(i);
-            if (i + 2 <= x1) compute_mu(i + 2);
-            if (i + 4 <= x1 + 1) stash(i + 4);
+            const int c1 = c0 + 1 == NC ? 0 : c0 + 1, c2 = c1 + 1 == NC ? 0 : c1 + 1;
+            const int c3 = c2 + 1 == NC ? 0 : c2 + 1, c4 = c3 + 1 == NC ? 0 : c3 + 1;
+            const int m1 = m0 + 1 == NM ? 0 : m0 + 1, m2 = m1 + 1 == NM ? 0 : m1 + 1;
+            compute_lam(i, cf(c0), cf(c1), gf(c0), gf(c1), mp(m0), mp(m1), bp(m0), bp(m1));
+            if (i + 2 <= x1) compute_mu(cf(c1), cf(c2), cf(c3), gf(c2), gf(c3), mp(m2), bp(m2));
+            if (i + 4 <= x1 + 1) stash(c4);
             if (i + 5 <= x1 + 1) fetch(i + 5);
             __syncthreads();
+            c0 = c1;
+            m0 = m1;
         }
     } else {
         for (int i = x0; i < x1; ++i) {
-            stash(i + 2);
+            stash(cslt(i + 2));
             if (i + 3 <= x1 + 1) fetch(i + 3);
             __syncthreads();
-            compute_mu(i + 1);
+            mu_of(i + 1);
             __syncthreads();
-            compute_lam(i);
+            const int s0 = cslt(i), s1 = cslt(i + 1), t0 = mslt(i), t1 = mslt(i + 1);
+            compute_lam(i, cf(s0), cf(s1), gf(s0), gf(s1), mp(t0), mp(t1), bp(t0), bp(t1));
         }
     }
     sD += aD.x + aD.y;

@@ -1,7 +1,13 @@
 // Periodic fast path of the Cahn-Hilliard right-hand side (tiling in
-// evx_ch_fast.cuh).  Same float32 operations, in the same order, as the generic
-// kernel and the reference (evoxels/problem_definition.py:350-371); the
-// translation unit is compiled with --fmad=false, so results are bit-identical.
+// evx_ch_fast.cuh), in two arithmetic forms:
+// * ExactMath: the same float32 operations, in the same order, as the generic
+//   kernel and the reference (evoxels/problem_definition.py:350-371); the
+//   translation unit is compiled with --fmad=false, so evx_ch_rhs is
+//   bit-identical to the reference.
+// * TolMath: the same formula with the constants folded and products fused
+//   (two-lane FFMA2), for the rhs passes inside the spectral loops (IMEX and
+//   exponential Euler steps, single and batched), whose FFT already differs
+//   from the reference's in the last bits; about 40% fewer instructions.
 //
 // Per x-plane i a tile: computes r on plane i, the chemical potential of plane
 // i+2 over the tile grown by one cell (3-slot ring), stores the prefetched
@@ -17,40 +23,100 @@ namespace evx {
 namespace {
 
 using namespace fast;
-using exact::add2;
-using exact::mul2;
-using exact::sub2;
-using exact::mul2_nofuse;
 
 // Two z-adjacent points at a time (two-lane sums, scalar products); every lane
 // performs exactly the scalar operations of lap7 / mu_hom / face_flux
 // (evx_common.cuh) in the same order, so results stay bit-identical.
-struct RhsK {   // broadcast constants
-    float2 ih2x, ih2y, ih2z, ih2sum, w, kappa, D, ihx, ihy, ihz;
+struct ExactMath {
+    struct C {   // broadcast constants
+        float2 ih2x, ih2y, ih2z, ih2sum, w, kappa, D, ih[3];
+        int bulk;
+    };
+    static __device__ __forceinline__ C make(const Geo& G, const ChP& P) {
+        return C{f2s(G.ih2[0]), f2s(G.ih2[1]), f2s(G.ih2[2]), f2s(G.ih2sum), f2s(P.w), f2s(P.kappa), f2s(P.D),
+                 {f2s(G.ih[0]), f2s(G.ih[1]), f2s(G.ih[2])}, P.bulk};
+    }
+    static __device__ __forceinline__ float2 lap(const C& K, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
+                                                 float2 zm, float2 zp) {
+        using exact::add2; using exact::sub2; using exact::mul2; using exact::mul2_nofuse;
+        float2 t = mul2(add2(xp, xm), K.ih2x);
+        t = add2(t, mul2(add2(yp, ym), K.ih2y));
+        t = add2(t, mul2(add2(zp, zm), K.ih2z));
+        return sub2(t, mul2(mul2_nofuse(f2s(2.f), c), K.ih2sum));
+    }
+    // mu = w*c*(1-c)*(1-2c) - kappa*lap(c)
+    static __device__ __forceinline__ float2 mu(const C& K, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
+                                                float2 zm, float2 zp) {
+        using exact::add2; using exact::sub2; using exact::mul2; using exact::mul2_nofuse;
+        float2 h;
+        if (K.bulk == EVX_BULK_REGULAR_SOLUTION) {
+            h = make_float2(mu_regular(K.w.x, c.x), mu_regular(K.w.x, c.y));
+        } else {
+            h = mul2_nofuse(K.w, c);                              // feeds a product
+            h = mul2_nofuse(h, sub2(f2s(1.f), c));                // feeds a product
+            h = mul2(h, sub2(f2s(1.f), mul2_nofuse(f2s(2.f), c)));   // 2c exact
+        }
+        return sub2(h, mul2(K.kappa, lap(K, c, xm, xp, ym, yp, zm, zp)));
+    }
+    // (cf*(1-cf)) * ((mu_hi - mu_lo)*ih), cf = 0.5*(c_hi + c_lo)
+    template <int AX>
+    static __device__ __forceinline__ float2 flux(const C& K, float2 clo, float2 chi, float2 mlo, float2 mhi) {
+        using exact::add2; using exact::sub2; using exact::mul2; using exact::mul2_nofuse;
+        const float2 cf = mul2_nofuse(f2s(0.5f), add2(chi, clo));   // exact
+        const float2 m = mul2_nofuse(cf, sub2(f2s(1.f), cf));        // feeds a product
+        return mul2(m, mul2_nofuse(sub2(mhi, mlo), K.ih[AX]));       // the inner one feeds a product
+    }
+    static __device__ __forceinline__ float2 div(const C& K, float2 fxp, float2 fxm, float2 fyp, float2 fym,
+                                                 float2 fzp, float2 fzm) {
+        using exact::add2; using exact::sub2; using exact::mul2; using exact::mul2_nofuse;
+        float2 d = mul2(sub2(fxp, fxm), K.ih[0]);
+        d = add2(d, mul2(sub2(fyp, fym), K.ih[1]));
+        d = add2(d, mul2(sub2(fzp, fzm), K.ih[2]));
+        return mul2_nofuse(K.D, d);   // the result is stored
+    }
 };
-__device__ __forceinline__ float2 lap7x2(const RhsK& K, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
-                                         float2 zm, float2 zp) {
-    float2 t = mul2(add2(xp, xm), K.ih2x);
-    t = add2(t, mul2(add2(yp, ym), K.ih2y));
-    t = add2(t, mul2(add2(zp, zm), K.ih2z));
-    return sub2(t, mul2(mul2_nofuse(f2s(2.f), c), K.ih2sum));
-}
-// mu = w*c*(1-c)*(1-2c) - kappa*lap(c)
-__device__ __forceinline__ float2 mu_x2(const RhsK& K, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
-                                        float2 zm, float2 zp) {
-    float2 h = mul2_nofuse(K.w, c);                       // feeds a product
-    h = mul2_nofuse(h, sub2(f2s(1.f), c));                // feeds a product
-    h = mul2(h, sub2(f2s(1.f), mul2_nofuse(f2s(2.f), c)));   // 2c exact
-    return sub2(h, mul2(K.kappa, lap7x2(K, c, xm, xp, ym, yp, zm, zp)));
-}
-// (cf*(1-cf)) * ((mu_hi - mu_lo)*ih), cf = 0.5*(c_hi + c_lo)
-__device__ __forceinline__ float2 flux_x2(float2 clo, float2 chi, float2 mlo, float2 mhi, float2 ih) {
-    const float2 cf = mul2_nofuse(f2s(0.5f), add2(chi, clo));   // exact
-    const float2 m = mul2_nofuse(cf, sub2(f2s(1.f), cf));        // feeds a product
-    return mul2(m, mul2_nofuse(sub2(mhi, mlo), ih));             // the inner one feeds a product
-}
 
-template <class T, bool FUSED>
+// The same rhs with the constants folded: -kappa into the Laplacian weights,
+// D*ih^2 into the divergence weights (the face flux is c(1-c)*(mu_hi - mu_lo)
+// with cf(1-cf) = s*(1/2 - s/4), s = c_lo + c_hi), every product fused where
+// it feeds a sum.
+struct TolMath {
+    struct C {
+        float2 lx, ly, lz, lc, w, dx, dy, dz;   // -kappa*ih2_a, 2*kappa*sum(ih2), w, D*ih2_a
+        int bulk;
+    };
+    static __device__ __forceinline__ C make(const Geo& G, const ChP& P) {
+        return C{f2s(-P.kappa * G.ih2[0]), f2s(-P.kappa * G.ih2[1]), f2s(-P.kappa * G.ih2[2]),
+                 f2s(2.f * P.kappa * G.ih2sum), f2s(P.w), f2s(P.D * G.ih2[0]), f2s(P.D * G.ih2[1]),
+                 f2s(P.D * G.ih2[2]), P.bulk};
+    }
+    static __device__ __forceinline__ float2 mu(const C& K, float2 c, float2 xm, float2 xp, float2 ym, float2 yp,
+                                                float2 zm, float2 zp) {
+        float2 t = mul2(add2(xp, xm), K.lx);
+        t = fma2(add2(yp, ym), K.ly, t);
+        t = fma2(add2(zp, zm), K.lz, t);
+        t = fma2(c, K.lc, t);                                     // -kappa*lap(c)
+        if (K.bulk == EVX_BULK_REGULAR_SOLUTION) {                // log(c) - log(1-c) + w*(1-2c)
+            const float2 lg = make_float2(logf(c.x) - logf(1.f - c.x), logf(c.y) - logf(1.f - c.y));
+            return add2(fma2(K.w, fma2(c, f2s(-2.f), f2s(1.f)), lg), t);
+        }
+        const float2 h = mul2(mul2(K.w, c), sub2(f2s(1.f), c));  // w*c*(1-c)
+        return fma2(h, fma2(c, f2s(-2.f), f2s(1.f)), t);
+    }
+    template <int AX>
+    static __device__ __forceinline__ float2 flux(const C&, float2 clo, float2 chi, float2 mlo, float2 mhi) {
+        const float2 sm = add2(clo, chi);
+        return mul2(mul2(sm, fma2(sm, f2s(-0.25f), f2s(0.5f))), sub2(mhi, mlo));
+    }
+    static __device__ __forceinline__ float2 div(const C& K, float2 fxp, float2 fxm, float2 fyp, float2 fym,
+                                                 float2 fzp, float2 fzm) {
+        float2 d = mul2(sub2(fxp, fxm), K.dx);
+        d = fma2(sub2(fyp, fym), K.dy, d);
+        return fma2(sub2(fzp, fzm), K.dz, d);
+    }
+};
+
+template <class T, bool FUSED, class M, bool DEFER>
 __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const float* __restrict__ upd,
                                          float* __restrict__ u_new, float* __restrict__ r, const Geo& G,
                                          const ChP& P, int k0, int j0, int x0, int x1, float* cs, float* ms) {
@@ -75,32 +141,42 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
     const int ra = 2 + 2 * ty, rc = 4 + 2 * tx;    // field row / column in shared memory
     const int gj = j0 + 2 * ty, gk = k0 + 2 * tx;   // global y / z of the patch origin
     const bool wk = gk < nz, wj0 = gj < ny && wk, wj1 = gj + 1 < ny && wk;
-    const RhsK K{f2s(G.ih2[0]), f2s(G.ih2[1]), f2s(G.ih2[2]), f2s(G.ih2sum), f2s(P.w), f2s(P.kappa), f2s(P.D),
-                 f2s(G.ih[0]), f2s(G.ih[1]), f2s(G.ih[2])};
+    const typename M::C K = M::make(G, P);
 
-    float4 pf[2];
+    // The loads of a plane are issued one plane ahead and consumed by its stash.  In the fused pass
+    // the update is added (and u_n stored) at the stash with DEFER, so no thread waits on its own
+    // prefetch; without DEFER (fewer registers: the persistent batched kernel) right after the loads.
+    float4 pf[2], pd[DEFER && FUSED ? 2 : 1];
+    auto add_store = [&](int p, size_t base, int s, float4 a, float4 d) {
+        const float2 lo = exact::add2(make_float2(a.x, a.y), make_float2(d.x, d.y));
+        const float2 hi = exact::add2(make_float2(a.z, a.w), make_float2(d.z, d.w));
+        a = make_float4(lo.x, lo.y, hi.x, hi.y);
+        if (p >= x0 && p < x1 && LP.own[s]) *reinterpret_cast<float4*>(u_new + base + LP.goff[s]) = a;
+        return a;
+    };
     auto fetch = [&](int p) {
         const size_t base = (size_t)pmod(p, nx) * plane;
-        const bool own_plane = p >= x0 && p < x1;
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
             if (!LP.valid[s]) continue;
-            float4 a = ldg4(u + base + LP.goff[s]);
+            pf[s] = ldg4(u + base + LP.goff[s]);
             if (FUSED) {
                 const float4 d = ldg4(upd + base + LP.goff[s]);
-                const float2 lo = add2(make_float2(a.x, a.y), make_float2(d.x, d.y));
-                const float2 hi = add2(make_float2(a.z, a.w), make_float2(d.z, d.w));
-                a = make_float4(lo.x, lo.y, hi.x, hi.y);
-                if (own_plane && LP.own[s]) *reinterpret_cast<float4*>(u_new + base + LP.goff[s]) = a;
+                if constexpr (DEFER) pd[s] = d;
+                else pf[s] = add_store(p, base, s, pf[s], d);
             }
-            pf[s] = a;
         }
     };
     auto stash = [&](int p) {
         float* dst = cs + cslot(p) * T::FIELD;
+        const size_t base = (size_t)pmod(p, nx) * plane;
 #pragma unroll
-        for (int s = 0; s < 2; ++s)
-            if (LP.valid[s]) sts4(dst + LP.soff[s], clip4(pf[s]));
+        for (int s = 0; s < 2; ++s) {
+            if (!LP.valid[s]) continue;
+            float4 a = pf[s];
+            if constexpr (FUSED && DEFER) a = add_store(p, base, s, a, pd[s]);
+            sts4(dst + LP.soff[s], clip4(a));
+        }
     };
     auto compute_mu = [&](int p) {
         const float* cc = cs + cslot(p) * T::FIELD;
@@ -115,8 +191,8 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
             const float2 zmA = make_float2(cc[a - 1], A.x), zpA = make_float2(A.y, cc[a + 2]);
             const float2 zmB = make_float2(cc[b - 1], B.x), zpB = make_float2(B.y, cc[b + 2]);
             // potential row = field row - 1
-            *reinterpret_cast<float2*>(mo + a - W) = mu_x2(K, A, lds2(cm + a), lds2(cp + a), up, B, zmA, zpA);
-            *reinterpret_cast<float2*>(mo + b - W) = mu_x2(K, B, lds2(cm + b), lds2(cp + b), A, dn, zmB, zpB);
+            *reinterpret_cast<float2*>(mo + a - W) = M::mu(K, A, lds2(cm + a), lds2(cp + a), up, B, zmA, zpA);
+            *reinterpret_cast<float2*>(mo + b - W) = M::mu(K, B, lds2(cm + b), lds2(cp + b), A, dn, zmB, zpB);
         }
     };
 
@@ -127,8 +203,8 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
         const float* m0 = ms + mslot(plo) * T::POT;
         const float* m1 = ms + mslot(plo + 1) * T::POT;
         const int a = ra * W + rc, b = a + W;
-        out[0] = flux_x2(lds2(c0 + a), lds2(c1 + a), lds2(m0 + a - W), lds2(m1 + a - W), K.ihx);
-        out[1] = flux_x2(lds2(c0 + b), lds2(c1 + b), lds2(m0 + b - W), lds2(m1 + b - W), K.ihx);
+        out[0] = M::template flux<0>(K, lds2(c0 + a), lds2(c1 + a), lds2(m0 + a - W), lds2(m1 + a - W));
+        out[1] = M::template flux<0>(K, lds2(c0 + b), lds2(c1 + b), lds2(m0 + b - W), lds2(m1 + b - W));
     };
 
     auto compute_r = [&](int i) {
@@ -140,21 +216,15 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
         const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
         const float2 mup = lds2(mm + a - 2 * W), MA = lds2(mm + a - W), MB = lds2(mm + b - W), mdn = lds2(mm + b);
         // z faces (left, mid) and (mid, right) of each row
-        const float2 zlA = flux_x2(make_float2(cc[a - 1], A.x), A, make_float2(mm[a - W - 1], MA.x), MA, K.ihz);
-        const float2 zhA = flux_x2(A, make_float2(A.y, cc[a + 2]), MA, make_float2(MA.y, mm[a - W + 2]), K.ihz);
-        const float2 zlB = flux_x2(make_float2(cc[b - 1], B.x), B, make_float2(mm[b - W - 1], MB.x), MB, K.ihz);
-        const float2 zhB = flux_x2(B, make_float2(B.y, cc[b + 2]), MB, make_float2(MB.y, mm[b - W + 2]), K.ihz);
+        const float2 zlA = M::template flux<2>(K, make_float2(cc[a - 1], A.x), A, make_float2(mm[a - W - 1], MA.x), MA);
+        const float2 zhA = M::template flux<2>(K, A, make_float2(A.y, cc[a + 2]), MA, make_float2(MA.y, mm[a - W + 2]));
+        const float2 zlB = M::template flux<2>(K, make_float2(cc[b - 1], B.x), B, make_float2(mm[b - W - 1], MB.x), MB);
+        const float2 zhB = M::template flux<2>(K, B, make_float2(B.y, cc[b + 2]), MB, make_float2(MB.y, mm[b - W + 2]));
         // y faces above, between and below the two rows
-        const float2 y0 = flux_x2(up, A, mup, MA, K.ihy), y1 = flux_x2(A, B, MA, MB, K.ihy);
-        const float2 y2 = flux_x2(B, dn, MB, mdn, K.ihy);
-        auto divr = [&](float2 fxp_, float2 fxm_, float2 fyp, float2 fym, float2 fzp, float2 fzm) {
-            float2 d = mul2(sub2(fxp_, fxm_), K.ihx);
-            d = add2(d, mul2(sub2(fyp, fym), K.ihy));
-            d = add2(d, mul2(sub2(fzp, fzm), K.ihz));
-            return mul2_nofuse(K.D, d);   // the result is stored
-        };
-        const float2 rA = divr(fxp[0], fxm[0], y1, y0, zhA, zlA);
-        const float2 rB = divr(fxp[1], fxm[1], y2, y1, zhB, zlB);
+        const float2 y0 = M::template flux<1>(K, up, A, mup, MA), y1 = M::template flux<1>(K, A, B, MA, MB);
+        const float2 y2 = M::template flux<1>(K, B, dn, MB, mdn);
+        const float2 rA = M::div(K, fxp[0], fxm[0], y1, y0, zhA, zlA);
+        const float2 rB = M::div(K, fxp[1], fxm[1], y2, y1, zhB, zlB);
         const size_t o = (size_t)i * plane + (size_t)gj * nz + gk;
         if (wj0) *reinterpret_cast<float2*>(r + o) = rA;
         if (wj1) *reinterpret_cast<float2*>(r + o + nz) = rB;
@@ -191,7 +261,7 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
     }
 }
 
-template <class T, bool FUSED>
+template <class T, bool FUSED, class M>
 __global__ void __launch_bounds__(THREADS, 4)
 ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, float* __restrict__ u_new,
                    float* __restrict__ r, Geo G, ChP P, int LX) {
@@ -200,7 +270,7 @@ ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, f
     const int x0 = blockIdx.z * LX;
     const int x1 = min(x0 + LX, G.nx);
     if (x0 >= x1) return;   // uniform across the block
-    rhs_tile<T, FUSED>(u, upd, u_new, r, G, P, blockIdx.x * T::TZ, blockIdx.y * T::TY, x0, x1, cs, ms);
+    rhs_tile<T, FUSED, M, true>(u, upd, u_new, r, G, P, blockIdx.x * T::TZ, blockIdx.y * T::TY, x0, x1, cs, ms);
 }
 
 __device__ __forceinline__ Geo batch_geo(const BatchInst& B) {
@@ -237,11 +307,11 @@ ch_rhs_batch_kernel(const float* __restrict__ u, const float* __restrict__ upd, 
         const Geo G = batch_geo(B);
         const size_t o = (size_t)B.off;
         if (B.tile == 0)
-            rhs_tile<TileWide, FUSED>(u + o, FUSED ? upd + o : nullptr, FUSED ? u_new + o : nullptr, r + o, G, B.P,
-                                      I.k0, I.j0, I.x0, I.x1, cs, ms);
+            rhs_tile<TileWide, FUSED, TolMath, false>(u + o, FUSED ? upd + o : nullptr, FUSED ? u_new + o : nullptr, r + o,
+                                               G, B.P, I.k0, I.j0, I.x0, I.x1, cs, ms);
         else
-            rhs_tile<TileSquare, FUSED>(u + o, FUSED ? upd + o : nullptr, FUSED ? u_new + o : nullptr, r + o, G,
-                                        B.P, I.k0, I.j0, I.x0, I.x1, cs, ms);
+            rhs_tile<TileSquare, FUSED, TolMath, false>(u + o, FUSED ? upd + o : nullptr, FUSED ? u_new + o : nullptr,
+                                                 r + o, G, B.P, I.k0, I.j0, I.x0, I.x1, cs, ms);
         __syncthreads();   // shared memory and s_item are reused by the next item
     }
 }
@@ -254,22 +324,29 @@ void init_rhs_occupancy() {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rhs_bps[0], ch_rhs_fast_kernel<TileWide, true>, THREADS, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rhs_bps[1], ch_rhs_fast_kernel<TileSquare, true>, THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rhs_bps[0], ch_rhs_fast_kernel<TileWide, true, TolMath>,
+                                                  THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_rhs_bps[1], ch_rhs_fast_kernel<TileSquare, true, TolMath>,
+                                                  THREADS, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_batch_bps, ch_rhs_batch_kernel<true>, THREADS, 0);
     for (int* b : {&g_rhs_bps[0], &g_rhs_bps[1], &g_batch_bps})
         if (*b < 1) *b = 1;
 }
 
 template <class T>
-int rhs_fast_launch_t(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
-                      const Geo& G, const ChP& P, cudaStream_t st, int bps) {
+int rhs_fast_launch_t(bool fused, bool exact, const float* u, const float* upd, float* u_new, float* r,
+                      const evx_grid* g, const Geo& G, const ChP& P, cudaStream_t st, int bps) {
     int lx;
     const dim3 grid = fast_grid<T>(g->nx, g->ny, g->nz, bps, g_sms, &lx);
     if (fused)
-        EVX_TIMED("ch_rhs_fused", st, ch_rhs_fast_kernel<T, true><<<grid, THREADS, 0, st>>>(u, upd, u_new, r, G, P, lx));
+        EVX_TIMED("ch_rhs_fused", st,
+                  ch_rhs_fast_kernel<T, true, TolMath><<<grid, THREADS, 0, st>>>(u, upd, u_new, r, G, P, lx));
+    else if (exact)
+        EVX_TIMED("ch_rhs", st,
+                  ch_rhs_fast_kernel<T, false, ExactMath><<<grid, THREADS, 0, st>>>(u, nullptr, nullptr, r, G, P, lx));
     else
-        EVX_TIMED("ch_rhs", st, ch_rhs_fast_kernel<T, false><<<grid, THREADS, 0, st>>>(u, nullptr, nullptr, r, G, P, lx));
+        EVX_TIMED("ch_rhs", st,
+                  ch_rhs_fast_kernel<T, false, TolMath><<<grid, THREADS, 0, st>>>(u, nullptr, nullptr, r, G, P, lx));
     count_launch();
     return check_launch("ch_rhs_fast_kernel");
 }
@@ -282,12 +359,13 @@ int ch_tile_variant(int nz) {
     return default_tile_variant(nz);
 }
 
-int ch_rhs_fast_launch(bool fused, const float* u, const float* upd, float* u_new, float* r, const evx_grid* g,
-                       const Geo& G, const ChP& P, cudaStream_t st) {
+int ch_rhs_fast_launch(bool fused, bool exact, const float* u, const float* upd, float* u_new, float* r,
+                       const evx_grid* g, const Geo& G, const ChP& P, cudaStream_t st) {
     init_rhs_occupancy();
+    if (fused && exact) return fail(EVX_ERR_UNSUPPORTED, "the fused rhs pass has the spectral loops' arithmetic only");
     if (ch_tile_variant(g->nz) == 1)
-        return rhs_fast_launch_t<TileSquare>(fused, u, upd, u_new, r, g, G, P, st, g_rhs_bps[1]);
-    return rhs_fast_launch_t<TileWide>(fused, u, upd, u_new, r, g, G, P, st, g_rhs_bps[0]);
+        return rhs_fast_launch_t<TileSquare>(fused, exact, u, upd, u_new, r, g, G, P, st, g_rhs_bps[1]);
+    return rhs_fast_launch_t<TileWide>(fused, exact, u, upd, u_new, r, g, G, P, st, g_rhs_bps[0]);
 }
 
 int batch_rhs_blocks_per_sm() {

@@ -38,11 +38,13 @@ namespace evx {
 // Kernel-side Cahn-Hilliard parameters.
 struct ChP {
     float D, kappa, w, A, sym_coef, dt;
+    int bulk;   // EVX_BULK_*
 };
 
 inline ChP make_chp(const evx_ch_params* p) {
     ChP o;
     o.D = p->D; o.kappa = p->kappa; o.w = p->w; o.A = p->A; o.sym_coef = p->sym_coef; o.dt = p->dt;
+    o.bulk = p->bulk;
     return o;
 }
 

@@ -93,6 +93,19 @@ __device__ __forceinline__ float mu_hom(float w, float c) {
     return __fmul_rn(t, __fsub_rn(1.f, __fmul_rn(2.f, c)));
 }
 
+// Regular-solution chemical potential log(c) - log(1-c) + w*(1-2c), in the
+// reference notebook's operation order (docs/notebooks/01-using-solvers.ipynb:
+// lib.log(c) - lib.log(1-c) + 3.0*(1-2*c)); CUDA's logf for the logarithms.
+__device__ __forceinline__ float mu_regular(float w, float c) {
+    const float t = __fsub_rn(logf(c), logf(__fsub_rn(1.f, c)));
+    return __fadd_rn(t, __fmul_rn(w, __fsub_rn(1.f, __fmul_rn(2.f, c))));
+}
+
+// The bulk term selected by evx_ch_params.bulk.
+__device__ __forceinline__ float mu_bulk(int bulk, float w, float c) {
+    return bulk == EVX_BULK_REGULAR_SOLUTION ? mu_regular(w, c) : mu_hom(w, c);
+}
+
 // Face flux m(cf)*grad: (cf*(1-cf)) * ((mu_hi - mu_lo)*ih), cf = 0.5*(c_hi + c_lo)
 // (evoxels/problem_definition.py:356-369, evoxels/fd_stencils.py:20-42).
 __device__ __forceinline__ float face_flux(float c_lo, float c_hi, float mu_lo, float mu_hi, float ih) {

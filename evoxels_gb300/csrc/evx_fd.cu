@@ -543,21 +543,31 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 float* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 
 // Device address of the scratch array on the current device.  The host-side
-// symbol is only a stand-in, so the address is looked up once per device,
-// with that device current, and cached.
-int noalloc_scratch(float** out) {
+// symbol is only a stand-in, so the address is looked up with that device
+// current.  It is looked up again on every call made outside a stream capture
+// (cheap), so a device reset or a new primary context never leaves a stale
+// address behind; a call on a capturing stream uses the address of the last
+// call outside a capture and fails if there was none on this device.
+int noalloc_scratch(float** out, cudaStream_t st) {
     int dev = 0;
     int rc = evx::check_cuda(cudaGetDevice(&dev), "evx_fd_forward_noalloc: cudaGetDevice");
     if (rc) return rc;
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
         return evx::fail(EVX_ERR_UNSUPPORTED, "evx_fd_forward_noalloc: device ordinal %d not supported", dev);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    rc = evx::check_cuda(cudaStreamIsCapturing(st, &cap), "evx_fd_forward_noalloc: cudaStreamIsCapturing");
+    if (rc) return rc;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         rc = evx::check_cuda(cudaGetSymbolAddress(&p, g_fd_noalloc_scratch),
                              "evx_fd_forward_noalloc: cudaGetSymbolAddress");
         if (rc) return rc;
         g_noalloc_ptr[dev] = static_cast<float*>(p);
+    } else if (!g_noalloc_ptr[dev]) {
+        return evx::fail(EVX_ERR_BAD_ARG,
+                         "evx_fd_forward_noalloc: the first call on device %d must come before any stream capture",
+                         dev);
     }
     *out = g_noalloc_ptr[dev];
     return EVX_OK;
@@ -576,7 +586,7 @@ extern "C" int evx_fd_forward_noalloc(const float* u_in, float* u_out, const evx
                     "use evx_fd_forward with a caller-provided scratch field",
                     n, (unsigned)EVX_FD_NOALLOC_MAX_VOXELS);
     float* scratch = nullptr;
-    if ((rc = noalloc_scratch(&scratch))) return rc;
+    if ((rc = noalloc_scratch(&scratch, as_stream(stream)))) return rc;
     Geo G = make_geo(g, bc);
     return fd_run(u_in, u_out, scratch, g, G, D, dt, nsteps, steps_per_pass, as_stream(stream));
 }

@@ -40,6 +40,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <mutex>
@@ -54,6 +55,8 @@ namespace {
 using namespace fft;
 
 __device__ int g_dev_status;       // bit 0: an x-pass barrier wait gave up
+constexpr int WAIT_POLLS = 1 << 22;
+__device__ int g_wait_polls = WAIT_POLLS;   // poll limit of the x-pass's tile-load waits
 
 #ifndef EVX_XPASS_MIN_BLOCKS
 #define EVX_XPASS_MIN_BLOCKS 2   // resident blocks per SM the register budget is sized for
@@ -251,10 +254,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-// Bounded wait on a phase; false if it did not complete within 2^22 polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait on a phase; false if it did not complete within `polls` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int polls) {
     const uint32_t a = smem_u32(bar);
-    for (int i = 0; i < (1 << 22); ++i) {
+    for (int i = 0; i < polls; ++i) {
         uint32_t ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -316,6 +319,7 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         if ((int)blockIdx.x < ntiles) issue_load(0, blockIdx.x);
     }
     __syncthreads();
+    const int polls = g_wait_polls;
     float t1 = 0.f, t2 = 0.f;
     int it = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
@@ -342,7 +346,7 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
 #pragma unroll
             for (int e = 0; e < N1; ++e) asm volatile("prefetch.global.L1 [%0];" ::"l"(dp + e * 256));
         }
-        if (!mbar_wait(&bar[slot], (uint32_t)(it / XSTAGES) & 1u)) atomicOr(&g_dev_status, 1);
+        const bool landed = mbar_wait(&bar[slot], (uint32_t)(it / XSTAGES) & 1u, polls);
         float2* xs = ring + (size_t)slot * TILE;
         const int m = tile * P + c.p;
         const int mc = m < M ? m : 0;
@@ -361,7 +365,17 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) xs[(N2 * n1 + c.n2) * P + c.p] = v[n1];
         fence_async_smem();
-        __syncthreads();
+        if (__syncthreads_or(!landed)) {
+            // a wait gave up: flag it, store nothing more, and leave once this tile's and the
+            // next tile's loads (the only ones in flight) have landed - again a bounded wait
+            if (tid == 0) {
+                atomicOr(&g_dev_status, 1);
+                mbar_wait(&bar[slot], (uint32_t)(it / XSTAGES) & 1u, WAIT_POLLS);
+                if (next < ntiles)
+                    mbar_wait(&bar[(it + 1) % XSTAGES], (uint32_t)((it + 1) / XSTAGES) & 1u, WAIT_POLLS);
+            }
+            break;
+        }
         if (tid == 0) {
 #pragma unroll
             for (int b = 0; b < BOXES; ++b) tma_store_2d(&tm, tile * P, b * ROWS, xs + b * ROWS * P);
@@ -406,14 +420,11 @@ template <int N1, int N2, int MODE, int EXT = 0>
 int xpass_launch_tile(const XpassArgs& A, cudaStream_t st, const char* slot) {
     constexpr int P = 256 / N2;
     const size_t smem = (size_t)N1 * N2 * P * sizeof(float2);
-    static bool attr = false;   // one flag per instantiation
-    if (!attr) {
-        const int rc = check_cuda(cudaFuncSetAttribute(xpass_kernel<N1, N2, MODE, EXT>,
-                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                                  "x-pass shared memory attribute");
-        if (rc) return rc;
-        attr = true;
-    }
+    // the attribute belongs to the current device's context: set it for every launch (cheap)
+    const int rc = check_cuda(cudaFuncSetAttribute(xpass_kernel<N1, N2, MODE, EXT>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                              "x-pass shared memory attribute");
+    if (rc) return rc;
     const int blocks = (A.M + P - 1) / P;
     if (A.n_xpart_out) *A.n_xpart_out = blocks;
     EVX_TIMED(slot, st,
@@ -429,20 +440,18 @@ int xpass_launch_tma(const XpassArgs& A, cudaStream_t st, const char* slot) {
     constexpr int P = 256 / N2, N = N1 * N2;
     constexpr int BOXES = (N + 255) / 256, ROWS = N / BOXES;
     const size_t smem = (size_t)XSTAGES * N * P * sizeof(float2);
-    static int grid_cap = 0;    // resident blocks on the device, per instantiation
-    if (!grid_cap) {
-        int rc = check_cuda(cudaFuncSetAttribute(xpass_tma_kernel<N1, N2, MODE>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                            "x-pass shared memory attribute");
-        if (rc) return rc;
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, xpass_tma_kernel<N1, N2, MODE>, 256, smem),
-                        "x-pass occupancy");
-        if (rc) return rc;
-        grid_cap = sms * (per > 0 ? per : 1);
-    }
+    // attribute and residency belong to the current device: queried for every launch (cheap)
+    int rc = check_cuda(cudaFuncSetAttribute(xpass_tma_kernel<N1, N2, MODE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "x-pass shared memory attribute");
+    if (rc) return rc;
+    int dev = 0, sms = 0, per = 0;
+    if ((rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, xpass_tma_kernel<N1, N2, MODE>, 256, smem),
+                    "x-pass occupancy");
+    if (rc) return rc;
+    const int grid_cap = std::max(1, sms) * (per > 0 ? per : 1);
     CUtensorMap tm;
     const cuuint64_t dims[2] = {(cuuint64_t)A.M, (cuuint64_t)N};
     const cuuint64_t strides[1] = {(cuuint64_t)A.M * sizeof(float2)};
@@ -535,14 +544,10 @@ int xpass_batch_t(int mode, float2* spec, float2* spec_h, const XBatchInst* xb, 
     constexpr int P = 256 / N2;
     const size_t smem = (size_t)N1 * N2 * P * sizeof(float2);
     const dim3 grid((M + P - 1) / P, count);
-    static bool attr[4] = {false, false, false, false};   // per mode of this (N1, N2)
     auto go = [&](auto kern, const char* slot) {
-        if (!attr[mode]) {
-            const int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                                      "x-pass shared memory attribute");
-            if (rc) return rc;
-            attr[mode] = true;
-        }
+        const int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                                  "x-pass shared memory attribute");
+        if (rc) return rc;
         EVX_TIMED(slot, st, (kern<<<grid, 256, smem, st>>>(spec, spec_h, dspec, xpart, M, nzh, nz, kx2, ky2, kz2,
                                                            0.f, 0.f, 0.f, xb, nullptr, nyk)));
         count_launch();
@@ -598,6 +603,18 @@ int xpass_launch(const XpassArgs& A, cudaStream_t st) {
 }
 
 }  // namespace evx
+
+extern "C" int evx_device_status_async(int* dst, void* stream) {
+    if (!dst) return evx::fail(EVX_ERR_BAD_ARG, "evx_device_status_async: null destination");
+    return evx::check_cuda(cudaMemcpyFromSymbolAsync(dst, evx::g_dev_status, sizeof(int), 0, cudaMemcpyDefault,
+                                                     evx::as_stream(stream)),
+                           "queue device status read");
+}
+
+extern "C" int evx_set_wait_polls(int polls) {
+    const int v = polls < 0 ? evx::WAIT_POLLS : polls;
+    return evx::check_cuda(cudaMemcpyToSymbol(evx::g_wait_polls, &v, sizeof(int)), "set wait poll limit");
+}
 
 extern "C" int evx_device_status(int reset) {
     int v = 0;

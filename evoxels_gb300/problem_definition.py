@@ -6,11 +6,19 @@ Same constructor signatures, attributes and error behaviour as the reference's
 calls ``evx_ch_rhs`` / ``evx_rd_rhs`` on the grid's CUDA device.
 
 Scope of the CUDA kernels:
-* ``CahnHilliard.mu_hom`` must be ``None`` (the default ``18/eps*c(1-c)(1-2c)``)
-  or a callable equal to ``w*c*(1-c)*(1-2c)`` for some constant ``w`` - the
-  form the reference uses when the bulk energy is pinned independently of
-  ``eps``.  The callable is probed once on CPU to find ``w``.
-* ``ReactionDiffusion.f`` must be ``None`` or a callable returning ``0``.
+* ``CahnHilliard.mu_hom`` must be ``None`` (the default ``18/eps*c(1-c)(1-2c)``),
+  a callable equal to ``w*c*(1-c)*(1-2c)`` for some constant ``w`` (the form
+  the reference uses when the bulk energy is pinned independently of ``eps``),
+  or a callable equal to the regular-solution potential
+  ``log(c) - log(1-c) + w*(1-2c)`` (the logarithmic free energy of the
+  reference's solver notebook; forward steps only, the adjoint and the batched
+  path take the double well).  The callable is probed once on CPU to find the
+  form and ``w``; any other form raises ``NotImplementedError``.
+* ``ReactionDiffusion.f`` may be any callable ``f(t, u[, lib])``: like the
+  reference it is user code, evaluated with ``lib = torch`` on the grid's
+  device and added to the stencil kernel's ``D*laplace(u)``; ``None`` (the
+  reference's zero source) lets the forward-Euler steps run fused in one
+  library call.
 """
 
 from __future__ import annotations
@@ -55,12 +63,37 @@ def double_well_coefficient(mu_hom, eps):
     return w
 
 
-def ch_params(eps, D, A, dt, w=None):
+def bulk_potential(mu_hom, eps):
+    """``(form, w)`` of a Cahn-Hilliard bulk term: ``(EVX_BULK_DOUBLE_WELL, w)`` for
+    ``w*c*(1-c)*(1-2c)`` (``None``: the reference default ``w = 18/eps``) or
+    ``(EVX_BULK_REGULAR_SOLUTION, w)`` for ``log(c) - log(1-c) + w*(1-2c)``; raises
+    ``NotImplementedError`` for any other callable."""
+    try:
+        return _lib.EVX_BULK_DOUBLE_WELL, double_well_coefficient(mu_hom, eps)
+    except NotImplementedError as e:
+        first = e
+    c = torch.tensor([0.05, 0.1, 0.25, 0.3, 0.45, 0.6, 0.8, 0.9], dtype=torch.float64)
+    logs = torch.log(c) - torch.log(1 - c)
+    try:
+        vals = torch.as_tensor(_eval_callable(mu_hom, c), dtype=torch.float64).expand_as(c)
+    except Exception:  # noqa: BLE001 - not a supported form
+        raise first from None
+    w = float((vals[2] - logs[2]) / (1 - 2 * c[2]))
+    if not torch.allclose(vals, logs + w * (1 - 2 * c), rtol=1e-12, atol=1e-12 * max(1.0, abs(w))):
+        raise NotImplementedError(
+            "evoxels_gb300 supports mu_hom of the forms w*c*(1-c)*(1-2c) (the reference default "
+            "18/eps*c*(1-c)*(1-2c) or a pinned coefficient) and log(c) - log(1-c) + w*(1-2c)") from None
+    return _lib.EVX_BULK_REGULAR_SOLUTION, w
+
+
+def ch_params(eps, D, A, dt, w=None, bulk=0):
     """``EvxChParams``: float32 roundings of the python-double constants the
     reference evaluates (evoxels/problem_definition.py:303-305,
-    evoxels/timesteppers.py:77); ``w`` defaults to ``18/eps``."""
+    evoxels/timesteppers.py:77); ``w`` defaults to ``18/eps``; ``bulk`` the
+    form of the bulk term (``EVX_BULK_*``)."""
     f = lambda x: float(np.float32(x))  # noqa: E731
     p = _lib.EvxChParams()
+    p.bulk = int(bulk)
     p.D = f(D)
     p.kappa = f(2 * eps)
     p.w = f(18 / eps if w is None else w)
@@ -127,7 +160,7 @@ class CahnHilliard(_BCMixin):
 
     def __post_init__(self):
         self.initialize_boundary_conditions()
-        self._w = double_well_coefficient(self.mu_hom, self.eps)
+        self._bulk, self._w = bulk_potential(self.mu_hom, self.eps)
         if self.mu_hom is None:
             eps = self.eps
             self.mu_hom = lambda c, lib=None: 18 / eps * c * (1 - c) * (1 - 2 * c)
@@ -145,7 +178,7 @@ class CahnHilliard(_BCMixin):
 
     def evx_params(self, dt=0.0):
         """float32 roundings of the python-double constants the reference evaluates."""
-        return ch_params(self.eps, self.D, self.A, dt, self._w)
+        return ch_params(self.eps, self.D, self.A, dt, self._w, self._bulk)
 
     def rhs(self, t, u):
         """``CahnHilliard.rhs`` on the GPU (evoxels/problem_definition.py:328-371)."""
@@ -170,11 +203,11 @@ class ReactionDiffusion(_BCMixin):
     _fourier_symbol: Any = field(init=False, repr=False, default=None)
 
     def __post_init__(self):
-        if self.f is not None:
-            probe = _eval_callable(self.f, 0.0, torch.zeros(2, dtype=torch.float64))
-            if not (isinstance(probe, (int, float)) and probe == 0):
-                raise NotImplementedError("evoxels_gb300 implements ReactionDiffusion with f = 0 only")
-        else:
+        # None is the reference's zero source (evoxels/problem_definition.py:201-203); any other
+        # callable is evaluated every step, as the reference does, so that a source vanishing at
+        # some (t, u) is never mistaken for zero
+        self.source_free = self.f is None
+        if self.f is None:
             self.f = lambda c=None, t=None, lib=None: 0
         self.initialize_boundary_conditions()
 
@@ -188,8 +221,13 @@ class ReactionDiffusion(_BCMixin):
             self._fourier_symbol = -self.D * self.A * self.k_squared()
         return self._fourier_symbol
 
+    def _eval_f(self, t, c):
+        """The source term ``f(t, c, lib)`` with ``lib = torch`` (evoxels/problem_definition.py:215-220)."""
+        return _eval_callable(self.f, t, c)
+
     def rhs(self, t, u):
-        """``D*laplace(pad_bc(u)) + 0`` on the GPU (evoxels/problem_definition.py:226-229)."""
+        """``D*laplace(pad_bc(u)) + f(t, u)`` (evoxels/problem_definition.py:226-229): the stencil term
+        by ``evx_rd_rhs``, then the user's source added (skipped for the zero source)."""
         u = self.vg.check_field(u)
         out = torch.empty_like(u)
         g = self.vg.evx_grid()
@@ -197,7 +235,9 @@ class ReactionDiffusion(_BCMixin):
         for ch in range(u.shape[0]):
             _lib.check(L.evx_rd_rhs(u[ch].data_ptr(), out[ch].data_ptr(), g, self._evx_bc,
                                     float(np.float32(self.D)), cuda_stream()), "evx_rd_rhs")
-        return out
+        if self.source_free:
+            return out
+        return out + self._eval_f(t, u)
 
 
 def ac_params(eps, gab, M, force, curvature, w=None):

@@ -106,8 +106,10 @@ class BaseSolver:
 
     def _handle_outputs(self, u, frame, time, vtk_out, verbose, plot_bounds, colormap):
         """Export, NaN abort, optional VTK (evoxels/solvers.py:152-187; no plotting)."""
+        from . import _lib
         u_out = u  # trim_ghost_nodes(pad_bc(u)) == u for cell-centred grids
         self._export_fields(u_out)
+        _lib.check_device_status(f"frame {frame}")
         has_nan = any(np.isnan(self.vf.fields[name]).any() for name in self.fieldnames)
         self._frame_tail(has_nan, frame, time, vtk_out)
 
@@ -130,7 +132,8 @@ class BaseSolver:
             pipe = {"stream": torch.cuda.Stream(dev),
                     "host": torch.empty(u.shape, dtype=u.dtype).pin_memory(),
                     "flag_dev": torch.zeros(1, dtype=torch.int32, device=dev),
-                    "flag_host": torch.zeros(1, dtype=torch.int32).pin_memory()}
+                    "flag_host": torch.zeros(1, dtype=torch.int32).pin_memory(),
+                    "status_host": torch.zeros(1, dtype=torch.int32).pin_memory()}
             self._pipe = pipe
         st = pipe["stream"]
         st.wait_stream(torch.cuda.current_stream(dev))
@@ -139,6 +142,9 @@ class BaseSolver:
                        "evx_nan_flag")
             pipe["host"].copy_(u, non_blocking=True)
             pipe["flag_host"].copy_(pipe["flag_dev"], non_blocking=True)
+            # the kernels' status word (a bounded wait that gave up) travels with the frame
+            _lib.check(_lib.lib().evx_device_status_async(pipe["status_host"].data_ptr(), st.cuda_stream),
+                       "evx_device_status_async")
             done = torch.cuda.Event()
             done.record(st)
         u.record_stream(st)   # the caching allocator keeps u until the copy has read it
@@ -147,6 +153,8 @@ class BaseSolver:
     def _finish_output(self, pending, vtk_out):
         done, frame, time = pending
         done.synchronize()
+        from . import _lib
+        _lib.raise_device_status(int(self._pipe["status_host"][0]), f"frame {frame}")
         host = self._pipe["host"]
         for i, name in enumerate(self.fieldnames):
             self.vf.set_field(name, host[i].numpy().copy())
@@ -173,7 +181,7 @@ class TimeDependentSolver(BaseSolver):
                 frame += 1
             if advance is not None:
                 n = min(n_out - i % n_out, max_iters - i)
-                u = advance(u, n)
+                u = advance(u, n, t0=time)
                 i += n
             else:
                 u = step(time, u)
@@ -233,7 +241,7 @@ class SteadyStatePseudoTimeSolver(BaseSolver):
                 continue
             n = min(cf - self.iter % cf, max_iters - self.iter)
             if advance is not None:
-                u = advance(u, n)
+                u = advance(u, n, t0=self.iter * time_increment)
             else:
                 for s in range(n):
                     u = step((self.iter + s) * time_increment, u)

@@ -149,8 +149,9 @@ class PseudoSpectralIMEX(TimeStepper):
                                           p.workspace.data_ptr(), cuda_stream()), "evx_ch_step")
         return out
 
-    def advance(self, u, nsteps, traj=None, nonfinite=None):
-        """``nsteps`` steps from ``u`` in one library call; ``traj`` receives u_1..u_n."""
+    def advance(self, u, nsteps, traj=None, nonfinite=None, t0=0.0):
+        """``nsteps`` steps from ``u`` in one library call; ``traj`` receives u_1..u_n.
+        (``t0``: the time of ``u``; the Cahn-Hilliard rhs does not depend on it.)"""
         u = self._check(u)
         out = torch.empty_like(u)
         p = self._plan
@@ -177,9 +178,13 @@ class ForwardEuler(TimeStepper):
     def order(self) -> int:
         return 1
 
+    def _fused(self):
+        """Forward Euler of a source-free reaction-diffusion problem runs in ``evx_fd_forward``."""
+        return isinstance(self.problem, ReactionDiffusion) and self.problem.source_free
+
     def step(self, t, u):
-        if isinstance(self.problem, ReactionDiffusion):
-            return self.advance(u, 1)
+        if self._fused():
+            return self.advance(u, 1, t0=t)
         u = self.problem.vg.check_field(u)
         r = self.problem.rhs(t, u)
         out = torch.empty_like(u)
@@ -187,10 +192,11 @@ class ForwardEuler(TimeStepper):
                                             out.data_ptr(), u.numel(), cuda_stream()), "evx_fe_update")
         return out
 
-    def advance(self, u, nsteps):
-        if not isinstance(self.problem, ReactionDiffusion):
-            for _ in range(nsteps):
-                u = self.step(0.0, u)
+    def advance(self, u, nsteps, t0=0.0):
+        """``nsteps`` steps from ``u`` at time ``t0``; step k sees the time ``t0 + k*dt``."""
+        if not self._fused():
+            for k in range(nsteps):
+                u = self.step(t0 + k * self.dt, u)
             return u
         pr = self.problem
         u = pr.vg.check_field(u)
@@ -294,6 +300,9 @@ class ExponentialEuler(TimeStepper):
             # the reference transforms over (C, Nx, Ny, Nz) and so couples channels;
             # evoxels_gb300 builds the single-field step only
             raise NotImplementedError("ExponentialEuler in evoxels_gb300 steps one field (C == 1)")
+        if isinstance(self.problem, CahnHilliard):
+            # the spectral loop's own rhs pass, so that n steps equal advance(u, n) bit for bit
+            return self.advance(u, 1, t0=t)
         r = self.problem.rhs(t, u)
         out = torch.empty_like(u)
         p = self._plan
@@ -302,14 +311,14 @@ class ExponentialEuler(TimeStepper):
                    "evx_spectral_update")
         return out
 
-    def advance(self, u, nsteps, nonfinite=None):
-        """``nsteps`` steps from ``u``.  For CahnHilliard one library call
+    def advance(self, u, nsteps, nonfinite=None, t0=0.0):
+        """``nsteps`` steps from ``u`` at time ``t0``.  For CahnHilliard one library call
         (``evx_ch_forward_mult``: each step's update is fused into the next
         step's rhs pass), bit-identical to ``nsteps`` calls of ``step``; other
-        problems step one at a time."""
+        problems step one at a time, step k at the time ``t0 + k*dt``."""
         if not isinstance(self.problem, CahnHilliard):
-            for _ in range(nsteps):
-                u = self.step(0.0, u)
+            for k in range(nsteps):
+                u = self.step(t0 + k * self.dt, u)
             return u
         u = self.problem.vg.check_field(u)
         if u.shape[0] != 1:

@@ -62,12 +62,20 @@ typedef struct evx_grid {
  * float32 rounding of the python-double expression the reference evaluates:
  *   D        = D
  *   kappa    = 2*eps                      (gradient coefficient, mu = mu_hom - kappa*lap)
- *   w        = 18/eps by default          (mu_hom = w*c*(1-c)*(1-2c))
+ *   w        = 18/eps by default          (bulk coefficient, below)
  *   A        = A (0.25)
  *   sym_coef = -2*eps*D*A                 (fourier_symbol = sym_coef*(k^2)^2)
- *   dt       = dt                         (prefac = dt/(1 - dt*symbol), evoxels/timesteppers.py:77) */
+ *   dt       = dt                         (prefac = dt/(1 - dt*symbol), evoxels/timesteppers.py:77)
+ *   bulk     = form of the homogeneous chemical potential mu_hom(c):
+ *              EVX_BULK_DOUBLE_WELL  w*c*(1-c)*(1-2c)   (the default, evoxels/problem_definition.py:305)
+ *              EVX_BULK_REGULAR_SOLUTION  log(c) - log(1-c) + w*(1-2c)   (the logarithmic free
+ *              energy the reference passes as a callable, docs/notebooks/01-using-solvers.ipynb;
+ *              forward steps only) */
+#define EVX_BULK_DOUBLE_WELL       0
+#define EVX_BULK_REGULAR_SOLUTION  1
 typedef struct evx_ch_params {
     float D, kappa, w, A, sym_coef, dt;
+    int32_t bulk;
 } evx_ch_params;
 
 /* Two-phase Allen-Cahn parameters (evoxels/problem_definition.py:374-447), the
@@ -298,6 +306,19 @@ int evx_fft_z_c2r(const float* spec, float* out, int nx, int ny, int nz, void* s
  * a bounded wait of the pipelined x-pass on its tile loads gave up (the
  * results of that call are invalid).  Returns -1 if the read itself failed. */
 int evx_device_status(int reset);
+
+/* Queue a copy of the device status word into dst (host-pinned or device
+ * memory) on the given stream, ordered after the work queued there before it; the
+ * asynchronous form of evx_device_status for loops that must not stall the
+ * device (a frame pipeline reads it with the frame's data). */
+int evx_device_status_async(int* dst, void* stream);
+
+/* Poll limit of the x-pass's bounded waits on its tile loads on the current
+ * device (default 2^22 when polls < 0).  A call whose wait runs out sets bit
+ * 0 of the device status, stops storing results and returns once its loads in
+ * flight have landed.  A limit of 0 makes every such wait give up at once,
+ * which exercises that path without any fault. */
+int evx_set_wait_polls(int polls);
 
 /* Tile shape of the periodic fast-path stencil kernels (single grids):
  * -1 automatic (32x32 when nz is a multiple of 32 but not of 64, else 16x64),

@@ -1,9 +1,12 @@
 """Generate the golden fixtures in this folder by running the evoxels reference.
 
-Run in a container that has the reference checked out (path in ``EVOXELS_REF``,
-default ``/root/reference``) and torch on CPU::
+Run where the reference is checked out, with its path in ``EVOXELS_REF`` (the
+folder that holds the ``evoxels`` package; there is no default), and torch on
+CPU::
 
-    python tests/golden/make_golden.py
+    EVOXELS_REF=<path of the evoxels checkout> python tests/golden/make_golden.py [--only=name,name]
+
+(``--only`` writes just the named fixtures.)
 
 The reference package is imported with a small shim: ``matplotlib`` is absent
 here, so stub modules stand in for it (only plotting uses it), and the package
@@ -27,12 +30,14 @@ import warnings
 import numpy as np
 import torch
 
-REF = os.environ.get("EVOXELS_REF", "/root/reference")
+REF = os.environ.get("EVOXELS_REF", "")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
 def import_reference():
     """Import the reference's torch-path modules without matplotlib/JAX."""
+    if not REF or not os.path.isdir(os.path.join(REF, "evoxels")):
+        raise SystemExit("set EVOXELS_REF to the folder holding the reference's evoxels package")
     for name in ("matplotlib", "matplotlib.pyplot", "matplotlib.widgets", "matplotlib.patches"):
         if name not in sys.modules:
             mod = types.ModuleType(name)
@@ -268,9 +273,34 @@ def main():
         verbose=False)
     out["driver_ch"] = dict(u0=u0, c=vf.fields["c"], n=20)
 
+    # 8) the regular-solution (logarithmic) bulk term of the reference's solver notebook
+    #    (docs/notebooks/01-using-solvers.ipynb): CahnHilliard.rhs and the drop-in driver
+    def regular_solution_mu(c, lib):
+        return lib.log(c) - lib.log(1 - c) + 3.0 * (1 - 2 * c)
+    for i, (shape, seed, bc) in enumerate([((12, 10, 16), 61, None),
+                                           ((9, 8, 12), 62, ("neumann", "periodic", "periodic"))]):
+        _, vg = make_vg(R, shape)
+        kw = dict(eps=3.0, D=1.0, mu_hom=regular_solution_mu)
+        if bc is not None:
+            kw["bc"] = bc
+        prob = PD.CahnHilliard(vg, **kw)
+        u0 = ch_field(shape, seed)
+        r = prob.rhs(0.0, vg.init_scalar_field(u0))
+        out[f"ch_log_rhs_{i}"] = dict(u0=u0, rhs=r.numpy(), shape=np.array(shape), bc=np.array(repr(bc)))
+    vf = R["voxelfields"].VoxelFields((16, 16, 16), domain_size=(16, 16, 16))
+    u0 = ch_field((16, 16, 16), 63)
+    vf.add_field("c", u0.copy())
+    R["precompiled_solvers.cahn_hilliard"].run_cahn_hilliard_solver(
+        vf, "c", "torch", jit=False, device="cpu", time_increment=0.1, frames=2, max_iters=20,
+        eps=3.0, diffusivity=1.0, mu_hom=regular_solution_mu, verbose=False)
+    out["driver_ch_log"] = dict(u0=u0, c=vf.fields["c"], n=20)
+
+    only = [a.split("=", 1)[1].split(",") for a in sys.argv[1:] if a.startswith("--only=")]
     for name, arrays in out.items():
+        if only and name not in only[0]:
+            continue
         np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrays)
-    print("wrote", len(out), "fixtures to", OUT)
+    print("wrote", len(only[0]) if only else len(out), "fixtures to", OUT)
 
 
 if __name__ == "__main__":

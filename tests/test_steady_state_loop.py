@@ -24,7 +24,7 @@ def _solver(check_freq, use_advance, calls, outputs):
     s.conv_crit, s.check_freq, s.fieldnames = 1e-4, check_freq, ["c"]
 
     class Stepper:
-        def advance(self, u, n):
+        def advance(self, u, n, t0=0.0):
             calls.append(("advance", n))
             for _ in range(n):
                 u = _step(u)

@@ -35,8 +35,8 @@ def _solver(use_advance, calls, outputs):
     s.async_output = False
 
     class Stepper:
-        def advance(self, u, n):
-            calls.append(("advance", n))
+        def advance(self, u, n, t0=0.0):
+            calls.append(("advance", n, t0))
             for _ in range(n):
                 u = _step(u)
             return u
@@ -62,7 +62,8 @@ def test_frames_match_reference_loop(max_iters, frames, use_advance):
     assert all(torch.equal(a, b) for (_, _, a), (_, _, b) in zip(outputs, ref_out))
     n_out = max_iters // frames
     if use_advance:   # one library call per frame interval, the last one cut at max_iters
-        assert [n for _, n in calls] == [min(n_out, max_iters - i) for i in range(0, max_iters, n_out)]
+        assert [n for _, n, _ in calls] == [min(n_out, max_iters - i) for i in range(0, max_iters, n_out)]
+        assert [t0 for _, _, t0 in calls] == [i * DT for i in range(0, max_iters, n_out)]
     else:
         assert [t for _, t in calls] == [i * DT for i in range(max_iters)]
 
