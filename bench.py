@@ -16,7 +16,9 @@ Python/torch) on the host cores with all threads, on the same workload; each
 step is a bounded sample (one forward + one adjoint step at the same size).
 
 Multi-GPU (torchrun): single-grid workloads run as independent replicas, one
-per rank (weak scaling, no collective on the data path).
+per rank (weak scaling, no collective on the data path); the batched workloads
+shard the 64 instances over the ranks (balanced by voxel count, strong scaling,
+no collective on the data path).
 """
 
 from __future__ import annotations
@@ -513,14 +515,22 @@ class Batched:
     dt = 0.1; forward, or forward (trajectory and increment spectra kept) + adjoint with
     parameter gradients."""
 
-    def __init__(self, torch, device, steps_per=50, adjoint=False, n_inst=64, autotune=True):
+    def __init__(self, torch, device, steps_per=50, adjoint=False, n_inst=64, autotune=True, rank=0, world=1):
         from evoxels_gb300.batched import BatchedCahnHilliard, BatchTuning
         self.torch = torch
+        self.sharded = world > 1   # under torchrun each rank advances its share of the 64 instances
         rng = np.random.default_rng(4)
         sides = rng.choice([32, 48, 64, 96, 128], n_inst)
         M = rng.uniform(0.5, 2.0, n_inst)
         kappa = rng.uniform(0.5, 3.0, n_inst)
-        self.shapes = [(int(a),) * 3 for a in sides]
+        all_shapes = [(int(a),) * 3 for a in sides]
+        all_fields = [0.5 + 0.1 * np.random.default_rng([4, i]).random(s) for i, s in enumerate(all_shapes)]
+        if self.sharded:
+            from evoxels_gb300.partition import shard
+            idx, self.shapes, M, kappa, self.fields = shard(all_shapes, rank, world, M, kappa, all_fields)
+            M, kappa = np.array(M), np.array(kappa)
+        else:
+            idx, self.shapes, self.fields = list(range(n_inst)), all_shapes, all_fields
         self.M, self.eps = M, kappa / 2
         self.pin = lambda c, lib=None: 18 / 3.0 * c * (1 - c) * (1 - 2 * c)
         tuning = BatchTuning()
@@ -530,7 +540,6 @@ class Batched:
             tuning = at.tune_batched(self.shapes, M, self.eps, 0.1, mu_hom=self.pin, steps=10)
             tuned = dict(tuning.__dict__)
         self.b = BatchedCahnHilliard(self.shapes, M, self.eps, 0.1, mu_hom=self.pin, tuning=tuning)
-        self.fields = [0.5 + 0.1 * np.random.default_rng([4, i]).random(s) for i, s in enumerate(self.shapes)]
         self.T = steps_per
         self.adj = adjoint
         self.n = self.b.voxels
@@ -546,6 +555,8 @@ class Batched:
             self.grads = torch.zeros((self.b.n, 3), dtype=torch.float64, device=device)
         self.units_per_step = self.n * self.T
         self.config = {"workload": "batched64_fwd_adj" if adjoint else "batched64_fwd", "instances": n_inst,
+                       "shard": ("rank %d of %d: %d instances (balanced by voxel count, no collective)"
+                                 % (rank, world, len(idx))) if self.sharded else "all instances on one GPU",
                        "sides": sorted(set(int(a) for a in sides)), "total_voxels": self.n,
                        "steps_per_bench_step": self.T, "dt": 0.1, "M_range": [0.5, 2.0], "kappa_range": [0.5, 3.0],
                        "bulk": "pinned 18/3", "seed": 4, "tuning": tuned or "defaults",
@@ -669,11 +680,11 @@ def batched_summary(torch, device, steps, warmup):
             "err_vs_fp64_forward_1_step": errs}
 
 
-def make_workload(name, torch, device, inner=None, spp=0, shape=None):
+def make_workload(name, torch, device, inner=None, spp=0, shape=None, rank=0, world=1):
     if name == "batched64_fwd":
-        return Batched(torch, device, inner or 50, adjoint=False)
+        return Batched(torch, device, inner or 50, adjoint=False, rank=rank, world=world)
     if name == "batched64_fwd_adj":
-        return Batched(torch, device, inner or 20, adjoint=True)
+        return Batched(torch, device, inner or 20, adjoint=True, rank=rank, world=world)
     if name == "ch256_fwd_adj":
         return ChFwdAdj(torch, device, 256, inner or 10, 6, shape=shape)
     if name == "ch512_fwd_adj":   # large single grid: forward + adjoint with stored trajectory
@@ -850,7 +861,9 @@ def main():
 
     from evoxels_gb300 import _lib
     L = _lib.lib()
-    wl = make_workload(args.workload, torch, device, args.inner_steps, args.fd_steps_per_pass, args.shape)
+    wl = make_workload(args.workload, torch, device, args.inner_steps, args.fd_steps_per_pass, args.shape,
+                       rank=rank, world=world)
+    sharded = getattr(wl, "sharded", False)
 
     for _ in range(warmup):
         wl.step()
@@ -882,7 +895,12 @@ def main():
         t = torch.tensor([ms], device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t)
-    units_total = wl.units_per_step * args.steps * world
+    if sharded:   # each rank advanced its own share: sum the voxel-steps over ranks
+        t = torch.tensor([float(wl.units_per_step)], device=device, dtype=torch.float64)
+        dist.all_reduce(t)
+        units_total = float(t) * args.steps
+    else:         # replicas: every rank advanced the whole workload
+        units_total = wl.units_per_step * args.steps * world
     value = units_total / (ms / 1e3)
 
     # ---- end to end: host buffers through the public API -------------------------
@@ -961,7 +979,7 @@ def main():
                          "bytes_per_voxel_step": step_bytes // wl.units_per_step}
 
     vs_plain = None
-    if isinstance(wl, Batched):
+    if isinstance(wl, Batched) and not sharded:
         plain_ms = wl.plain(max(2, min(args.steps, 5)))
         vs_plain = {"plain_ms_per_step": round(plain_ms, 3), "plain_value": round(wl.units_per_step / (plain_ms / 1e3), 1),
                     "speedup": round(plain_ms / (ms / args.steps), 3),
@@ -983,11 +1001,12 @@ def main():
         "warmup": warmup,
         "ms_per_step": round(ms / args.steps, 4),
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong" if sharded else "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded U[0,1) fields, no dataset)",
-        "config": dict(wl.config, parallelism=("replicas x%d" % world) if world > 1 else "single GPU"),
+        "config": dict(wl.config, parallelism=("instances sharded x%d" % world) if sharded else
+                       ("replicas x%d" % world) if world > 1 else "single GPU"),
         "roofline": roofline,
         "step_roofline": step_roofline,
         "kernel_breakdown": breakdown,

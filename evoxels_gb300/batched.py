@@ -21,6 +21,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from .partition import shard
 from .problem_definition import ch_params, double_well_coefficient
 from .voxelgrid import _require_cuda, cuda_stream, grid_factors
 
@@ -89,6 +90,22 @@ class BatchedCahnHilliard:
         self.offsets = [int(o) for o in offs]
         self.sizes = [int(np.prod(s)) for s in self.shapes]
         self.workspace = torch.empty(int(L.evx_batch_workspace_bytes(h)), dtype=torch.uint8, device=self.device)
+
+    @classmethod
+    def for_rank(cls, shapes, rank, world_size, D=1.0, eps=3.0, **kw):
+        """The instances this rank advances when a batch is sharded over ``world_size`` GPUs, one
+        process per GPU: ``partition_instances(shapes, world_size)[rank]`` (balanced by voxel count,
+        the same split on every rank; independent instances need no collective).  ``D`` and ``eps``
+        are for the whole batch; ``global_index`` maps the shard's instances to positions in
+        ``shapes``, and ``pack_shard(fields)`` packs this rank's fields from the whole list."""
+        idx, sub, d, e = shard(shapes, rank, world_size, D, eps)
+        b = cls(sub, d, e, **kw)
+        b.global_index = idx
+        return b
+
+    def pack_shard(self, fields, out=None):
+        """Pack this shard's instances from the fields of the whole batch (see ``for_rank``)."""
+        return self.pack([fields[i] for i in getattr(self, "global_index", range(len(fields)))], out)
 
     def __del__(self):
         try:

@@ -30,3 +30,24 @@ def partition_instances(shapes, world_size):
 
 def my_instances(shapes, rank, world_size):
     return partition_instances(shapes, world_size)[rank]
+
+
+def shard(shapes, rank, world_size, *per_instance):
+    """This rank's share of a batch: ``(indices, shapes, *per_instance values)`` of the instances
+    ``partition_instances(shapes, world_size)[rank]``.  ``per_instance`` are scalars (broadcast) or
+    sequences with one value per instance (mobility, eps, fields, ...).  Every rank derives the same
+    split from the same list, so no collective is needed to agree on it."""
+    if not 0 <= rank < world_size:
+        raise ValueError(f"rank {rank} outside world of {world_size}")
+    idx = partition_instances(shapes, world_size)[rank]
+    n = len(shapes)
+    out = [idx, [tuple(shapes[i]) for i in idx]]
+    for v in per_instance:
+        if np.isscalar(v) or (isinstance(v, np.ndarray) and v.ndim == 0):
+            out.append([v] * len(idx))
+        else:
+            if len(v) != n:
+                raise ValueError(f"per-instance values: {len(v)} for {n} instances")
+            out.append([v[i] for i in idx])
+    return tuple(out)
+

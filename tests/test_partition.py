@@ -57,3 +57,63 @@ def test_two_ranks_agree_on_a_disjoint_cover():
         assert p.exitcode == 0
     assert sorted(set(owners)) == [1, 2] and all(o in (1, 2) for o in owners)
     assert sum(loads) == sum(int(np.prod(s)) for s in shapes)
+
+
+def _shard_worker(rank, world, port, out):
+    """One rank of a sharded batch: its share of the instances, each advanced by the oracle (the
+    CPU stand-in for the batched GPU step); the results are gathered only to check them."""
+    import oracle
+    from evoxels_gb300.partition import shard
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    shapes, M, eps, fields = _batch()
+    idx, sub, m, e, f = shard(shapes, rank, world, M, eps, fields)
+    mine = {i: oracle.ch_imex_run(torch.tensor(fi).unsqueeze(0), 2, 0.1, float(ei), float(mi)).numpy()
+            for i, fi, mi, ei in zip(idx, f, m, e)}
+    assert [tuple(s) for s in sub] == [tuple(shapes[i]) for i in idx]
+    got = [None] * world
+    dist.all_gather_object(got, mine)
+    if rank == 0:
+        out.put(got)
+    dist.destroy_process_group()
+
+
+def _batch():
+    rng = np.random.default_rng(5)
+    shapes = [(int(a), int(a), 4) for a in rng.choice([4, 6, 8], 7)]
+    M = rng.uniform(0.5, 2.0, 7)
+    eps = rng.uniform(0.5, 3.0, 7) / 2
+    fields = [0.5 + 0.1 * np.random.default_rng([5, i]).random(s) for i, s in enumerate(shapes)]
+    return shapes, M, eps, fields
+
+
+def test_sharded_batch_two_ranks_equals_one_rank():
+    import oracle
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29600 + (os.getpid() % 1000)
+    procs = [ctx.Process(target=_shard_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = q.get(timeout=180)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    shapes, M, eps, fields = _batch()
+    merged = {}
+    for part in got:
+        assert not set(part) & set(merged)          # disjoint shares
+        merged.update(part)
+    assert sorted(merged) == list(range(len(shapes)))
+    for i, f in enumerate(fields):
+        ref = oracle.ch_imex_run(torch.tensor(f).unsqueeze(0), 2, 0.1, float(eps[i]), float(M[i])).numpy()
+        np.testing.assert_array_equal(merged[i], ref)
+
+
+def test_shard_validates_its_arguments():
+    from evoxels_gb300.partition import shard
+    with pytest.raises(ValueError):
+        shard([(4, 4, 4)], 1, 1)
+    with pytest.raises(ValueError):
+        shard([(4, 4, 4), (4, 4, 4)], 0, 2, [1.0])
