@@ -45,7 +45,7 @@ FALLBACK_HBM_GBS = 6800.0
 # captures summarised under profiles/ (rhs and pullback at 256^3, forward Euler
 # at 512^3); traffic grows in proportion to the voxels a launch processes.
 NCU_DRAM_BYTES_PER_VOXEL = {
-    "ch_rhs_fused": (153.137408e6 + 92.517888e6) / 256 ** 3,
+    "ch_rhs_fused": (153.348096e6 + 90.268416e6) / 256 ** 3,
     "ch_pullback_grads": (344.547840e6 + 54.629120e6) / 256 ** 3,
     "fd_step": (561.215488e6 + 497.061376e6) / 512 ** 3,
     "fd_tblock2": (554.379264e6 + 495.615488e6) / 512 ** 3,
@@ -815,7 +815,7 @@ def cpu_sample(workload_name, torch, seconds_cap=30.0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ch256_fwd_adj")

@@ -425,6 +425,64 @@ int capture_chunk(evx_batch* b, void* ws, int steps) {
 
 }  // namespace
 
+namespace evx {
+namespace {
+// Every offset the batched kernels derive from the descriptors, checked against
+// the buffers they index before anything is uploaded: each instance's field
+// slice (16-byte aligned, disjoint, inside the packed field), every work item
+// inside its instance with the tiles of an instance covering it exactly once,
+// the spectrum, stored-spectrum and partial-sum ranges of every instance, and
+// the k^2 table offsets.  A failure is a bug in the layout code.
+int validate_layout(const evx_batch* b, const std::vector<BatchInst>& hinst, const std::vector<BatchItem>& items,
+                    const std::vector<KInst>& hk, const std::vector<RInst>& hr, const std::vector<XBatchInst>& hxb,
+                    size_t k2_len) {
+    auto bad = [](const char* what, int i) {
+        return fail(EVX_ERR_BAD_ARG, "batched layout check failed (internal error): %s, instance %d", what, i);
+    };
+    const int n = b->n;
+    std::vector<std::pair<long long, long long>> spans;
+    std::vector<long long> covered(n, 0);
+    for (int ii = 0; ii < n; ++ii) {
+        const BatchInst& B = hinst[ii];
+        const long long ni = (long long)B.nx * B.ny * B.nz, nsi = (long long)B.nx * B.ny * (B.nz / 2 + 1);
+        if (B.off < 0 || B.off % 4 || B.off + ni > (long long)b->total) return bad("field slice", ii);
+        if (B.tile != 0 && B.tile != 1) return bad("tile variant", ii);
+        spans.emplace_back(B.off, B.off + ni);
+        const KInst& K = hk[ii];
+        if (K.soff < 0 || K.soff + nsi > (long long)b->total_spec) return bad("spectrum slice", ii);
+        if (K.nx != B.nx || K.ny != B.ny || K.nzh != B.nz / 2 + 1) return bad("k-space shape", ii);
+        if (K.kx < 0 || K.ky != K.kx + B.nx || K.kz != K.ky + B.ny || (size_t)K.kz + K.nzh > k2_len)
+            return bad("k^2 tables", ii);
+        const int Mx = B.ny * (B.nz / 2 + 1);
+        const long long dsz = K.xmode ? (long long)xpass_spectrum_floats(B.nx, Mx) / 2 : nsi;
+        if (K.doff < 0 || 2 * (K.doff + dsz) > (long long)b->spec_floats) return bad("stored spectrum", ii);
+        if (hxb[ii].soff != K.soff || hxb[ii].doff != K.doff || hxb[ii].xoff != K.xoff) return bad("x-pass descriptor", ii);
+        const RInst& R = hr[ii];
+        if (R.xpart0 != K.xoff || R.nxpart < 1 || (size_t)R.xpart0 + R.nxpart > std::max<size_t>(1, b->n_xpart))
+            return bad("partial-sum slots", ii);
+        if (R.part0 < 0 || R.nparts < 1 || R.part0 + R.nparts > (int)items.size()) return bad("work-item slots", ii);
+    }
+    std::sort(spans.begin(), spans.end());
+    for (size_t i = 1; i < spans.size(); ++i)
+        if (spans[i].first < spans[i - 1].second) return bad("overlapping field slices", (int)i);
+    for (const BatchItem& it : items) {
+        if (it.inst < 0 || it.inst >= n) return bad("work item instance", it.inst);
+        const BatchInst& B = hinst[it.inst];
+        const int TZ = B.tile ? 32 : 64, TY = B.tile ? 32 : 16;
+        if (it.x0 < 0 || it.x0 >= it.x1 || it.x1 > B.nx || it.k0 < 0 || it.k0 >= B.nz || it.k0 % TZ ||
+            it.j0 < 0 || it.j0 >= B.ny || it.j0 % TY)
+            return bad("work item bounds", it.inst);
+        if (it.part < hr[it.inst].part0 || it.part >= hr[it.inst].part0 + hr[it.inst].nparts)
+            return bad("work item slot", it.inst);
+        covered[it.inst] += (long long)(it.x1 - it.x0) * std::min(TZ, B.nz - it.k0) * std::min(TY, B.ny - it.j0);
+    }
+    for (int ii = 0; ii < n; ++ii)
+        if (covered[ii] != (long long)hinst[ii].nx * hinst[ii].ny * hinst[ii].nz) return bad("tile cover", ii);
+    return EVX_OK;
+}
+}  // namespace
+}  // namespace evx
+
 extern "C" {
 
 int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, const evx_batch_tuning* tune, int flags) {
@@ -613,6 +671,7 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
     }
     b->spec_floats = 2 * doff;
     b->n_xpart = xoff;
+    int rc0;
     // largest work items first (longest-processing-time order for the persistent blocks)
     std::stable_sort(items.begin(), items.end(), [&](const BatchItem& a, const BatchItem& c) {
         auto cost = [&](const BatchItem& x) {
@@ -622,6 +681,7 @@ int evx_batch_create(evx_batch** out, const evx_batch_instance* inst, int n, con
         return cost(a) > cost(c);
     });
     b->n_items = (int)items.size();
+    if ((rc0 = validate_layout(b, hinst, items, hk, hr, hxb, k2.size()))) return cleanup(rc0);
     // one device allocation for the tables
     const size_t s_inst = al256(sizeof(BatchInst) * n), s_items = al256(sizeof(BatchItem) * items.size());
     const size_t s_k = al256(sizeof(KInst) * n), s_r = al256(sizeof(RInst) * n), s_k2 = al256(sizeof(float) * k2.size());

@@ -23,8 +23,21 @@ namespace {
 
 using namespace fast;
 
-constexpr int RING_C = NC * MAX_FIELD, RING_M = NM * MAX_POT;
-constexpr size_t ADJ_SMEM = (size_t)(2 * RING_C + 2 * RING_M) * sizeof(float) + 4 * 8 * sizeof(double);
+// Shared-memory rings of c, g (field planes) and mu, mub (potential planes): one block barrier
+// per plane needs NC / NM slots, two barriers per plane 4 / 2 (less shared memory).
+template <bool ONEBAR>
+struct Rings {
+    static constexpr int C = (ONEBAR ? NC : 4) * MAX_FIELD, M = (ONEBAR ? NM : 2) * MAX_POT;
+    static constexpr size_t SMEM = (size_t)(2 * C + 2 * M) * sizeof(float) + 4 * 8 * sizeof(double);
+};
+// Resident blocks per SM the single-grid gradient kernels are built for: 2 (128 registers, one
+// barrier per plane) or 3 (80 registers, two barriers per plane, 68 KB of shared memory).
+#ifndef EVX_PULLBACK_MIN_BLOCKS
+#define EVX_PULLBACK_MIN_BLOCKS 2
+#endif
+constexpr bool PB_ONEBAR = EVX_PULLBACK_MIN_BLOCKS < 3;
+using PbRings = Rings<PB_ONEBAR>;
+using BatchRings = Rings<false>;   // the persistent batched kernel: two barriers per plane
 
 // Two points of a patch row (z-adjacent) are processed together with the
 // sm_100 two-lane fp32 instructions (FADD2 / FMUL2 / FFMA2).  Constants are
@@ -37,7 +50,6 @@ struct PbK {
     float2 gq1[3], gq2[3];   // -D*ih2_a/4, D*ih2_a/2
     float2 hw[3], nhw[3];    // 0.5*D*ih2_a and its negative
     float2 lk[3], lkc;       // -kappa*ih2_a, 2*kappa*sum(ih2): -kappa*Laplacian
-    float2 l[3], lc;         // ih2_a, -2*sum(ih2): the Laplacian itself (gradient sums)
     float2 w, w6, nw6;       // w, 6w, -6w
 };
 __device__ __forceinline__ PbK make_pbk(const Geo& G, const ChP& P) {
@@ -50,10 +62,8 @@ __device__ __forceinline__ PbK make_pbk(const Geo& G, const ChP& P) {
         K.hw[a] = f2s(0.5f * dg);
         K.nhw[a] = f2s(-0.5f * dg);
         K.lk[a] = f2s(-P.kappa * G.ih2[a]);
-        K.l[a] = f2s(G.ih2[a]);
     }
     K.lkc = f2s(2.f * P.kappa * G.ih2sum);
-    K.lc = f2s(-2.f * G.ih2sum);
     K.w = f2s(P.w);
     K.w6 = f2s(6.f * P.w);
     K.nw6 = f2s(-6.f * P.w);
@@ -247,7 +257,7 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     };
 
     // x face cbar'' of the output patch between planes (c0, g0, m0) and (c1, g1, m1)
-    float2 cfx_m[2], c_prev[2], b_prev[2];
+    float2 cfx_m[2], b_prev[2];
     auto x_faces_b = [&](const float* c0, const float* c1, const float* g0, const float* g1, const float* m0,
                          const float* m1, float2 out[2]) {
         out[0] = cfb2<0>(K, lds2(c0 + pa), lds2(c1 + pa), lds2(m0 + pa - W), lds2(m1 + pa - W), lds2(g0 + pa),
@@ -313,14 +323,14 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             if (wj1) *reinterpret_cast<float2*>(lam_out + o + nz) = oB;
         }
         if (GR) {
-            const float2 lcA = lapw(K.l, K.lc, A, c_prev[0], lds2(cx + pa), up, B, zmA, zpA);
-            const float2 lcB = lapw(K.l, K.lc, B, c_prev[1], lds2(cx + pb), A, dn, zmB, zpB);
+            // -<mub, L(c)> from mu = w*phi(c) - kappa*L(c) at the point: sum mub*mu and sum mub*phi,
+            // combined as (sum mub*mu - w*sum mub*phi)/kappa at the end
             if (wj0) {
-                aK = fma2(mul2(f2s(-1.f), bA), lcA, aK);
+                aK = fma2(bA, MA, aK);
                 aW = fma2(bA, phi2(A), aW);
             }
             if (wj1) {
-                aK = fma2(mul2(f2s(-1.f), bB), lcB, aK);
+                aK = fma2(bB, MB, aK);
                 aW = fma2(bB, phi2(B), aW);
             }
             if (GR == 1) {
@@ -336,8 +346,6 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
                 aH = fma2(h1, sub2(n1, u1r), aH);
             }
         }
-        c_prev[0] = A;
-        c_prev[1] = B;
         b_prev[0] = bA;
         b_prev[1] = bB;
     };
@@ -391,8 +399,6 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     {
         const int s0 = cslt(x0 - 1), s1 = cslt(x0), t0 = mslt(x0 - 1), t1 = mslt(x0);
         x_faces_b(cf(s0), cf(s1), gf(s0), gf(s1), mp(t0), mp(t1), cfx_m);
-        c_prev[0] = lds2(cf(s0) + pa);
-        c_prev[1] = lds2(cf(s0) + pb);
         b_prev[0] = lds2(bp(t0) + pa - W);
         b_prev[1] = lds2(bp(t0) + pb - W);
     }
@@ -428,22 +434,22 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         }
     }
     sD += aD.x + aD.y;
-    sK += aK.x + aK.y;
+    sK += ((aK.x + aK.y) - P.w * (aW.x + aW.y)) / P.kappa;
     sW += aW.x + aW.y;
     sH += aH.x + aH.y;
 }
 
 template <class T, int GR>
-__global__ void __launch_bounds__(THREADS, GR ? 2 : 3)
+__global__ void __launch_bounds__(THREADS, GR ? EVX_PULLBACK_MIN_BLOCKS : 3)
 ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ gfield, const float* __restrict__ lam,
                         const float* __restrict__ hfield, const float* __restrict__ u1, float* __restrict__ lam_out,
                         double* __restrict__ part, Geo G, ChP P, int seg, GradSink sink) {
     extern __shared__ __align__(16) float smem[];
     float* cs = smem;
-    float* gs = cs + RING_C;
-    float* ms = gs + RING_C;
-    float* bs = ms + RING_M;
-    double* red = reinterpret_cast<double*>(bs + RING_M);   // [4][8]
+    float* gs = cs + PbRings::C;
+    float* ms = gs + PbRings::C;
+    float* bs = ms + PbRings::M;
+    double* red = reinterpret_cast<double*>(bs + PbRings::M);   // [4][8]
     // block b owns planes [b*seg, b*seg + seg) of the tile-major sequence of
     // (tile, x) planes: one wave of equal segments, a segment that crosses a
     // tile boundary finishes one tile and starts the next
@@ -456,7 +462,7 @@ ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ g
         const int t = (int)(s0 / G.nx);
         const int xa = (int)(s0 - (long)t * G.nx);
         const int xb = (int)min((long)G.nx, xa + (s1 - s0));
-        pullback_tile<T, GR>(u, gfield, lam, hfield, u1, lam_out, G, P, (t % ntz) * T::TZ, (t / ntz) * T::TY, xa,
+        pullback_tile<T, GR, PB_ONEBAR>(u, gfield, lam, hfield, u1, lam_out, G, P, (t % ntz) * T::TZ, (t / ntz) * T::TY, xa,
                              xb, cs, gs, ms, bs, sD, sK, sW, sH);
         s0 += xb - xa;   // the tile's last barrier protects the rings from the next tile's prologue
     }
@@ -492,10 +498,10 @@ ch_pullback_batch_kernel(const float* __restrict__ u, const float* __restrict__ 
                          const BatchItem* __restrict__ items, int n_items, int* __restrict__ counter) {
     extern __shared__ __align__(16) float smem[];
     float* cs = smem;
-    float* gs = cs + RING_C;
-    float* ms = gs + RING_C;
-    float* bs = ms + RING_M;
-    double* red = reinterpret_cast<double*>(bs + RING_M);
+    float* gs = cs + BatchRings::C;
+    float* ms = gs + BatchRings::C;
+    float* bs = ms + BatchRings::M;
+    double* red = reinterpret_cast<double*>(bs + BatchRings::M);
     __shared__ int s_item;
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
@@ -529,20 +535,20 @@ void init_occupancy() {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-    auto setup = [](auto kern, int* out) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ADJ_SMEM);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, THREADS, ADJ_SMEM);
+    auto setup = [](auto kern, int* out, size_t smem) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, THREADS, smem);
         if (*out < 1) *out = 1;
     };
-    setup(ch_pullback_fast_kernel<TileWide, 0>, &g_bps[0][0]);
-    setup(ch_pullback_fast_kernel<TileWide, 1>, &g_bps[0][1]);
-    setup(ch_pullback_fast_kernel<TileWide, 2>, &g_bps[0][2]);
-    setup(ch_pullback_fast_kernel<TileSquare, 0>, &g_bps[1][0]);
-    setup(ch_pullback_fast_kernel<TileSquare, 1>, &g_bps[1][1]);
-    setup(ch_pullback_fast_kernel<TileSquare, 2>, &g_bps[1][2]);
-    setup(ch_pullback_batch_kernel<0>, &g_batch_bps[0]);
-    setup(ch_pullback_batch_kernel<1>, &g_batch_bps[1]);
-    setup(ch_pullback_batch_kernel<2>, &g_batch_bps[2]);
+    setup(ch_pullback_fast_kernel<TileWide, 0>, &g_bps[0][0], PbRings::SMEM);
+    setup(ch_pullback_fast_kernel<TileWide, 1>, &g_bps[0][1], PbRings::SMEM);
+    setup(ch_pullback_fast_kernel<TileWide, 2>, &g_bps[0][2], PbRings::SMEM);
+    setup(ch_pullback_fast_kernel<TileSquare, 0>, &g_bps[1][0], PbRings::SMEM);
+    setup(ch_pullback_fast_kernel<TileSquare, 1>, &g_bps[1][1], PbRings::SMEM);
+    setup(ch_pullback_fast_kernel<TileSquare, 2>, &g_bps[1][2], PbRings::SMEM);
+    setup(ch_pullback_batch_kernel<0>, &g_batch_bps[0], BatchRings::SMEM);
+    setup(ch_pullback_batch_kernel<1>, &g_batch_bps[1], BatchRings::SMEM);
+    setup(ch_pullback_batch_kernel<2>, &g_batch_bps[2], BatchRings::SMEM);
 }
 
 // One wave of blocks over equal segments of the tile-major (tile, x) plane
@@ -572,14 +578,14 @@ int pb_launch_t(int grads, const float* u, const float* g, const float* lam, con
     if (n_part_used) *n_part_used = nb;
     if (grads == 1)
         EVX_TIMED("ch_pullback_grads", st,
-                  ch_pullback_fast_kernel<T, 1><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, seg, S));
+                  ch_pullback_fast_kernel<T, 1><<<grid, THREADS, PbRings::SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, seg, S));
     else if (grads == 2)
         EVX_TIMED("ch_pullback_grads_spec", st,
-                  ch_pullback_fast_kernel<T, 2><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out, part,
+                  ch_pullback_fast_kernel<T, 2><<<grid, THREADS, PbRings::SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out, part,
                                                                                  G, P, seg, S));
     else
         EVX_TIMED("ch_pullback", st,
-                  ch_pullback_fast_kernel<T, 0><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
+                  ch_pullback_fast_kernel<T, 0><<<grid, THREADS, PbRings::SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
                                                                                  nullptr, G, P, seg, S));
     count_launch();
     return check_launch("ch_pullback_fast_kernel");
@@ -621,15 +627,15 @@ int batch_pullback_launch(int grads, const float* u, const float* g, const float
     if (rc) return rc;
     if (grads == 1)
         EVX_TIMED("batch_pullback_grads", st,
-                  ch_pullback_batch_kernel<1><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, h, u1, lam_out, part, insts,
+                  ch_pullback_batch_kernel<1><<<grid, THREADS, BatchRings::SMEM, st>>>(u, g, lam, h, u1, lam_out, part, insts,
                                                                                items, n_items, counter));
     else if (grads == 2)
         EVX_TIMED("batch_pullback_grads_spec", st,
-                  ch_pullback_batch_kernel<2><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
+                  ch_pullback_batch_kernel<2><<<grid, THREADS, BatchRings::SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
                                                                                part, insts, items, n_items, counter));
     else
         EVX_TIMED("batch_pullback", st,
-                  ch_pullback_batch_kernel<0><<<grid, THREADS, ADJ_SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
+                  ch_pullback_batch_kernel<0><<<grid, THREADS, BatchRings::SMEM, st>>>(u, g, lam, nullptr, nullptr, lam_out,
                                                                                nullptr, insts, items, n_items, counter));
     count_launch();
     return check_launch("ch_pullback_batch_kernel");

@@ -182,3 +182,39 @@ def test_batched_xpass_groups_match_cufft3d(cuda_lib, variant):
         assert oracle.rel_to_max(la[i].cpu().numpy(), lb[i].cpu().numpy()) < 1e-5, i
         # real-space gradient sums difference float32 states: the cross-FFT bar
         np.testing.assert_allclose(ga[i], gb[i], rtol=1e-3, atol=1e-9)
+
+
+ODD = [(8, 12, 100), (24, 20, 36), (16, 24, 64), (8, 12, 100), (48, 8, 4), (12, 16, 8), (32, 32, 32), (64, 8, 12),
+       (6, 5, 28), (8, 12, 100)]
+
+
+@pytest.mark.parametrize("tune", [{}, {"x_chunk": 3}, {"tile_variant": 1, "x_chunk": 5}, {"fft_group_max": 1},
+                                  {"tile_variant": 0, "blocks_per_sm": 1}])
+def test_batched_odd_group_layouts_match_single_grids(cuda_lib, tune):
+    """Ten instances in eight shape groups (padding between groups, nz down to 4, ny below the tile
+    height, x chunks that do not divide nx), every tile shape and chunking: the layout passes the
+    batch's own descriptor check at creation, and every instance (forward with trajectory, then the
+    adjoint) equals the instance run alone within 1e-6 / 1e-5."""
+    from evoxels_gb300.adjoint import CahnHilliardAdjoint
+    from evoxels_gb300.batched import BatchedCahnHilliard, BatchTuning
+    d = [1.0 + 0.1 * i for i in range(len(ODD))]
+    e = [0.5 + 0.2 * i for i in range(len(ODD))]
+    b = BatchedCahnHilliard(ODD, d, e, 0.1, tuning=BatchTuning(**tune))
+    f = [oracle.seeded_ch_field(s, 300 + i) for i, s in enumerate(ODD)]
+    n = 3
+    states = torch.empty((n + 1) * b.total, dtype=torch.float32, device="cuda")
+    states[:b.total].copy_(b.pack(f))
+    out = b.forward(states[:b.total], n, traj=states[b.total:])
+    lam = b.pack([np.random.default_rng([13, i]).random(s) - 0.5 for i, s in enumerate(ODD)])
+    grads = torch.zeros((b.n, 3), dtype=torch.float64, device="cuda")
+    lo = b.unpack(b.adjoint(states, n, lam, grads))
+    outs = b.unpack(out)
+    lams = b.unpack(lam)
+    for i, s in enumerate(ODD):
+        vg, prob, st = single(s, d[i], e[i])
+        ref = st.advance(torch.tensor(f[i], dtype=torch.float32, device="cuda").unsqueeze(0), n)
+        assert oracle.rel_to_max(outs[i].cpu().numpy(), ref.cpu().numpy()) < 1e-6, (i, tune)
+        r = CahnHilliardAdjoint(vg, 0.1)
+        tr = torch.stack([b.unpack(states[k * b.total:(k + 1) * b.total])[i][0] for k in range(n + 1)]).contiguous()
+        lr = r.adjoint(tr, n, lams[i].contiguous(), d[i], e[i], None)
+        assert oracle.rel_to_max(lo[i].cpu().numpy(), lr.cpu().numpy()) < 1e-5, (i, tune)
