@@ -24,7 +24,7 @@ import torch
 from . import _lib
 from .problem_definition import CahnHilliard
 from .timesteppers import get_plan
-from .voxelgrid import VoxelGridGB300, cuda_stream
+from .voxelgrid import VoxelGridGB300, cuda_stream, normalize_bc
 
 
 class CahnHilliardAdjoint:
@@ -39,14 +39,23 @@ class CahnHilliardAdjoint:
     adjoint forms the mobility gradient sums by Parseval in k-space; this
     costs one more field-sized buffer per step and saves an inverse FFT and
     two field reads per adjoint step.
+
+    ``bc``: the problem's boundary conditions; a Neumann or Dirichlet x axis
+    selects the mirrored-x step (y and z periodic, as the reference's FFT
+    steppers require), whose adjoint gives ``dL/dc0`` only (parameter
+    gradients raise ``NotImplementedError``).
     """
 
-    def __init__(self, vg: VoxelGridGB300, dt=0.1, A=0.25, pinned_w=None, spectral=True):
+    def __init__(self, vg: VoxelGridGB300, dt=0.1, A=0.25, pinned_w=None, spectral=True, bc=None):
         self.vg = vg
         self.dt = float(dt)
         self.A = float(A)
         self.pinned_w = pinned_w
-        self.plan = get_plan(vg, grads=True)
+        self.bc = None if bc is None else normalize_bc(bc, vg.convention)
+        if self.bc is not None and all(kind == "periodic" for kind, _ in self.bc):
+            self.bc = None
+        self.mirrored = self.bc is not None
+        self.plan = get_plan(vg, grads=not self.mirrored, bc=self.bc)
         self.spec_floats = int(_lib.lib().evx_ch_spectrum_floats(self.plan.handle)) if spectral else 0
         self.n = int(np.prod(vg.shape))
         self._pcache = {}
@@ -62,7 +71,10 @@ class CahnHilliardAdjoint:
 
     def _make_params(self, D, eps):
         mu = None if self.pinned_w is None else (lambda c, lib=None, w=self.pinned_w: w * c * (1 - c) * (1 - 2 * c))
-        prob = CahnHilliard(self.vg, eps=float(eps), D=float(D), mu_hom=mu, A=self.A)
+        kw = {} if self.bc is None else {"bc": self.bc}
+        prob = CahnHilliard(self.vg, eps=float(eps), D=float(D), mu_hom=mu, A=self.A, **kw)
+        if self.bc is not None:
+            prob.verify_fft_bc_config()
         return prob.evx_params(self.dt)
 
     def new_spectra(self, nsteps):

@@ -14,6 +14,16 @@
 //   lam_i  = lam'_i + [0 <= u_i <= 1] * cbar_i       (torch.clip passes the gradient inside [0,1])
 // L is the periodic 7-point Laplacian, which is symmetric.
 //
+// A Neumann or Dirichlet x axis (the mirrored-x step; y and z stay periodic):
+// the reference pads c and mu with the same ghost g = a*cell + b (a = 1 Neumann,
+// -1 Dirichlet; evoxels/boundary_conditions.py:33-59) and r lives on interior
+// cells only.  Folding the ghosts' cotangents back into the boundary cell gives,
+// at a boundary cell: g = 0 on the ghost side, the boundary face's Gb term in
+// mub weighted by (1 - a), its cfb term weighted by (1 + a)/2 instead of 1/2,
+// mub continued by a*mub into the ghost for L(mub), and mu by its forward ghost.
+// The spectral operator of the mirrored step is symmetric too (see
+// ch_apply_spectral), so g = P lam' is the forward operator applied to lam'.
+//
 // Parameter gradients (optional): with a = kappa*D*A (fourier_symbol = -a k^4,
 // evoxels/problem_definition.py:303) and K = irfft.diag(prefac*k^4/N).rfft,
 //   dL/dD     += <g, div>            - kappa*A*<K lam', u' - u>
@@ -61,23 +71,31 @@ ch_pullback_kernel(const float* __restrict__ u, const float* __restrict__ g, con
     const float D = P.D, kap = P.kappa, w = P.w;
     const float ihx = G.ih[0], ihy = G.ih[1], ihz = G.ih[2];
     double sD = 0.0, sK = 0.0, sW = 0.0, sH = 0.0;
+    const bool xb = G.kind[0] != EVX_BC_PERIODIC;          // ghosts in x (y and z periodic)
+    const float ax = G.kind[0] == EVX_BC_DIRICHLET ? -1.f : 1.f;
+    auto xin = [&](int p) { return xb ? min(max(p, 0), G.nx - 1) : p; };   // the plane a ghost derives from
 
     auto load_plane = [&](int p) {
-        const int gp = pmod(p, G.nx);
+        const bool ghost = xb && (p < 0 || p >= G.nx);
+        const int gp = xb ? xin(p) : pmod(p, G.nx);
         const int sl = (p + 10) % 5;
         for (int e = tid; e < CY * CZ; e += CH_THREADS) {
             const int jj = e / CZ, kk = e - jj * CZ;
             const int gj = pmod(j0 + jj - 2, G.ny), gk = pmod(k0 + kk - 2, G.nz);
             const size_t idx = (size_t)gp * plane + (size_t)gj * G.nz + gk;
-            cs[sl][jj][kk] = clip01(__ldg(u + idx));
-            gs[sl][jj][kk] = __ldg(g + idx);
+            const float c = clip01(__ldg(u + idx));
+            cs[sl][jj][kk] = ghost ? (p < 0 ? ghost_lo(G, 0, c) : ghost_hi(G, 0, c)) : c;
+            gs[sl][jj][kk] = ghost ? 0.f : __ldg(g + idx);
         }
     };
 
-    // mu and mub on plane p over the tile grown by one cell
+    // mu and mub on plane p over the tile grown by one cell; a ghost plane holds the forward
+    // ghost of mu and a*mub of the boundary plane it derives from
     auto compute_mu = [&](int p) {
-        const int s0 = (p + 10) % 5, sm = (p + 9) % 5, sp = (p + 11) % 5;
+        const int q = xin(p);
+        const int s0 = (q + 10) % 5, sm = (q + 9) % 5, sp = (q + 11) % 5;
         const int sl = (p + 9) % 3;
+        const float fm = (xb && q == 0) ? 1.f - ax : 1.f, fp = (xb && q == G.nx - 1) ? 1.f - ax : 1.f;
         for (int e = tid; e < MY * MZ; e += CH_THREADS) {
             const int a = e / MZ, b = e - a * MZ;
             const int jj = a + 1, kk = b + 1;
@@ -86,16 +104,21 @@ ch_pullback_kernel(const float* __restrict__ u, const float* __restrict__ g, con
             const float cym = cs[s0][jj - 1][kk], cyp = cs[s0][jj + 1][kk];
             const float czm = cs[s0][jj][kk - 1], czp = cs[s0][jj][kk + 1];
             const float lap = lap7(G, c, cxm, cxp, cym, cyp, czm, czp);
-            ms[sl][a][b] = __fsub_rn(mu_hom(w, c), __fmul_rn(kap, lap));
+            float mu = __fsub_rn(mu_hom(w, c), __fmul_rn(kap, lap));
             const float gc = gs[s0][jj][kk];
             // Gbar on the faces: Fb * m(cf)
             auto gb = [&](float c_lo, float c_hi, float g_lo, float g_hi, float ih) {
                 const float cf = 0.5f * (c_lo + c_hi);
                 return ih * D * (g_lo - g_hi) * (cf * (1.f - cf));
             };
-            float v = ihx * (gb(cxm, c, gs[sm][jj][kk], gc, ihx) - gb(c, cxp, gc, gs[sp][jj][kk], ihx));
+            float v = ihx * (fm * gb(cxm, c, gs[sm][jj][kk], gc, ihx) - fp * gb(c, cxp, gc, gs[sp][jj][kk], ihx));
             v += ihy * (gb(cym, c, gs[s0][jj - 1][kk], gc, ihy) - gb(c, cyp, gc, gs[s0][jj + 1][kk], ihy));
             v += ihz * (gb(czm, c, gs[s0][jj][kk - 1], gc, ihz) - gb(c, czp, gc, gs[s0][jj][kk + 1], ihz));
+            if (p != q) {
+                mu = p < 0 ? ghost_lo(G, 0, mu) : ghost_hi(G, 0, mu);
+                v *= ax;
+            }
+            ms[sl][a][b] = mu;
             mb[sl][a][b] = v;
         }
     };
@@ -110,8 +133,9 @@ ch_pullback_kernel(const float* __restrict__ u, const float* __restrict__ g, con
             const int jj = a + 2, kk = b + 2, ja = a + 1, kb = b + 1;
             const float c = cs[s0][jj][kk], mu = ms[m0][ja][kb], mub = mb[m0][ja][kb], gc = gs[s0][jj][kk];
             float acc = 0.f, div = 0.f;
-            // one axis: neighbours (lo, hi) of c, mu, g
-            auto axis = [&](float c_lo, float c_hi, float m_lo, float m_hi, float g_lo, float g_hi, float ih) {
+            // one axis: neighbours (lo, hi) of c, mu, g; wlo / whi weight the faces' cbar terms
+            auto axis = [&](float c_lo, float c_hi, float m_lo, float m_hi, float g_lo, float g_hi, float ih,
+                            float wlo = 1.f, float whi = 1.f) {
                 // + face (c, c_hi)
                 const float cfp = 0.5f * (c + c_hi);
                 const float Gp = (m_hi - mu) * ih;
@@ -120,13 +144,14 @@ ch_pullback_kernel(const float* __restrict__ u, const float* __restrict__ g, con
                 const float cfm = 0.5f * (c_lo + c);
                 const float Gm = (mu - m_lo) * ih;
                 const float Fbm = ih * D * (g_lo - gc);
-                acc += 0.5f * ((Fbp * Gp) * (1.f - 2.f * cfp) + (Fbm * Gm) * (1.f - 2.f * cfm));
+                acc += 0.5f * (whi * ((Fbp * Gp) * (1.f - 2.f * cfp)) + wlo * ((Fbm * Gm) * (1.f - 2.f * cfm)));
                 if (GRADS) div += ((cfp * (1.f - cfp)) * Gp - (cfm * (1.f - cfm)) * Gm) * ih;
             };
             const float cxm = cs[sm][jj][kk], cxp = cs[sp][jj][kk];
             const float cym = cs[s0][jj - 1][kk], cyp = cs[s0][jj + 1][kk];
             const float czm = cs[s0][jj][kk - 1], czp = cs[s0][jj][kk + 1];
-            axis(cxm, cxp, ms[mm][ja][kb], ms[mp][ja][kb], gs[sm][jj][kk], gs[sp][jj][kk], ihx);
+            axis(cxm, cxp, ms[mm][ja][kb], ms[mp][ja][kb], gs[sm][jj][kk], gs[sp][jj][kk], ihx,
+                 (xb && i == 0) ? 1.f + ax : 1.f, (xb && i == G.nx - 1) ? 1.f + ax : 1.f);
             axis(cym, cyp, ms[m0][ja - 1][kb], ms[m0][ja + 1][kb], gs[s0][jj - 1][kk], gs[s0][jj + 1][kk], ihy);
             axis(czm, czp, ms[m0][ja][kb - 1], ms[m0][ja][kb + 1], gs[s0][jj][kk - 1], gs[s0][jj][kk + 1], ihz);
             const float lmb = lap7(G, mub, mb[mm][ja][kb], mb[mp][ja][kb], mb[m0][ja - 1][kb], mb[m0][ja + 1][kb],
@@ -283,7 +308,9 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
     if ((reinterpret_cast<uintptr_t>(lam_in) | reinterpret_cast<uintptr_t>(lam_out)) & 15)
         return fail(EVX_ERR_BAD_ARG, "lam_in and lam_out must be 16-byte aligned");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
-    if (plan->xext) return fail(EVX_ERR_UNSUPPORTED, "the adjoint of the mirrored-x spectral step is not built");
+    if (plan->xext && (grads || spectra))
+        return fail(EVX_ERR_UNSUPPORTED,
+                    "the mirrored-x (Neumann/Dirichlet x) adjoint gives dL/du only: pass no gradients or spectra");
     if (prm->bulk != EVX_BULK_DOUBLE_WELL)
         return fail(EVX_ERR_UNSUPPORTED, "the adjoint is built for the double-well bulk term w*c(1-c)(1-2c)");
     const bool want = grads != nullptr;
@@ -321,6 +348,21 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
     int* counter = reinterpret_cast<int*>(part + plan->n_part * 4);
     if (spectral && (rc = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), st), "reduction counter"))) return rc;
     const float* lam = lam_in;
+    if (plan->xext) {   // mirrored x: g = P lam' by the (symmetric) forward operator, generic pullback with ghosts
+        const Geo Gb = make_geo(g, &plan->bc);
+        float* gout = reinterpret_cast<float*>(ws_at(workspace, plan->off_upd));
+        for (int s = nsteps - 1; s >= 0; --s) {
+            float* dst = (s % 2 == 0) ? lam_out : lbuf;
+            if ((rc = ch_apply_spectral(plan, lam, gbuf, gout, spec, P, st))) return rc;
+            EVX_TIMED("ch_pullback", st,
+                      ch_pullback_kernel<false><<<sg, dim3(32, 8), 0, st>>>(states + (size_t)s * N, gout, lam, nullptr,
+                                                                             nullptr, dst, nullptr, Gb, P, lx));
+            count_launch();
+            if ((rc = check_launch("ch_pullback_kernel"))) return rc;
+            lam = dst;
+        }
+        return EVX_OK;
+    }
     for (int s = nsteps - 1; s >= 0; --s) {
         float* dst = (s % 2 == 0) ? lam_out : lbuf;
         int nxp = 0;   // x-pass partial-sum slots of this step

@@ -350,6 +350,31 @@ int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_
     return check_launch("ch_kspace_fwd_kernel");
 }
 
+// out = P in, the step's spectral operator irfft . diag(prefac/N) . rfft with the x mirror
+// extension of a non-periodic x axis (evoxels/timesteppers.py:85-89, boundary_conditions.py:64-70).
+// P is symmetric (prefac depends on k^2 only, and the extension, the multiply and the restriction
+// to the first nx planes commute with the reflection), so this is also its adjoint.  ext: 2*n floats
+// of scratch for the cuFFT 3-D mirror path; out: 2*n floats on that path, n otherwise.
+int ch_apply_spectral(evx_ch_plan* plan, const float* in, float* ext, float* out, float2* spec, const ChP& P,
+                      cudaStream_t st) {
+    int rc;
+    const float* src = in;
+    if (plan->xext && !plan->xmode) {
+        const size_t N = plan->n;
+        if ((rc = check_cuda(cudaMemcpyAsync(ext, in, N * sizeof(float), cudaMemcpyDeviceToDevice, st),
+                             "mirror extension copy")))
+            return rc;
+        EVX_TIMED("ch_mirror_x", st, ch_mirror_x_kernel<<<elementwise_grid(N), 256, 0, st>>>(
+            ext, plan->g.nx, (size_t)plan->g.ny * plan->g.nz, plan->xext == 2 ? -1.f : 1.f));
+        count_launch();
+        if ((rc = check_launch("ch_mirror_x_kernel"))) return rc;
+        src = ext;
+    }
+    if ((rc = ch_r2c(plan, src, spec, st))) return rc;
+    if ((rc = ch_kspace_forward(plan, spec, P, st))) return rc;
+    return ch_c2r(plan, spec, out, false, st);
+}
+
 }  // namespace evx
 
 using namespace evx;

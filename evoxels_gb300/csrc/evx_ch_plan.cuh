@@ -69,6 +69,10 @@ __device__ __forceinline__ float imex_prefac(float k2, float sym_coef, float dt)
 // Forward k-space multiply: spec *= prefac(k) then * invN (in that order);
 // with dspec (x-pass plans only) the product is also stored there.
 int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st, float2* dspec = nullptr);
+// out = P in, the step's (symmetric) spectral operator, x mirror extension included; ext: 2*n
+// floats of scratch and out 2*n floats on a cuFFT 3-D mirror plan, out n floats otherwise.
+int ch_apply_spectral(evx_ch_plan* plan, const float* in, float* ext, float* out, float2* spec, const ChP& P,
+                      cudaStream_t st);
 
 // Fused spectral x-pass (evx_fftx.cu): mode 0 forward multiply (and optional
 // store of the increment spectrum into dspec), 1 adjoint g, 2 adjoint g and h

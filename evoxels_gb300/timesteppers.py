@@ -134,19 +134,18 @@ class PseudoSpectralIMEX(TimeStepper):
         return self.dt / (1 - self.dt * self.problem.fourier_symbol)
 
     def _check(self, u):
-        u = self.problem.vg.check_field(u)
-        if u.shape[0] != 1:
-            # the reference transforms over (C, Nx, Ny, Nz) and so couples channels;
-            # evoxels_gb300 builds the single-field step only
-            raise NotImplementedError("PseudoSpectralIMEX in evoxels_gb300 steps one field (C == 1)")
-        return u
+        return self.problem.vg.check_field(u)
 
     def step(self, t, u):
+        """One step of every channel.  The reference transforms the whole ``(C, Nx, Ny, Nz)`` field, but
+        its multiplier does not depend on the channel frequency, so the channel transform and its inverse
+        cancel and the step is the single-field step of each channel (up to rounding)."""
         u = self._check(u)
         out = torch.empty_like(u)
         p = self._plan
-        _lib.check(_lib.lib().evx_ch_step(p.handle, u.data_ptr(), out.data_ptr(), self._params,
-                                          p.workspace.data_ptr(), cuda_stream()), "evx_ch_step")
+        for ch in range(u.shape[0]):
+            _lib.check(_lib.lib().evx_ch_step(p.handle, u[ch].data_ptr(), out[ch].data_ptr(), self._params,
+                                              p.workspace.data_ptr(), cuda_stream()), "evx_ch_step")
         return out
 
     def advance(self, u, nsteps, traj=None, nonfinite=None, t0=0.0):
@@ -157,13 +156,16 @@ class PseudoSpectralIMEX(TimeStepper):
         p = self._plan
         tp = 0
         if traj is not None:
+            if u.shape[0] != 1:
+                raise NotImplementedError("a kept trajectory is built for one channel (C == 1)")
             if traj.dtype != torch.float32 or not traj.is_contiguous() or traj.numel() < nsteps * p.n:
                 raise ValueError("traj must be a contiguous float32 tensor holding nsteps fields")
             tp = traj.data_ptr()
         nf = nonfinite.data_ptr() if nonfinite is not None else None
-        _lib.check(_lib.lib().evx_ch_forward(p.handle, u.data_ptr(), out.data_ptr(), int(nsteps), tp or None,
-                                             self._params, nf, p.workspace.data_ptr(), cuda_stream()),
-                   "evx_ch_forward")
+        for ch in range(u.shape[0]):   # channels step independently (see step)
+            _lib.check(_lib.lib().evx_ch_forward(p.handle, u[ch].data_ptr(), out[ch].data_ptr(), int(nsteps),
+                                                 tp or None, self._params, nf, p.workspace.data_ptr(),
+                                                 cuda_stream()), "evx_ch_forward")
         return out
 
 
@@ -295,20 +297,19 @@ class ExponentialEuler(TimeStepper):
         return 1
 
     def step(self, t, u):
+        """One step of every channel (the channel transform of the reference's ``(C, Nx, Ny, Nz)`` FFT
+        cancels against its inverse: the table does not depend on the channel frequency)."""
         u = self.problem.vg.check_field(u)
-        if u.shape[0] != 1:
-            # the reference transforms over (C, Nx, Ny, Nz) and so couples channels;
-            # evoxels_gb300 builds the single-field step only
-            raise NotImplementedError("ExponentialEuler in evoxels_gb300 steps one field (C == 1)")
         if isinstance(self.problem, CahnHilliard):
             # the spectral loop's own rhs pass, so that n steps equal advance(u, n) bit for bit
             return self.advance(u, 1, t0=t)
         r = self.problem.rhs(t, u)
         out = torch.empty_like(u)
         p = self._plan
-        _lib.check(_lib.lib().evx_spectral_update(p.handle, u.data_ptr(), r.data_ptr(), self._mult.data_ptr(),
-                                                  out.data_ptr(), p.workspace.data_ptr(), cuda_stream()),
-                   "evx_spectral_update")
+        for ch in range(u.shape[0]):
+            _lib.check(_lib.lib().evx_spectral_update(p.handle, u[ch].data_ptr(), r[ch].data_ptr(),
+                                                      self._mult.data_ptr(), out[ch].data_ptr(),
+                                                      p.workspace.data_ptr(), cuda_stream()), "evx_spectral_update")
         return out
 
     def advance(self, u, nsteps, nonfinite=None, t0=0.0):
@@ -321,14 +322,14 @@ class ExponentialEuler(TimeStepper):
                 u = self.step(t0 + k * self.dt, u)
             return u
         u = self.problem.vg.check_field(u)
-        if u.shape[0] != 1:
-            raise NotImplementedError("ExponentialEuler in evoxels_gb300 steps one field (C == 1)")
         out = torch.empty_like(u)
         p = self._plan
         nf = nonfinite.data_ptr() if nonfinite is not None else None
-        _lib.check(_lib.lib().evx_ch_forward_mult(p.handle, u.data_ptr(), out.data_ptr(), int(nsteps),
-                                                  self._mult.data_ptr(), self.problem.evx_params(self.dt), nf,
-                                                  p.workspace.data_ptr(), cuda_stream()), "evx_ch_forward_mult")
+        prm = self.problem.evx_params(self.dt)
+        for ch in range(u.shape[0]):
+            _lib.check(_lib.lib().evx_ch_forward_mult(p.handle, u[ch].data_ptr(), out[ch].data_ptr(), int(nsteps),
+                                                      self._mult.data_ptr(), prm, nf, p.workspace.data_ptr(),
+                                                      cuda_stream()), "evx_ch_forward_mult")
         return out
 
 

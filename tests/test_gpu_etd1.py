@@ -125,10 +125,13 @@ def test_etd1_allen_cahn_driver_and_errors(cuda_lib):
     for _ in range(6):
         ref = oracle.imex_step(ref, m, lambda w: oracle.ac_rhs(w, eps=2.0, bc=bc), bc)
     assert oracle.rel_to_max(vf.fields["phi"], ref.numpy()[0]) < 3e-5
-    # channels couple in the reference's 4-D transform: one field only
+    # two channels: the reference's 4-D transform (channel axis included) against per-channel steps
     st = ExponentialEuler(CahnHilliard(vg_for((8, 8, 8))), 0.1)
-    with pytest.raises(NotImplementedError):
-        st.step(0.0, torch.rand((2, 8, 8, 8), device=DEV))
+    u2 = oracle.seeded_ch_field((2, 8, 8, 8), 96)
+    got = st.step(0.0, torch.tensor(u2, dtype=torch.float32, device=DEV)).cpu().numpy()
+    m8 = oracle.etd1_multiplier(-2 * 3.0 * 1.0 * 0.25 * oracle.rfft_k_squared((8, 8, 8), dtype=torch.float64) ** 2, 0.1)
+    ref2 = oracle.imex_step(torch.tensor(u2), m8, lambda w: oracle.ch_rhs(w))
+    assert oracle.rel_to_max(got, ref2.numpy()) < 1e-5
     plan = get_plan(st.problem.vg)
     x = torch.zeros((1, 8, 8, 8), device=DEV)
     with pytest.raises(_lib.EvxError, match="NULL"):
