@@ -171,14 +171,25 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     const size_t plane = (size_t)ny * nz;
     const PbK K = make_pbk(G, P);
     const LoadPlan LP = make_load_plan<T>(tid, j0, k0, ny, nz);
-    int mo_[2];   // field offsets of the potential patches (upper row, left column)
-    bool mv[2];
-#pragma unroll
-    for (int m = 0; m < 2; ++m) {
-        const int pidx = tid + m * THREADS;
-        mv[m] = pidx < T::NMU;
-        const int py = mv[m] ? pidx / T::MPZ : 0;
-        mo_[m] = (1 + 2 * py) * W + 2 + 2 * (pidx - py * T::MPZ);
+    // Stage-A work (mu and mub over the tile grown by one cell, T::NMU 2x2 patches): patch tid for
+    // every thread, and the patches beyond THREADS split into single rows over the first 2*(NMU -
+    // THREADS) threads, so the warps that take the extra work carry half a patch more, not a whole one
+    // (the block barrier waits for the slowest warp every plane).
+    constexpr int NHALF = T::NMU > THREADS ? 2 * (T::NMU - THREADS) : 0;
+    static_assert(NHALF <= THREADS, "at most one extra row per thread");
+    int mo_[1];   // field offset of this thread's potential patch (upper row, left column)
+    bool mv[1];
+    mv[0] = tid < T::NMU;
+    {
+        const int py = mv[0] ? tid / T::MPZ : 0;
+        mo_[0] = (1 + 2 * py) * W + 2 + 2 * (tid - py * T::MPZ);
+    }
+    const bool hv = tid < NHALF;   // this thread's extra row
+    int ho;
+    {
+        const int q = hv ? THREADS + (tid >> 1) : 0;
+        const int py = q / T::MPZ;
+        ho = (1 + 2 * py + (tid & 1)) * W + 2 + 2 * (q - py * T::MPZ);
     }
     const int ra = 2 + 2 * ty, rc = 4 + 2 * tx;
     const int gj = j0 + 2 * ty, gk = k0 + 2 * tx;
@@ -207,7 +218,8 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             }
     };
 
-    float2 gxm[2][2];   // Gb'' on the x face below the current potential plane, per patch row
+    float2 gxm[1][2];   // Gb'' on the x face below the current potential plane, per patch row
+    float2 gxh;         // the same for the extra row
     // x faces between field slots c0/g0 (plane p) and c1/g1 (plane p+1) of potential patch m
     auto gx_faces = [&](const float* c0, const float* c1, const float* g0, const float* g1, int m, float2 out[2]) {
         const int a = mo_[m], b = a + W;
@@ -220,7 +232,7 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     auto compute_mu = [&](const float* cm, const float* cc, const float* cp, const float* gc, const float* gp,
                           float* mo, float* bo) {
 #pragma unroll
-        for (int m = 0; m < 2; ++m) {
+        for (int m = 0; m < 1; ++m) {
             if (!mv[m]) continue;
             const int a = mo_[m], b = a + W;
             const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
@@ -253,6 +265,22 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             }
             *reinterpret_cast<float2*>(bo + a - W) = bA;
             *reinterpret_cast<float2*>(bo + b - W) = bB;
+        }
+        if (hv) {   // the extra row: the same terms for one row
+            const int a = ho;
+            const float2 up = lds2(cc + a - W), A = lds2(cc + a), dn = lds2(cc + a + W);
+            const float2 zmA = make_float2(cc[a - 1], A.x), zpA = make_float2(A.y, cc[a + 2]);
+            *reinterpret_cast<float2*>(mo + a - W) =
+                fma2(K.w, phi2(A), lapw(K.lk, K.lkc, A, lds2(cm + a), lds2(cp + a), up, dn, zmA, zpA));
+            const float2 gA = lds2(gc + a);
+            const float2 gxp = gb2<0>(K, A, lds2(cp + a), gA, lds2(gp + a));
+            float2 bA = sub2(gxh, gxp);
+            gxh = gxp;
+            const float2 gup = lds2(gc + a - W), gdn = lds2(gc + a + W);
+            const float2 gzmA = make_float2(gc[a - 1], gA.x), gzpA = make_float2(gA.y, gc[a + 2]);
+            bA = add2(bA, sub2(gb2<2>(K, zmA, A, gzmA, gA), gb2<2>(K, A, zpA, gA, gzpA)));
+            bA = add2(bA, sub2(gb2<1>(K, up, A, gup, gA), gb2<1>(K, A, dn, gA, gdn)));
+            *reinterpret_cast<float2*>(bo + a - W) = bA;
         }
     };
 
@@ -372,9 +400,9 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         }
         fetch(x0 + 3);
         __syncthreads();
-#pragma unroll
-        for (int m = 0; m < 2; ++m)
-            if (mv[m]) gx_faces(cf(cslt(x0 - 2)), cf(cslt(x0 - 1)), gf(cslt(x0 - 2)), gf(cslt(x0 - 1)), m, gxm[m]);
+        if (mv[0]) gx_faces(cf(cslt(x0 - 2)), cf(cslt(x0 - 1)), gf(cslt(x0 - 2)), gf(cslt(x0 - 1)), 0, gxm[0]);
+        if (hv) gxh = gb2<0>(K, lds2(cf(cslt(x0 - 2)) + ho), lds2(cf(cslt(x0 - 1)) + ho), lds2(gf(cslt(x0 - 2)) + ho),
+                             lds2(gf(cslt(x0 - 1)) + ho));
         mu_of(x0 - 1);
         mu_of(x0);
         mu_of(x0 + 1);
@@ -389,9 +417,9 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         }
         fetch(x0 + 2);
         __syncthreads();
-#pragma unroll
-        for (int m = 0; m < 2; ++m)
-            if (mv[m]) gx_faces(cf(cslt(x0 - 2)), cf(cslt(x0 - 1)), gf(cslt(x0 - 2)), gf(cslt(x0 - 1)), m, gxm[m]);
+        if (mv[0]) gx_faces(cf(cslt(x0 - 2)), cf(cslt(x0 - 1)), gf(cslt(x0 - 2)), gf(cslt(x0 - 1)), 0, gxm[0]);
+        if (hv) gxh = gb2<0>(K, lds2(cf(cslt(x0 - 2)) + ho), lds2(cf(cslt(x0 - 1)) + ho), lds2(gf(cslt(x0 - 2)) + ho),
+                             lds2(gf(cslt(x0 - 1)) + ho));
         mu_of(x0 - 1);
         mu_of(x0);
         __syncthreads();

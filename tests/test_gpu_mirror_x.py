@@ -93,12 +93,13 @@ def test_mirror_x_driver_and_errors(cuda_lib):
     assert st.pad(u).shape == (1, 2 * shape[0]) + shape[1:]
     assert torch.equal(st.pad(u)[:, shape[0]:], -torch.flip(u, [1]))
     assert tuple(prob.k_squared().shape) == (2 * shape[0], shape[1], shape[2] // 2 + 1)
-    # gradients of the mirrored step are not built: a clear error, not a silent periodic run
+    # parameter gradients of the mirrored step are not built: a clear error, not a silent periodic run
     plan = get_plan(prob.vg, bc=prob.bc)
     lam = torch.zeros_like(u)
-    with pytest.raises(NotImplementedError):
+    grads = torch.zeros(3, dtype=torch.float64, device=DEV)
+    with pytest.raises(NotImplementedError, match="dL/du only"):
         _lib.check(cuda_lib.evx_ch_adjoint(plan.handle, torch.cat([u, u]).data_ptr(), 1, lam.data_ptr(),
-                                           torch.empty_like(lam).data_ptr(), prob.evx_params(0.1), None,
+                                           torch.empty_like(lam).data_ptr(), prob.evx_params(0.1), grads.data_ptr(),
                                            plan.workspace.data_ptr(), 0), "adjoint")
 
 
