@@ -42,8 +42,7 @@ class CahnHilliardAdjoint:
 
     ``bc``: the problem's boundary conditions; a Neumann or Dirichlet x axis
     selects the mirrored-x step (y and z periodic, as the reference's FFT
-    steppers require), whose adjoint gives ``dL/dc0`` only (parameter
-    gradients raise ``NotImplementedError``).
+    steppers require); its parameter gradients use the real-space sums.
     """
 
     def __init__(self, vg: VoxelGridGB300, dt=0.1, A=0.25, pinned_w=None, spectral=True, bc=None):

@@ -308,9 +308,8 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
     if ((reinterpret_cast<uintptr_t>(lam_in) | reinterpret_cast<uintptr_t>(lam_out)) & 15)
         return fail(EVX_ERR_BAD_ARG, "lam_in and lam_out must be 16-byte aligned");
     if (nsteps < 0) return fail(EVX_ERR_BAD_ARG, "nsteps must be >= 0");
-    if (plan->xext && (grads || spectra))
-        return fail(EVX_ERR_UNSUPPORTED,
-                    "the mirrored-x (Neumann/Dirichlet x) adjoint gives dL/du only: pass no gradients or spectra");
+    if (plan->xext && spectra)
+        return fail(EVX_ERR_UNSUPPORTED, "stored increment spectra need a periodic x-pass plan");
     if (prm->bulk != EVX_BULK_DOUBLE_WELL)
         return fail(EVX_ERR_UNSUPPORTED, "the adjoint is built for the double-well bulk term w*c(1-c)(1-2c)");
     const bool want = grads != nullptr;
@@ -328,7 +327,7 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
                        key_f(prm->A), key_f(prm->sym_coef), key_f(prm->dt), (uint64_t)prm->bulk};
     return plan->graphs.run(key, as_stream(stream), [&](cudaStream_t st) -> int {
     int rc;
-    if ((rc = ch_plan_bind(plan, workspace, st, want && !spectral))) return rc;
+    if ((rc = ch_plan_bind(plan, workspace, st, want && !spectral && !plan->xext))) return rc;
     const evx_grid* g = &plan->g;
     const Geo G = make_geo(g, nullptr);
     const ChP P = make_chp(prm);
@@ -348,17 +347,53 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
     int* counter = reinterpret_cast<int*>(part + plan->n_part * 4);
     if (spectral && (rc = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), st), "reduction counter"))) return rc;
     const float* lam = lam_in;
-    if (plan->xext) {   // mirrored x: g = P lam' by the (symmetric) forward operator, generic pullback with ghosts
+    if (plan->xext) {   // mirrored x: generic pullback with ghosts
         const Geo Gb = make_geo(g, &plan->bc);
         float* gout = reinterpret_cast<float*>(ws_at(workspace, plan->off_upd));
+        const float invNe = (float)(1.0 / ((double)plan->nxe * g->ny * g->nz));
         for (int s = nsteps - 1; s >= 0; --s) {
             float* dst = (s % 2 == 0) ? lam_out : lbuf;
-            if ((rc = ch_apply_spectral(plan, lam, gbuf, gout, spec, P, st))) return rc;
-            EVX_TIMED("ch_pullback", st,
-                      ch_pullback_kernel<false><<<sg, dim3(32, 8), 0, st>>>(states + (size_t)s * N, gout, lam, nullptr,
-                                                                             nullptr, dst, nullptr, Gb, P, lx));
+            const float* us = states + (size_t)s * N;
+            if (!want) {   // g = P lam' by the (symmetric) forward operator
+                if ((rc = ch_apply_spectral(plan, lam, gbuf, gout, spec, P, st))) return rc;
+                EVX_TIMED("ch_pullback", st,
+                          ch_pullback_kernel<false><<<sg, dim3(32, 8), 0, st>>>(us, gout, lam, nullptr, nullptr, dst,
+                                                                                 nullptr, Gb, P, lx));
+                count_launch();
+                if ((rc = check_launch("ch_pullback_kernel"))) return rc;
+                lam = dst;
+                continue;
+            }
+            // g = P lam' and h = K lam' (K: prefac*k^4/N), both symmetric on the extended grid as well
+            float* hout = gbuf;   // the extension scratch is consumed by the R2C before h is written
+            if (plan->xmode) {
+                if ((rc = ch_r2c(plan, lam, spec, st))) return rc;
+                XpassArgs a = xpass_args(plan, 2, spec, P);
+                a.spec_h = spec_h;
+                if ((rc = xpass_launch(a, st))) return rc;
+            } else {
+                if ((rc = check_cuda(cudaMemcpyAsync(gbuf, lam, N * sizeof(float), cudaMemcpyDeviceToDevice, st),
+                                     "mirror extension copy")))
+                    return rc;
+                if ((rc = ch_mirror_x(plan, gbuf, st))) return rc;
+                if ((rc = ch_r2c(plan, gbuf, spec, st))) return rc;
+                EVX_TIMED("ch_kspace_adj", st, ch_kspace_adj_kernel<<<elementwise_grid(plan->nspec), 256, 0, st>>>(
+                    spec, spec_h, g->ny, plan->nzh, plan->nspec, plan->kx2, plan->ky2, plan->kz2, P.sym_coef, P.dt,
+                    invNe));
+                count_launch();
+                if ((rc = check_launch("ch_kspace_adj_kernel"))) return rc;
+            }
+            if ((rc = ch_c2r(plan, spec, gout, false, st))) return rc;
+            if ((rc = ch_c2r(plan, spec_h, hout, false, st))) return rc;
+            EVX_TIMED("ch_pullback_grads", st,
+                      ch_pullback_kernel<true><<<sg, dim3(32, 8), 0, st>>>(us, gout, lam, hout, us + N, dst, part, Gb,
+                                                                            P, lx));
             count_launch();
             if ((rc = check_launch("ch_pullback_kernel"))) return rc;
+            EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_kernel<<<1, 256, 0, st>>>(
+                part, (int)(sg.x * sg.y * sg.z), grads, kA, DA));
+            count_launch();
+            if ((rc = check_launch("ch_grad_reduce_kernel"))) return rc;
             lam = dst;
         }
         return EVX_OK;

@@ -350,6 +350,14 @@ int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_
     return check_launch("ch_kspace_fwd_kernel");
 }
 
+// The x mirror extension of a field of nx planes held in a buffer of 2*nx planes (in place).
+int ch_mirror_x(const evx_ch_plan* plan, float* buf, cudaStream_t st) {
+    EVX_TIMED("ch_mirror_x", st, ch_mirror_x_kernel<<<elementwise_grid(plan->n), 256, 0, st>>>(
+        buf, plan->g.nx, (size_t)plan->g.ny * plan->g.nz, plan->xext == 2 ? -1.f : 1.f));
+    count_launch();
+    return check_launch("ch_mirror_x_kernel");
+}
+
 // out = P in, the step's spectral operator irfft . diag(prefac/N) . rfft with the x mirror
 // extension of a non-periodic x axis (evoxels/timesteppers.py:85-89, boundary_conditions.py:64-70).
 // P is symmetric (prefac depends on k^2 only, and the extension, the multiply and the restriction
@@ -364,10 +372,7 @@ int ch_apply_spectral(evx_ch_plan* plan, const float* in, float* ext, float* out
         if ((rc = check_cuda(cudaMemcpyAsync(ext, in, N * sizeof(float), cudaMemcpyDeviceToDevice, st),
                              "mirror extension copy")))
             return rc;
-        EVX_TIMED("ch_mirror_x", st, ch_mirror_x_kernel<<<elementwise_grid(N), 256, 0, st>>>(
-            ext, plan->g.nx, (size_t)plan->g.ny * plan->g.nz, plan->xext == 2 ? -1.f : 1.f));
-        count_launch();
-        if ((rc = check_launch("ch_mirror_x_kernel"))) return rc;
+        if ((rc = ch_mirror_x(plan, ext, st))) return rc;
         src = ext;
     }
     if ((rc = ch_r2c(plan, src, spec, st))) return rc;

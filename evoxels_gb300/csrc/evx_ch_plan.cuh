@@ -69,6 +69,8 @@ __device__ __forceinline__ float imex_prefac(float k2, float sym_coef, float dt)
 // Forward k-space multiply: spec *= prefac(k) then * invN (in that order);
 // with dspec (x-pass plans only) the product is also stored there.
 int ch_kspace_forward(evx_ch_plan* plan, float2* spec, const ChP& P, cudaStream_t st, float2* dspec = nullptr);
+// The x mirror extension (even / odd by the plan's x BC) of nx planes into 2*nx planes, in place.
+int ch_mirror_x(const evx_ch_plan* plan, float* buf, cudaStream_t st);
 // out = P in, the step's (symmetric) spectral operator, x mirror extension included; ext: 2*n
 // floats of scratch and out 2*n floats on a cuFFT 3-D mirror plan, out n floats otherwise.
 int ch_apply_spectral(evx_ch_plan* plan, const float* in, float* ext, float* out, float2* spec, const ChP& P,

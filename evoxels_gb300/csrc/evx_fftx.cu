@@ -487,9 +487,12 @@ int xpass_launch_m(const XpassArgs& A, cudaStream_t st) {
 
 template <int N1, int N2>
 int xpass_launch_t(const XpassArgs& A, cudaStream_t st) {
-    if (A.ext) {   // mirrored-x forward step: per-tile kernel (odd or even extension)
-        if ((A.mode != 0 && A.mode != 4) || A.dspec)
-            return fail(EVX_ERR_UNSUPPORTED, "mirrored-x x-pass: forward only");
+    if (A.ext) {   // mirrored-x step: per-tile kernel (odd or even extension)
+        if ((A.mode != 0 && A.mode != 2 && A.mode != 4) || A.dspec)
+            return fail(EVX_ERR_UNSUPPORTED, "mirrored-x x-pass: modes 0, 2 and 4 without stored spectra");
+        if (A.mode == 2)   // adjoint g and h (parameter gradients of the mirrored step)
+            return A.ext == 2 ? xpass_launch_tile<N1, N2, 2, 2>(A, st, "ch_xpass_adj_mirror")
+                              : xpass_launch_tile<N1, N2, 2, 1>(A, st, "ch_xpass_adj_mirror");
         if (A.mode == 4)
             return A.ext == 2 ? xpass_launch_tile<N1, N2, 4, 2>(A, st, "xpass_mult_mirror")
                               : xpass_launch_tile<N1, N2, 4, 1>(A, st, "xpass_mult_mirror");

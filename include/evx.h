@@ -255,9 +255,10 @@ int evx_ch_forward(evx_ch_plan* plan, const float* u_in, float* u_out, int nstep
  * grads (optional device double[3]) accumulates dL/dD, dL/dkappa, dL/dw
  * (kappa, w as in evx_ch_params; needs a plan made with flags bit 0).
  * lam_in is read only; lam_in and lam_out must be 16-byte aligned (they feed
- * cuFFT R2C).  On a plan of evx_ch_plan_create_bc with a Neumann or Dirichlet
- * x axis (the mirrored-x step, evoxels/boundary_conditions.py:64-70) the
- * adjoint gives dL/du_0 only: grads must be NULL. */
+ * cuFFT R2C).  A plan of evx_ch_plan_create_bc with a Neumann or Dirichlet
+ * x axis (the mirrored-x step, evoxels/boundary_conditions.py:64-70) gives the
+ * adjoint of that step; its grads need no flags bit 0, and it keeps no stored
+ * spectra (evx_ch_adjoint_spectra with spectra = NULL). */
 int evx_ch_adjoint(evx_ch_plan* plan, const float* states, int nsteps,
                    const float* lam_in, float* lam_out, const evx_ch_params* p,
                    double* grads, void* workspace, void* stream);

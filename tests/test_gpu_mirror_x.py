@@ -93,25 +93,31 @@ def test_mirror_x_driver_and_errors(cuda_lib):
     assert st.pad(u).shape == (1, 2 * shape[0]) + shape[1:]
     assert torch.equal(st.pad(u)[:, shape[0]:], -torch.flip(u, [1]))
     assert tuple(prob.k_squared().shape) == (2 * shape[0], shape[1], shape[2] // 2 + 1)
-    # parameter gradients of the mirrored step are not built: a clear error, not a silent periodic run
+    # stored increment spectra are a periodic x-pass feature: a clear error on the mirrored step
     plan = get_plan(prob.vg, bc=prob.bc)
     lam = torch.zeros_like(u)
-    grads = torch.zeros(3, dtype=torch.float64, device=DEV)
-    with pytest.raises(NotImplementedError, match="dL/du only"):
-        _lib.check(cuda_lib.evx_ch_adjoint(plan.handle, torch.cat([u, u]).data_ptr(), 1, lam.data_ptr(),
-                                           torch.empty_like(lam).data_ptr(), prob.evx_params(0.1), grads.data_ptr(),
-                                           plan.workspace.data_ptr(), 0), "adjoint")
+    spec = torch.zeros(4096, dtype=torch.float32, device=DEV)
+    with pytest.raises(NotImplementedError, match="periodic x-pass"):
+        _lib.check(cuda_lib.evx_ch_adjoint_spectra(plan.handle, torch.cat([u, u]).data_ptr(), spec.data_ptr(), 1,
+                                                   lam.data_ptr(), torch.empty_like(lam).data_ptr(),
+                                                   prob.evx_params(0.1), None, plan.workspace.data_ptr(), 0),
+                   "adjoint")
 
 
 def _fp64_mirror_vjp(u0, lam, n, eps, D, bc, dt=0.1):
-    """dL/du_0 of <lam, u_n> through n FP64 oracle steps of the mirrored-x scheme (torch autograd)."""
+    """dL/du_0, dL/dD and dL/deps of <lam, u_n> through n FP64 oracle steps of the mirrored-x scheme
+    (torch autograd; eps also sets the default bulk term 18/eps)."""
     u = torch.tensor(u0).unsqueeze(0).requires_grad_(True)
-    prefac = oracle.imex_prefac(tuple(u0.shape), dt, eps, D, 0.25, (1.0, 1.0, 1.0), torch.float64, bc)
+    Dt = torch.tensor(float(D), dtype=torch.float64, requires_grad=True)
+    et = torch.tensor(float(eps), dtype=torch.float64, requires_grad=True)
+    k2 = oracle.rfft_k_squared_nonperiodic(tuple(u0.shape), (1.0, 1.0, 1.0), torch.float64)
+    prefac = dt / (1 - dt * (-2 * et * Dt * 0.25 * k2 ** 2))
+    mh = lambda c, lib=None: 18 / et * c * (1 - c) * (1 - 2 * c)  # noqa: E731
     v = u
     for _ in range(n):
-        v = oracle.imex_step(v, prefac, lambda w: oracle.ch_rhs(w, eps, D, bc), bc)
-    (g,) = torch.autograd.grad(v, u, grad_outputs=torch.tensor(lam).unsqueeze(0))
-    return g[0].numpy()
+        v = oracle.imex_step(v, prefac, lambda w: oracle.ch_rhs(w, et, Dt, bc, (1.0, 1.0, 1.0), mh), bc)
+    g, gD, ge = torch.autograd.grad(v, (u, Dt, et), grad_outputs=torch.tensor(lam).unsqueeze(0))
+    return g[0].numpy(), float(gD), float(ge)
 
 
 # x-pass with the extension inside (power-of-two nx) and cuFFT 3-D on 2*nx; some voxels outside [0, 1]
@@ -120,8 +126,8 @@ def _fp64_mirror_vjp(u0, lam, n, eps, D, bc, dt=0.1):
 def test_mirror_x_adjoint_vs_fp64_autograd(cuda_lib, shape, b):
     """The adjoint of the mirrored-x step (Neumann, homogeneous and inhomogeneous Dirichlet x) over three
     steps of the GPU trajectory against torch autograd through the FP64 oracle's mirrored steps from the
-    same float64 field: within 1e-4 relative to max (the periodic adjoint's bar); parameter gradients
-    are refused on this path."""
+    same float64 field: dL/du_0 within 1e-4 relative to max (the periodic adjoint's bar), dL/dD and
+    dL/deps within 1e-3 (the real-space sums difference float32 states)."""
     from evoxels_gb300 import _lib
     from evoxels_gb300.adjoint import CahnHilliardAdjoint
     bc = BCS[b]
@@ -135,10 +141,15 @@ def test_mirror_x_adjoint_vs_fp64_autograd(cuda_lib, shape, b):
     traj[0] = gpu(u0)[0]
     r.forward(traj[0:1], n, D, eps, traj=traj[1:])
     got = r.adjoint(traj, n, gpu(lam), D, eps, None).cpu().numpy()[0]
-    ref = _fp64_mirror_vjp(u0, lam, n, eps, D, bc)
+    ref, rD, re = _fp64_mirror_vjp(u0, lam, n, eps, D, bc)
     assert oracle.rel_to_max(got, ref) < 1e-4, oracle.rel_to_max(got, ref)
-    with pytest.raises(NotImplementedError, match="dL/du only"):
-        r.adjoint(traj, n, gpu(lam), D, eps, torch.zeros(3, dtype=torch.float64, device=DEV))
+    grads = torch.zeros(3, dtype=torch.float64, device=DEV)
+    got2 = r.adjoint(traj, n, gpu(lam), D, eps, grads).cpu().numpy()[0]
+    # g comes from the g-and-h multiply on this path: the same dL/du up to rounding
+    assert oracle.rel_to_max(got2, got) < 1e-6
+    gD, ge = r.param_grads(grads, eps)
+    assert abs(gD - rD) <= 1e-3 * abs(rD), (gD, rD)
+    assert abs(ge - re) <= 1e-3 * abs(re), (ge, re)
 
 
 class _nowarn:
