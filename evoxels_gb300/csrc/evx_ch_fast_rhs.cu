@@ -18,6 +18,7 @@
 // x-chunk) and the batched kernel (persistent blocks pulling instance x tile x
 // x-chunk work items from a global counter).
 #include "evx_ch_fast.cuh"
+#include "evx_graph.cuh"
 
 namespace evx {
 namespace {
@@ -392,6 +393,7 @@ int batch_rhs_launch(bool fused, const float* u, const float* upd, float* u_new,
 
 extern "C" int evx_set_tile_variant(int variant) {
     if (variant < -1 || variant > 1) return evx::fail(EVX_ERR_BAD_ARG, "tile variant must be -1, 0 or 1");
+    if (evx::g_tile_override != variant) evx::bump_config_epoch();
     evx::g_tile_override = variant;
     return EVX_OK;
 }

@@ -11,7 +11,8 @@
 //   - launches that graph for every later call with the key.
 // A call that cannot be captured (a capture error, a failed instantiation)
 // runs eagerly from then on.  Calls made while the caller's stream is itself
-// being captured, or while kernel timing is on, always run eagerly.  The
+// being captured, or while kernel timing is on, always run eagerly.  A change
+// of kernel choice (the stencil tile shape) drops every cached graph.  The
 // graphs hold the same kernels with the same arguments as the eager path, so
 // results are bit-identical.  The launch counter counts a replayed graph's
 // kernels once per replay.
@@ -29,6 +30,8 @@ namespace evx {
 bool graphs_enabled();                       // evx_set_graphs; off while kernel timing is on
 unsigned long long launch_counter();
 void uncount_launch(unsigned long long n);   // undo the counts of a capture (nothing ran)
+unsigned long long config_epoch();           // bumped by every change of kernel choice
+void bump_config_epoch();
 
 using GraphKey = std::vector<uint64_t>;
 
@@ -65,6 +68,13 @@ class GraphCache {
         }
         if (cs != cudaStreamCaptureStatusNone) return body(st);
         std::lock_guard<std::mutex> lk(mu_);
+        const unsigned long long ep = config_epoch();
+        if (ep != epoch_) {
+            for (auto& x : ents_)
+                if (x.exec) cudaGraphExecDestroy(x.exec);
+            ents_.clear();
+            epoch_ = ep;
+        }
         ++tick_;
         Ent* e = find(key);
         if (!e) {   // first sighting
@@ -148,6 +158,7 @@ class GraphCache {
 
     std::mutex mu_;
     std::vector<Ent> ents_;
+    unsigned long long epoch_ = 0;
     cudaStream_t cap_ = nullptr;
     unsigned long long tick_ = 0;
 };

@@ -85,7 +85,11 @@ void uncount_launch(unsigned long long n) { g_launches.fetch_sub(n, std::memory_
 namespace {
 // -1: not yet read from the environment (EVX_GRAPHS=0 turns graph replay off)
 std::atomic<int> g_graphs{-1};
+std::atomic<unsigned long long> g_config_epoch{0};
 }  // namespace
+
+unsigned long long config_epoch() { return g_config_epoch.load(std::memory_order_relaxed); }
+void bump_config_epoch() { g_config_epoch.fetch_add(1, std::memory_order_relaxed); }
 
 bool graphs_enabled() {
     int v = g_graphs.load(std::memory_order_relaxed);

@@ -325,7 +325,8 @@ int evx_set_wait_polls(int polls);
 
 /* Tile shape of the periodic fast-path stencil kernels (single grids):
  * -1 automatic (32x32 when nz is a multiple of 32 but not of 64, else 16x64),
- * 0 = 16x64, 1 = 32x32.  Results are bit-identical for every choice. */
+ * 0 = 16x64, 1 = 32x32.  Results are bit-identical for every choice.  A
+ * change drops the plans' captured step graphs. */
 int evx_set_tile_variant(int variant);
 
 /* ---- batched uneven instances ---------------------------------------------
