@@ -322,6 +322,19 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     const int polls = g_wait_polls;
     float t1 = 0.f, t2 = 0.f;
     int it = 0;
+    // mode 3: a tile's stored spectrum goes into registers (N1 <= 16) as soon as the previous tile's
+    // multiplier stage has consumed its own, so the loads are in flight through that tile's inverse
+    // stage, its store and this tile's first stage; N1 = 32 prefetches into L1 instead
+    constexpr bool PRE = MODE == 3 && N1 <= 16;
+    float2 dpre[PRE ? N1 : 1];
+    auto load_pre = [&](int t) {
+        const float2* dp = dspec + (size_t)t * N1 * 256 + tid;
+#pragma unroll
+        for (int e = 0; e < N1; ++e) dpre[e] = __ldcs(dp + e * 256);
+    };
+    if constexpr (PRE) {
+        if ((int)blockIdx.x < ntiles) load_pre(blockIdx.x);
+    }
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int slot = it % XSTAGES;
         const int next = tile + gridDim.x;
@@ -332,16 +345,7 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
             issue_load((it + 1) % XSTAGES, next);
             if (MODE == 3) prefetch_l2(dspec + (size_t)next * N1 * 256, N1 * 256 * sizeof(float2));
         }
-        // mode 3: this tile's stored spectrum (in L2 from the previous tile's
-        // prefetch) into registers now, in flight while the tile's data arrives
-        // and its first stage runs; N1 = 32 prefetches into L1 instead
-        constexpr bool PRE = MODE == 3 && N1 <= 16;
-        float2 dpre[PRE ? N1 : 1];
-        if constexpr (PRE) {
-            const float2* dp = dspec + (size_t)tile * N1 * 256 + tid;
-#pragma unroll
-            for (int e = 0; e < N1; ++e) dpre[e] = __ldcs(dp + e * 256);
-        } else if (MODE == 3) {
+        if constexpr (MODE == 3 && !PRE) {
             const float2* dp = dspec + (size_t)tile * N1 * 256 + tid;
 #pragma unroll
             for (int e = 0; e < N1; ++e) asm volatile("prefetch.global.L1 [%0];" ::"l"(dp + e * 256));
@@ -361,6 +365,9 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         float2 hv[1];
         mid_stage<N1, N2, MODE, PRE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1,
                                      t2, mult + mc, M, &dpre);
+        if constexpr (PRE) {
+            if (next < ntiles) load_pre(next);
+        }
         inv_stage1<N1, N2>(v, xs, c);
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) xs[(N2 * n1 + c.n2) * P + c.p] = v[n1];
