@@ -70,13 +70,15 @@ __device__ int g_wait_polls = WAIT_POLLS;   // poll limit of the x-pass's tile-l
 // reads are consecutive whichever of y or z is contiguous).  dsp points at the tile's stored
 // spectrum ([element][thread], thread offset included).
 // PRE (mode 3): the stored spectrum values come preloaded in dpre[q*N2 + k2].
-template <int N1, int N2, int MODE, bool PRE = false>
+// KXR: the thread's kx^2 values come preloaded in kxr[q*N2 + k2] (they depend on the thread only).
+template <int N1, int N2, int MODE, bool PRE = false, bool KXR = false>
 __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 2 ? N1 : 1], float2* xs,
                                           const Col<N1, N2>& c, float ky2v, float kz2v, float wz,
                                           const float* __restrict__ kx2, float sym_coef, float dt, float invN,
                                           float2* __restrict__ dsp, float& t1, float& t2,
                                           const float* __restrict__ mrow = nullptr, int M = 0,
-                                          const float2 (*dpre)[PRE ? N1 : 1] = nullptr) {
+                                          const float2 (*dpre)[PRE ? N1 : 1] = nullptr,
+                                          const float (*kxr)[KXR ? N1 : 1] = nullptr) {
     constexpr int N = N1 * N2, Q = N1 / N2;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -88,7 +90,8 @@ __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) {
             const int kx = k1 + N1 * k2;
-            const float k2s = __fadd_rn(__fadd_rn(__ldg(kx2 + kx), ky2v), kz2v);
+            const float kx2v = KXR ? (*kxr)[KXR ? q * N2 + k2 : 0] : __ldg(kx2 + kx);
+            const float k2s = __fadd_rn(__fadd_rn(kx2v, ky2v), kz2v);
             if constexpr (MODE == 4) {
                 const float mv = __ldg(mrow + (size_t)kx * M);
                 a[k2] = make_float2(__fmul_rn(__fmul_rn(a[k2].x, mv), invN), __fmul_rn(__fmul_rn(a[k2].y, mv), invN));
@@ -335,6 +338,16 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     if constexpr (PRE) {
         if ((int)blockIdx.x < ntiles) load_pre(blockIdx.x);
     }
+    // the thread's kx^2 values, the same for every tile (modes 0, 1 and 4: registers to spare)
+    constexpr bool KXR = MODE == 0 || MODE == 1 || MODE == 4;
+    float kxr[KXR ? N1 : 1];
+    if constexpr (KXR) {
+        constexpr int Q = N1 / N2;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) kxr[q * N2 + k2] = __ldg(kx2 + (N2 > 1 ? c.n2 * Q + q : q) + N1 * k2);
+    }
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int slot = it % XSTAGES;
         const int next = tile + gridDim.x;
@@ -363,8 +376,8 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         for (int n1 = 0; n1 < N1; ++n1) v[n1] = xs[(N2 * n1 + c.n2) * P + c.p];
         fwd_stage1<N1, N2>(v, xs, c);
         float2 hv[1];
-        mid_stage<N1, N2, MODE, PRE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1,
-                                     t2, mult + mc, M, &dpre);
+        mid_stage<N1, N2, MODE, PRE, KXR>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp,
+                                          t1, t2, mult + mc, M, &dpre, &kxr);
         if constexpr (PRE) {
             if (next < ntiles) load_pre(next);
         }
