@@ -70,15 +70,16 @@ __device__ int g_wait_polls = WAIT_POLLS;   // poll limit of the x-pass's tile-l
 // reads are consecutive whichever of y or z is contiguous).  dsp points at the tile's stored
 // spectrum ([element][thread], thread offset included).
 // PRE (mode 3): the stored spectrum values come preloaded in dpre[q*N2 + k2].
-// KXR: the thread's kx^2 values come preloaded in kxr[q*N2 + k2] (they depend on the thread only).
-template <int N1, int N2, int MODE, bool PRE = false, bool KXR = false>
+// KX: where kx^2 comes from - 0 the global table kx2, 1 the thread's values preloaded in
+// kxr[q*N2 + k2] (they depend on the thread only), 2 a copy of the table in shared memory (kx2).
+template <int N1, int N2, int MODE, bool PRE = false, int KX = 0>
 __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 2 ? N1 : 1], float2* xs,
                                           const Col<N1, N2>& c, float ky2v, float kz2v, float wz,
                                           const float* __restrict__ kx2, float sym_coef, float dt, float invN,
                                           float2* __restrict__ dsp, float& t1, float& t2,
                                           const float* __restrict__ mrow = nullptr, int M = 0,
                                           const float2 (*dpre)[PRE ? N1 : 1] = nullptr,
-                                          const float (*kxr)[KXR ? N1 : 1] = nullptr) {
+                                          const float (*kxr)[KX == 1 ? N1 : 1] = nullptr) {
     constexpr int N = N1 * N2, Q = N1 / N2;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -90,7 +91,10 @@ __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) {
             const int kx = k1 + N1 * k2;
-            const float kx2v = KXR ? (*kxr)[KXR ? q * N2 + k2 : 0] : __ldg(kx2 + kx);
+            float kx2v;
+            if constexpr (KX == 1) kx2v = (*kxr)[q * N2 + k2];
+            else if constexpr (KX == 2) kx2v = kx2[kx];
+            else kx2v = __ldg(kx2 + kx);
             const float k2s = __fadd_rn(__fadd_rn(kx2v, ky2v), kz2v);
             if constexpr (MODE == 4) {
                 const float mv = __ldg(mrow + (size_t)kx * M);
@@ -307,8 +311,10 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     constexpr uint32_t TILE_BYTES = TILE * sizeof(float2);
     extern __shared__ __align__(128) float2 ring[];   // [XSTAGES][TILE], each [x][p]
     __shared__ __align__(8) uint64_t bar[XSTAGES];
+    __shared__ float s_kx2[N];                        // kx^2 table (modes 2 and 3)
     const int tid = threadIdx.x;
     const C c{tid % P, tid / P, P};
+    for (int i = tid; i < N; i += 256) s_kx2[i] = __ldg(kx2 + i);   // published by the barrier below
 
     auto issue_load = [&](int slot, int tile) {
         mbar_expect_tx(&bar[slot], TILE_BYTES);
@@ -338,10 +344,11 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     if constexpr (PRE) {
         if ((int)blockIdx.x < ntiles) load_pre(blockIdx.x);
     }
-    // the thread's kx^2 values, the same for every tile (modes 0, 1 and 4: registers to spare)
-    constexpr bool KXR = MODE == 0 || MODE == 1 || MODE == 4;
-    float kxr[KXR ? N1 : 1];
-    if constexpr (KXR) {
+    // the thread's kx^2 values, the same for every tile: in registers where there are registers to
+    // spare (modes 0, 1 and 4), else read from a copy of the table in shared memory
+    constexpr int KX = (MODE == 0 || MODE == 1 || MODE == 4) ? 1 : 2;
+    float kxr[KX == 1 ? N1 : 1];
+    if constexpr (KX == 1) {
         constexpr int Q = N1 / N2;
 #pragma unroll
         for (int q = 0; q < Q; ++q)
@@ -376,8 +383,8 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         for (int n1 = 0; n1 < N1; ++n1) v[n1] = xs[(N2 * n1 + c.n2) * P + c.p];
         fwd_stage1<N1, N2>(v, xs, c);
         float2 hv[1];
-        mid_stage<N1, N2, MODE, PRE, KXR>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp,
-                                          t1, t2, mult + mc, M, &dpre, &kxr);
+        mid_stage<N1, N2, MODE, PRE, KX>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), KX == 2 ? s_kx2 : kx2, sym_coef,
+                                         dt, invN, dsp, t1, t2, mult + mc, M, &dpre, &kxr);
         if constexpr (PRE) {
             if (next < ntiles) load_pre(next);
         }
