@@ -205,6 +205,21 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
         for (int e = 0; e < N1; ++e) dpre[e] = __ldcs(dsp + e * 256);
     }
 
+    // kx^2 of the thread's frequencies (modes 0, 1 and 4 up to nx = 128: in registers, loaded with the
+    // tile) or the whole table in shared memory (where the registers are taken)
+    constexpr int KX = (MODE == 0 || MODE == 1 || MODE == 4) && N1 * N2 <= 128 ? 1 : 2;
+    float kxr[KX == 1 ? N1 : 1];
+    __shared__ float s_kx2[KX == 2 ? N1 * N2 : 1];
+    if constexpr (KX == 1) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) kxr[q * N2 + k2] = __ldg(kx2 + (N2 > 1 ? c.n2 * Q + q : q) + N1 * k2);
+    } else {
+        for (int i = tid; i < N1 * N2; i += 256) s_kx2[i] = __ldg(kx2 + i);
+        __syncthreads();
+    }
+
     constexpr int NH = (N1 * N2) / 2;   // physical rows with EXT
     float2 v[N1];
 #pragma unroll
@@ -219,8 +234,8 @@ xpass_kernel(float2* __restrict__ spec, float2* __restrict__ spec_h, float2* __r
     }
     fwd_stage1<N1, N2>(v, xs, c);
     float2 hv[MODE == 2 ? N1 : 1];
-    mid_stage<N1, N2, MODE, PRE>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), kx2, sym_coef, dt, invN, dsp, t1, t2,
-                                 mult + mc, M, &dpre);
+    mid_stage<N1, N2, MODE, PRE, KX>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), KX == 2 ? s_kx2 : kx2, sym_coef, dt,
+                                     invN, dsp, t1, t2, mult + mc, M, &dpre, &kxr);
     auto store = [&](float2* dst) {
         if (live) {
 #pragma unroll
