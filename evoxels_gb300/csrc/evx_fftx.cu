@@ -346,10 +346,10 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     const int polls = g_wait_polls;
     float t1 = 0.f, t2 = 0.f;
     int it = 0;
-    // mode 3: a tile's stored spectrum goes into registers (N1 <= 16) as soon as the previous tile's
-    // multiplier stage has consumed its own, so the loads are in flight through that tile's inverse
-    // stage, its store and this tile's first stage; N1 = 32 prefetches into L1 instead
-    constexpr bool PRE = MODE == 3 && N1 <= 16;
+    // mode 3: a tile's stored spectrum goes into registers as soon as the previous tile's multiplier
+    // stage has consumed its own, so the loads are in flight through that tile's inverse stage, its
+    // store and this tile's first stage (N1 = 32: one block per SM, 236 registers)
+    constexpr bool PRE = MODE == 3;
     float2 dpre[PRE ? N1 : 1];
     auto load_pre = [&](int t) {
         const float2* dp = dspec + (size_t)t * N1 * 256 + tid;
@@ -379,11 +379,6 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
             bulk_wait_read<1>();
             issue_load((it + 1) % XSTAGES, next);
             if (MODE == 3) prefetch_l2(dspec + (size_t)next * N1 * 256, N1 * 256 * sizeof(float2));
-        }
-        if constexpr (MODE == 3 && !PRE) {
-            const float2* dp = dspec + (size_t)tile * N1 * 256 + tid;
-#pragma unroll
-            for (int e = 0; e < N1; ++e) asm volatile("prefetch.global.L1 [%0];" ::"l"(dp + e * 256));
         }
         const bool landed = mbar_wait(&bar[slot], (uint32_t)(it / XSTAGES) & 1u, polls);
         float2* xs = ring + (size_t)slot * TILE;
