@@ -56,9 +56,8 @@ __global__ void batch_kspace_fwd_kernel(float2* __restrict__ spec, const KInst* 
     float2* ds = dspec ? dspec + K.doff : nullptr;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int k = (int)(e % K.nzh);
-        const size_t t = e / K.nzh;
-        const int j = (int)(t % K.ny), i = (int)(t / K.ny);
+        int i, j, k;
+        spec_ijk(e, K.ny, K.nzh, i, j, k);
         const float kk = __fadd_rn(__fadd_rn(__ldg(k2 + K.kx + i), __ldg(k2 + K.ky + j)), __ldg(k2 + K.kz + k));
         const float pre = imex_prefac(kk, K.sym_coef, K.dt);
         float2 v = s[e];
@@ -85,9 +84,8 @@ __global__ void batch_kspace_adj_spec_kernel(float2* __restrict__ spec, const fl
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     float t1 = 0.f, t2 = 0.f;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int k = (int)(e % K.nzh);
-        const size_t t = e / K.nzh;
-        const int j = (int)(t % K.ny), i = (int)(t / K.ny);
+        int i, j, k;
+        spec_ijk(e, K.ny, K.nzh, i, j, k);
         const float kk = (__ldg(k2 + K.kx + i) + __ldg(k2 + K.ky + j)) + __ldg(k2 + K.kz + k);
         const float k4 = kk * kk;
         const float pre = K.dt / (1.f - K.dt * (K.sym_coef * k4));
@@ -125,9 +123,8 @@ __global__ void batch_kspace_adj_kernel(float2* __restrict__ spec, float2* __res
     float2* sh = spec_h ? spec_h + K.soff : nullptr;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int k = (int)(e % K.nzh);
-        const size_t t = e / K.nzh;
-        const int j = (int)(t % K.ny), i = (int)(t / K.ny);
+        int i, j, k;
+        spec_ijk(e, K.ny, K.nzh, i, j, k);
         const float kk = (__ldg(k2 + K.kx + i) + __ldg(k2 + K.ky + j)) + __ldg(k2 + K.kz + k);
         const float k4 = kk * kk;
         const float sg = (K.dt / (1.f - K.dt * (K.sym_coef * k4))) * K.invN;

@@ -223,10 +223,8 @@ __global__ void ch_kspace_fwd_kernel(float2* __restrict__ spec, int ny, int nzh,
                                      const float* __restrict__ kz2, float sym_coef, float dt, float invN) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int k = (int)(e % nzh);
-        const size_t t = e / nzh;
-        const int j = (int)(t % ny);
-        const int i = (int)(t / ny);
+        int i, j, k;
+        spec_ijk(e, ny, nzh, i, j, k);
         const float k2 = __fadd_rn(__fadd_rn(__ldg(kx2 + i), __ldg(ky2 + j)), __ldg(kz2 + k));
         const float k4 = __fmul_rn(k2, k2);
         const float den = __fsub_rn(1.f, __fmul_rn(dt, __fmul_rn(sym_coef, k4)));

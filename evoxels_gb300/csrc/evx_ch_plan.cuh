@@ -58,6 +58,22 @@ int ch_plan_bind(evx_ch_plan* plan, void* workspace, cudaStream_t st, bool need_
 int ch_r2c(evx_ch_plan* plan, const float* in, float2* out, cudaStream_t st);
 int ch_c2r(evx_ch_plan* plan, float2* in, float* out, bool batch2, cudaStream_t st);
 
+// (i, j, k) of element e of an [nx][ny][nzh] spectrum: 32-bit divisions while e fits in 32 bits
+// (every half spectrum up to 1024^3), 64-bit beyond.
+__device__ __forceinline__ void spec_ijk(size_t e, int ny, int nzh, int& i, int& j, int& k) {
+    if (e < (size_t(1) << 32)) {
+        const unsigned u = (unsigned)e, t = u / (unsigned)nzh, ii = t / (unsigned)ny;
+        k = (int)(u - t * (unsigned)nzh);
+        j = (int)(t - ii * (unsigned)ny);
+        i = (int)ii;
+    } else {
+        const size_t t = e / (size_t)nzh;
+        k = (int)(e - t * (size_t)nzh);
+        j = (int)(t % (size_t)ny);
+        i = (int)(t / (size_t)ny);
+    }
+}
+
 // IMEX prefactor dt * (1/(1 - dt*(sym_coef*k4))) with k4 = (k^2)^2, in the
 // reference's float32 operation order (evoxels/timesteppers.py:77).
 __device__ __forceinline__ float imex_prefac(float k2, float sym_coef, float dt) {
