@@ -198,24 +198,37 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
     };
 
     float2 fxm[2] = {f2s(0.f), f2s(0.f)};   // x flux on the face below the current plane (rows a, b)
+    // c and mu of the current plane at the patch points (rows a, b), carried from the x faces of the
+    // plane below, where they were the upper side
+    float2 cA, cB, mA, mB;
     auto x_faces = [&](int plo, float2 out[2]) {
         const float* c0 = cs + cslot(plo) * T::FIELD;
         const float* c1 = cs + cslot(plo + 1) * T::FIELD;
         const float* m0 = ms + mslot(plo) * T::POT;
         const float* m1 = ms + mslot(plo + 1) * T::POT;
         const int a = ra * W + rc, b = a + W;
-        out[0] = M::template flux<0>(K, lds2(c0 + a), lds2(c1 + a), lds2(m0 + a - W), lds2(m1 + a - W));
-        out[1] = M::template flux<0>(K, lds2(c0 + b), lds2(c1 + b), lds2(m0 + b - W), lds2(m1 + b - W));
+        cA = lds2(c1 + a);
+        cB = lds2(c1 + b);
+        mA = lds2(m1 + a - W);
+        mB = lds2(m1 + b - W);
+        out[0] = M::template flux<0>(K, lds2(c0 + a), cA, lds2(m0 + a - W), mA);
+        out[1] = M::template flux<0>(K, lds2(c0 + b), cB, lds2(m0 + b - W), mB);
     };
 
     auto compute_r = [&](int i) {
         const float* cc = cs + cslot(i) * T::FIELD;
         const float* mm = ms + mslot(i) * T::POT;
+        const float* cx = cs + cslot(i + 1) * T::FIELD;
+        const float* mx = ms + mslot(i + 1) * T::POT;
         const int a = ra * W + rc, b = a + W;     // field offsets; potential offsets are one row up
-        float2 fxp[2];
-        x_faces(i, fxp);
-        const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
-        const float2 mup = lds2(mm + a - 2 * W), MA = lds2(mm + a - W), MB = lds2(mm + b - W), mdn = lds2(mm + b);
+        const float2 A = cA, B = cB, MA = mA, MB = mB;
+        cA = lds2(cx + a);
+        cB = lds2(cx + b);
+        mA = lds2(mx + a - W);
+        mB = lds2(mx + b - W);
+        const float2 fxp[2] = {M::template flux<0>(K, A, cA, MA, mA), M::template flux<0>(K, B, cB, MB, mB)};
+        const float2 up = lds2(cc + a - W), dn = lds2(cc + b + W);
+        const float2 mup = lds2(mm + a - 2 * W), mdn = lds2(mm + b);
         // z faces (left, mid) and (mid, right) of each row
         const float2 zlA = M::template flux<2>(K, make_float2(cc[a - 1], A.x), A, make_float2(mm[a - W - 1], MA.x), MA);
         const float2 zhA = M::template flux<2>(K, A, make_float2(A.y, cc[a + 2]), MA, make_float2(MA.y, mm[a - W + 2]));
