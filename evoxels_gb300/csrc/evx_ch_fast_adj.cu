@@ -286,12 +286,20 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
 
     // x face cbar'' of the output patch between planes (c0, g0, m0) and (c1, g1, m1)
     float2 cfx_m[2], b_prev[2];
-    auto x_faces_b = [&](const float* c0, const float* c1, const float* g0, const float* g1, const float* m0,
-                         const float* m1, float2 out[2]) {
-        out[0] = cfb2<0>(K, lds2(c0 + pa), lds2(c1 + pa), lds2(m0 + pa - W), lds2(m1 + pa - W), lds2(g0 + pa),
-                         lds2(g1 + pa));
-        out[1] = cfb2<0>(K, lds2(c0 + pb), lds2(c1 + pb), lds2(m0 + pb - W), lds2(m1 + pb - W), lds2(g0 + pb),
-                         lds2(g1 + pb));
+    // c, mu and g of the current output plane at the patch points (rows a, b), carried from the x faces
+    // of the plane below, where they were the upper side
+    float2 xc[2], xm[2], xg[2];
+    auto x_faces_b = [&](const float* c1, const float* g1, const float* m1, float2 out[2]) {
+        const float2 c1a = lds2(c1 + pa), c1b = lds2(c1 + pb), m1a = lds2(m1 + pa - W), m1b = lds2(m1 + pb - W);
+        const float2 g1a = lds2(g1 + pa), g1b = lds2(g1 + pb);
+        out[0] = cfb2<0>(K, xc[0], c1a, xm[0], m1a, xg[0], g1a);
+        out[1] = cfb2<0>(K, xc[1], c1b, xm[1], m1b, xg[1], g1b);
+        xc[0] = c1a;
+        xc[1] = c1b;
+        xm[0] = m1a;
+        xm[1] = m1b;
+        xg[0] = g1a;
+        xg[1] = g1b;
     };
 
     // lam on plane i: field slots cc (i), cx (i+1), g slots gc (i), gx (i+1), potential slots mm / bb (i)
@@ -300,19 +308,18 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
                            const float* mm, const float* mx, const float* bb, const float* bx) {
         // acc: sum of the cbar'' face values around each point
         float2 accA, accB;
+        const float2 A = xc[0], B = xc[1], MA = xm[0], MB = xm[1], gA = xg[0], gB = xg[1];
         {
             float2 cfx_p[2];
-            x_faces_b(cc, cx, gc, gx, mm, mx, cfx_p);
+            x_faces_b(cx, gx, mx, cfx_p);
             accA = add2(cfx_m[0], cfx_p[0]);
             accB = add2(cfx_m[1], cfx_p[1]);
             cfx_m[0] = cfx_p[0];
             cfx_m[1] = cfx_p[1];
         }
-        const float2 up = lds2(cc + pa - W), A = lds2(cc + pa), B = lds2(cc + pb), dn = lds2(cc + pb + W);
+        const float2 up = lds2(cc + pa - W), dn = lds2(cc + pb + W);
         const float2 zmA = make_float2(cc[pa - 1], A.x), zpA = make_float2(A.y, cc[pa + 2]);
         const float2 zmB = make_float2(cc[pb - 1], B.x), zpB = make_float2(B.y, cc[pb + 2]);
-        const float2 MA = lds2(mm + pa - W), MB = lds2(mm + pb - W);
-        const float2 gA = lds2(gc + pa), gB = lds2(gc + pb);
         {   // z faces
             const float2 mzmA = make_float2(mm[pa - W - 1], MA.x), mzpA = make_float2(MA.y, mm[pa - W + 2]);
             const float2 mzmB = make_float2(mm[pb - W - 1], MB.x), mzpB = make_float2(MB.y, mm[pb - W + 2]);
@@ -426,7 +433,13 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     }
     {
         const int s0 = cslt(x0 - 1), s1 = cslt(x0), t0 = mslt(x0 - 1), t1 = mslt(x0);
-        x_faces_b(cf(s0), cf(s1), gf(s0), gf(s1), mp(t0), mp(t1), cfx_m);
+        xc[0] = lds2(cf(s0) + pa);
+        xc[1] = lds2(cf(s0) + pb);
+        xm[0] = lds2(mp(t0) + pa - W);
+        xm[1] = lds2(mp(t0) + pb - W);
+        xg[0] = lds2(gf(s0) + pa);
+        xg[1] = lds2(gf(s0) + pb);
+        x_faces_b(cf(s1), gf(s1), mp(t1), cfx_m);
         b_prev[0] = lds2(bp(t0) + pa - W);
         b_prev[1] = lds2(bp(t0) + pb - W);
     }
@@ -468,7 +481,7 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
 }
 
 template <class T, int GR>
-__global__ void __launch_bounds__(THREADS, GR ? EVX_PULLBACK_MIN_BLOCKS : 3)
+__global__ void __launch_bounds__(THREADS, EVX_PULLBACK_MIN_BLOCKS)
 ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ gfield, const float* __restrict__ lam,
                         const float* __restrict__ hfield, const float* __restrict__ u1, float* __restrict__ lam_out,
                         double* __restrict__ part, Geo G, ChP P, int seg, GradSink sink) {
