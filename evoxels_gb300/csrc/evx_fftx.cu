@@ -326,10 +326,14 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     constexpr uint32_t TILE_BYTES = TILE * sizeof(float2);
     extern __shared__ __align__(128) float2 ring[];   // [XSTAGES][TILE], each [x][p]
     __shared__ __align__(8) uint64_t bar[XSTAGES];
-    __shared__ float s_kx2[N];                        // kx^2 table (modes 2 and 3)
+    // the thread's kx^2 values are the same for every tile: in registers where there are registers to
+    // spare (modes 0, 1 and 4), else read from a copy of the table in shared memory
+    constexpr int KX = (MODE == 0 || MODE == 1 || MODE == 4) ? 1 : 2;
+    __shared__ float s_kx2[KX == 2 ? N : 1];
     const int tid = threadIdx.x;
     const C c{tid % P, tid / P, P};
-    for (int i = tid; i < N; i += 256) s_kx2[i] = __ldg(kx2 + i);   // published by the barrier below
+    if constexpr (KX == 2)
+        for (int i = tid; i < N; i += 256) s_kx2[i] = __ldg(kx2 + i);   // published by the barrier below
 
     auto issue_load = [&](int slot, int tile) {
         mbar_expect_tx(&bar[slot], TILE_BYTES);
@@ -359,9 +363,6 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     if constexpr (PRE) {
         if ((int)blockIdx.x < ntiles) load_pre(blockIdx.x);
     }
-    // the thread's kx^2 values, the same for every tile: in registers where there are registers to
-    // spare (modes 0, 1 and 4), else read from a copy of the table in shared memory
-    constexpr int KX = (MODE == 0 || MODE == 1 || MODE == 4) ? 1 : 2;
     float kxr[KX == 1 ? N1 : 1];
     if constexpr (KX == 1) {
         constexpr int Q = N1 / N2;
