@@ -72,14 +72,17 @@ __device__ int g_wait_polls = WAIT_POLLS;   // poll limit of the x-pass's tile-l
 // PRE (mode 3): the stored spectrum values come preloaded in dpre[q*N2 + k2].
 // KX: where kx^2 comes from - 0 the global table kx2, 1 the thread's values preloaded in
 // kxr[q*N2 + k2] (they depend on the thread only), 2 a copy of the table in shared memory (kx2).
-template <int N1, int N2, int MODE, bool PRE = false, int KX = 0>
+// TW (N1 = N2 = 16 only): the inverse inter-stage twiddles are the conjugates of the thread's split
+// forward twiddles tw (W^{n2*j} = tw->at(j)) instead of reads of the constant table.
+template <int N1, int N2, int MODE, bool PRE = false, int KX = 0, bool TW = false>
 __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 2 ? N1 : 1], float2* xs,
                                           const Col<N1, N2>& c, float ky2v, float kz2v, float wz,
                                           const float* __restrict__ kx2, float sym_coef, float dt, float invN,
                                           float2* __restrict__ dsp, float& t1, float& t2,
                                           const float* __restrict__ mrow = nullptr, int M = 0,
                                           const float2 (*dpre)[PRE ? N1 : 1] = nullptr,
-                                          const float (*kxr)[KX == 1 ? N1 : 1] = nullptr) {
+                                          const float (*kxr)[KX == 1 ? N1 : 1] = nullptr,
+                                          const Tw16<false>* tw = nullptr) {
     constexpr int N = N1 * N2, Q = N1 / N2;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -124,8 +127,13 @@ __device__ __forceinline__ void mid_stage(float2 (&v)[N1], float2 (&hv)[MODE == 
             if constexpr (MODE == 2) dft<N2, true>(b);
 #pragma unroll
             for (int j = 0; j < N2; ++j) {
-                xs[c.xi(k1, j)] = cmul(a[j], w512<true>((j * k1) * (512 / N)));
-                if constexpr (MODE == 2) hv[q * N2 + j] = cmul(b[j], w512<true>((j * k1) * (512 / N)));
+                if constexpr (TW) {
+                    static_assert(N1 == 16 && N2 == 16 && MODE != 2, "split twiddles: 16 x 16 columns");
+                    xs[c.xi(k1, j)] = j ? cmul(a[j], conjf2(tw->at(j))) : a[j];
+                } else {
+                    xs[c.xi(k1, j)] = cmul(a[j], w512<true>((j * k1) * (512 / N)));
+                    if constexpr (MODE == 2) hv[q * N2 + j] = cmul(b[j], w512<true>((j * k1) * (512 / N)));
+                }
             }
         } else {
             v[q] = a[0];
@@ -363,6 +371,10 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     if constexpr (PRE) {
         if ((int)blockIdx.x < ntiles) load_pre(blockIdx.x);
     }
+    // modes 0 and 1 on 16 x 16 columns: the thread's inter-stage twiddles in registers (split form)
+    constexpr bool TW = (MODE == 0 || MODE == 1) && N1 == 16 && N2 == 16;
+    Tw16<false> tw;
+    if constexpr (TW) tw.init(c.n2);
     float kxr[KX == 1 ? N1 : 1];
     if constexpr (KX == 1) {
         constexpr int Q = N1 / N2;
@@ -392,10 +404,11 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
         float2 v[N1];
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) v[n1] = xs[(N2 * n1 + c.n2) * P + c.p];
-        fwd_stage1<N1, N2>(v, xs, c);
+        if constexpr (TW) fwd_stage1_tw16(v, xs, c, tw);
+        else fwd_stage1<N1, N2>(v, xs, c);
         float2 hv[1];
-        mid_stage<N1, N2, MODE, PRE, KX>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), KX == 2 ? s_kx2 : kx2, sym_coef,
-                                         dt, invN, dsp, t1, t2, mult + mc, M, &dpre, &kxr);
+        mid_stage<N1, N2, MODE, PRE, KX, TW>(v, hv, xs, c, ky2v, kz2v, kz_weight(kz, nz), KX == 2 ? s_kx2 : kx2,
+                                             sym_coef, dt, invN, dsp, t1, t2, mult + mc, M, &dpre, &kxr, &tw);
         if constexpr (PRE) {
             if (next < ntiles) load_pre(next);
         }
