@@ -371,8 +371,8 @@ xpass_tma_kernel(const __grid_constant__ CUtensorMap tm, float2* __restrict__ ds
     if constexpr (PRE) {
         if ((int)blockIdx.x < ntiles) load_pre(blockIdx.x);
     }
-    // modes 0 and 1 on 16 x 16 columns: the thread's inter-stage twiddles in registers (split form)
-    constexpr bool TW = (MODE == 0 || MODE == 1) && N1 == 16 && N2 == 16;
+    // 16 x 16 columns: the thread's inter-stage twiddles in registers (split form)
+    constexpr bool TW = (MODE == 0 || MODE == 1 || MODE == 3) && N1 == 16 && N2 == 16;
     Tw16<false> tw;
     if constexpr (TW) tw.init(c.n2);
     float kxr[KX == 1 ? N1 : 1];
