@@ -24,7 +24,22 @@ mse_grad_kernel(const float* __restrict__ u, const float* __restrict__ t, size_t
     // per-thread float partial sums (a few dozen terms each), double across threads
     float accf = 0.f;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+    size_t tail0 = 0;
+    // 16-byte accesses where every array allows them, the last n % 4 elements one by one
+    if (((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(t) | reinterpret_cast<uintptr_t>(lam)) & 15) == 0) {
+        const size_t n4 = n / 4;
+        for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += stride) {
+            const float4 a = __ldg(reinterpret_cast<const float4*>(u) + e), b = __ldg(reinterpret_cast<const float4*>(t) + e);
+            const float4 d = make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+            if (lam) reinterpret_cast<float4*>(lam)[e] = make_float4(scale * d.x, scale * d.y, scale * d.z, scale * d.w);
+            accf = fmaf(d.x, d.x, accf);
+            accf = fmaf(d.y, d.y, accf);
+            accf = fmaf(d.z, d.z, accf);
+            accf = fmaf(d.w, d.w, accf);
+        }
+        tail0 = n4 * 4;
+    }
+    for (size_t e = tail0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
         const float d = __ldg(u + e) - __ldg(t + e);
         if (lam) lam[e] = scale * d;
         accf = fmaf(d, d, accf);
