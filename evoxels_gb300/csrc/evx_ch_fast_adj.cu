@@ -593,7 +593,8 @@ void init_occupancy() {
 }
 
 // One wave of blocks over equal segments of the tile-major (tile, x) plane
-// sequence, at least 16 planes each (the x halo costs 6 plane loads per piece).
+// sequence, at least 8 planes each (the x halo costs 6 plane loads per piece; on small grids
+// a shorter piece that fills more of the slots still wins).
 template <class T>
 dim3 pb_grid(const evx_grid* g, int grads, int* seg) {
     const int v = std::is_same<T, TileWide>::value ? 0 : 1;
@@ -601,7 +602,7 @@ dim3 pb_grid(const evx_grid* g, int grads, int* seg) {
     const long total = tiles * g->nx;
     const long slots = (long)std::max(1, g_bps[v][grads]) * std::max(1, g_sms);
     long len = (total + slots - 1) / slots;
-    len = std::max(len, std::min<long>(16, g->nx));
+    len = std::max(len, std::min<long>(8, g->nx));
     *seg = (int)len;
     return dim3((unsigned)((total + len - 1) / len));
 }
