@@ -46,12 +46,12 @@ FALLBACK_HBM_GBS = 6800.0
 # at 512^3) of the kernels as they are now built; traffic grows in proportion to
 # the voxels a launch processes.  A kernel change needs a new capture here.
 NCU_DRAM_BYTES_PER_VOXEL = {
-    "ch_rhs_fused": (153.348096e6 + 90.268416e6) / 256 ** 3,
+    "ch_rhs_fused": (153.186048e6 + 92.427520e6) / 256 ** 3,
     "ch_pullback_grads": (344.547840e6 + 54.629120e6) / 256 ** 3,
     "fd_step": (561.215488e6 + 497.061376e6) / 512 ** 3,
     "fd_tblock2": (554.379264e6 + 495.615488e6) / 512 ** 3,
-    "ch_xpass_adj_spec": (135.309568e6 + 8.653312e6) / 256 ** 3,
-    "ch_xpass_fwd_store": (67.669760e6 + 74.822400e6) / 256 ** 3,
+    "ch_xpass_adj_spec": (135.312128e6 + 9.059584e6) / 256 ** 3,
+    "ch_xpass_fwd_store": (67.669760e6 + 74.952704e6) / 256 ** 3,
     "ch_xpass_fwd": (135.399168e6 + 74.517248e6) / (512 * 256 * 256),
     "ch_pullback_grads_spec": (309.864192e6 + 57.453056e6) / 256 ** 3,
     "ac_rhs": (68.689152e6 + 24.427008e6) / 256 ** 3,
