@@ -392,7 +392,9 @@ bool all_periodic(const Geo& G) {
 // false, which lets the periodic fast path fuse its products
 int ch_rhs_launch(bool fused, bool exact, const float* u, const float* upd, float* u_new, float* r,
                   const evx_grid* g, const Geo& G, const ChP& P, cudaStream_t st) {
-    if (all_periodic(G) && fast_ok(g, {u, upd, u_new, r}))
+    // the tile kernels: periodic grids, and (spectral loops only) a Neumann or Dirichlet x axis
+    const bool yz_periodic = G.kind[1] == EVX_BC_PERIODIC && G.kind[2] == EVX_BC_PERIODIC;
+    if ((all_periodic(G) || (!exact && yz_periodic)) && fast_ok(g, {u, upd, u_new, r}))
         return ch_rhs_fast_launch(fused, exact, u, upd, u_new, r, g, G, P, st);
     dim3 grid; int lx;
     ch_stencil_grid(g, &grid, &lx);

@@ -117,7 +117,10 @@ struct TolMath {
     }
 };
 
-template <class T, bool FUSED, class M, bool DEFER>
+// XB: a Neumann or Dirichlet x axis (y and z periodic; the spectral loops' mirrored-x step).  Planes
+// outside [0, nx) are still staged (wrapped) but never read: the x neighbours of the boundary planes
+// are the ghosts of the boundary values, for c and for mu alike (evoxels pads both).
+template <class T, bool FUSED, class M, bool DEFER, bool XB = false>
 __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const float* __restrict__ upd,
                                          float* __restrict__ u_new, float* __restrict__ r, const Geo& G,
                                          const ChP& P, int k0, int j0, int x0, int x1, float* cs, float* ms) {
@@ -179,11 +182,17 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
             sts4(dst + LP.soff[s], clip4(a));
         }
     };
+    // x ghost of a pair of boundary values: Neumann the values, Dirichlet 2v - values
+    auto xghost = [&](float2 v, bool lo) -> float2 {
+        if (G.kind[0] == EVX_BC_NEUMANN) return v;
+        return sub2(f2s(lo ? G.lo[0] : G.hi[0]), v);
+    };
     auto compute_mu = [&](int p) {
         const float* cc = cs + cslot(p) * T::FIELD;
         const float* cm = cs + cslot(p - 1) * T::FIELD;
         const float* cp = cs + cslot(p + 1) * T::FIELD;
         float* mo = ms + mslot(p) * T::POT;
+        const bool glo = XB && p == 0, ghi = XB && p == nx - 1;
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
             if (!mv[m]) continue;
@@ -191,9 +200,11 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
             const float2 up = lds2(cc + a - W), A = lds2(cc + a), B = lds2(cc + b), dn = lds2(cc + b + W);
             const float2 zmA = make_float2(cc[a - 1], A.x), zpA = make_float2(A.y, cc[a + 2]);
             const float2 zmB = make_float2(cc[b - 1], B.x), zpB = make_float2(B.y, cc[b + 2]);
+            const float2 xmA = glo ? xghost(A, true) : lds2(cm + a), xmB = glo ? xghost(B, true) : lds2(cm + b);
+            const float2 xpA = ghi ? xghost(A, false) : lds2(cp + a), xpB = ghi ? xghost(B, false) : lds2(cp + b);
             // potential row = field row - 1
-            *reinterpret_cast<float2*>(mo + a - W) = M::mu(K, A, lds2(cm + a), lds2(cp + a), up, B, zmA, zpA);
-            *reinterpret_cast<float2*>(mo + b - W) = M::mu(K, B, lds2(cm + b), lds2(cp + b), A, dn, zmB, zpB);
+            *reinterpret_cast<float2*>(mo + a - W) = M::mu(K, A, xmA, xpA, up, B, zmA, zpA);
+            *reinterpret_cast<float2*>(mo + b - W) = M::mu(K, B, xmB, xpB, A, dn, zmB, zpB);
         }
     };
 
@@ -211,8 +222,13 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
         cB = lds2(c1 + b);
         mA = lds2(m1 + a - W);
         mB = lds2(m1 + b - W);
-        out[0] = M::template flux<0>(K, lds2(c0 + a), cA, lds2(m0 + a - W), mA);
-        out[1] = M::template flux<0>(K, lds2(c0 + b), cB, lds2(m0 + b - W), mB);
+        if (XB && plo == -1) {   // the face below plane 0: the ghosts of plane 0
+            out[0] = M::template flux<0>(K, xghost(cA, true), cA, xghost(mA, true), mA);
+            out[1] = M::template flux<0>(K, xghost(cB, true), cB, xghost(mB, true), mB);
+        } else {
+            out[0] = M::template flux<0>(K, lds2(c0 + a), cA, lds2(m0 + a - W), mA);
+            out[1] = M::template flux<0>(K, lds2(c0 + b), cB, lds2(m0 + b - W), mB);
+        }
     };
 
     auto compute_r = [&](int i) {
@@ -226,7 +242,14 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
         cB = lds2(cx + b);
         mA = lds2(mx + a - W);
         mB = lds2(mx + b - W);
-        const float2 fxp[2] = {M::template flux<0>(K, A, cA, MA, mA), M::template flux<0>(K, B, cB, MB, mB)};
+        float2 fxp[2];
+        if (XB && i == nx - 1) {   // the face above the last plane: its ghosts
+            fxp[0] = M::template flux<0>(K, A, xghost(A, false), MA, xghost(MA, false));
+            fxp[1] = M::template flux<0>(K, B, xghost(B, false), MB, xghost(MB, false));
+        } else {
+            fxp[0] = M::template flux<0>(K, A, cA, MA, mA);
+            fxp[1] = M::template flux<0>(K, B, cB, MB, mB);
+        }
         const float2 up = lds2(cc + a - W), dn = lds2(cc + b + W);
         const float2 mup = lds2(mm + a - 2 * W), mdn = lds2(mm + b);
         // z faces (left, mid) and (mid, right) of each row
@@ -275,7 +298,7 @@ __device__ __forceinline__ void rhs_tile(const float* __restrict__ u, const floa
     }
 }
 
-template <class T, bool FUSED, class M>
+template <class T, bool FUSED, class M, bool XB = false>
 __global__ void __launch_bounds__(THREADS, 4)
 ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, float* __restrict__ u_new,
                    float* __restrict__ r, Geo G, ChP P, int LX) {
@@ -284,7 +307,7 @@ ch_rhs_fast_kernel(const float* __restrict__ u, const float* __restrict__ upd, f
     const int x0 = blockIdx.z * LX;
     const int x1 = min(x0 + LX, G.nx);
     if (x0 >= x1) return;   // uniform across the block
-    rhs_tile<T, FUSED, M, true>(u, upd, u_new, r, G, P, blockIdx.x * T::TZ, blockIdx.y * T::TY, x0, x1, cs, ms);
+    rhs_tile<T, FUSED, M, true, XB>(u, upd, u_new, r, G, P, blockIdx.x * T::TZ, blockIdx.y * T::TY, x0, x1, cs, ms);
 }
 
 __device__ __forceinline__ Geo batch_geo(const BatchInst& B) {
@@ -352,7 +375,16 @@ int rhs_fast_launch_t(bool fused, bool exact, const float* u, const float* upd, 
                       const evx_grid* g, const Geo& G, const ChP& P, cudaStream_t st, int bps) {
     int lx;
     const dim3 grid = fast_grid<T>(g->nx, g->ny, g->nz, bps, g_sms, &lx);
-    if (fused)
+    if (G.kind[0] != EVX_BC_PERIODIC) {   // mirrored-x step (the caller has y and z periodic)
+        if (exact) return fail(EVX_ERR_UNSUPPORTED, "fast rhs: a non-periodic x axis has the spectral loops' arithmetic only");
+        if (fused)
+            EVX_TIMED("ch_rhs_fused", st,
+                      ch_rhs_fast_kernel<T, true, TolMath, true><<<grid, THREADS, 0, st>>>(u, upd, u_new, r, G, P, lx));
+        else
+            EVX_TIMED("ch_rhs", st,
+                      ch_rhs_fast_kernel<T, false, TolMath, true><<<grid, THREADS, 0, st>>>(u, nullptr, nullptr, r, G, P,
+                                                                                          lx));
+    } else if (fused)
         EVX_TIMED("ch_rhs_fused", st,
                   ch_rhs_fast_kernel<T, true, TolMath><<<grid, THREADS, 0, st>>>(u, upd, u_new, r, G, P, lx));
     else if (exact)
