@@ -345,7 +345,7 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
     int* counter = reinterpret_cast<int*>(part + plan->n_part * 4);
     if (spectral && (rc = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), st), "reduction counter"))) return rc;
     const float* lam = lam_in;
-    if (plan->xext) {   // mirrored x: generic pullback with ghosts
+    if (plan->xext) {   // mirrored x: pullback with x ghosts (the tile kernel where the fields allow it)
         const Geo Gb = make_geo(g, &plan->bc);
         float* gout = reinterpret_cast<float*>(ws_at(workspace, plan->off_upd));
         const float invNe = (float)(1.0 / ((double)plan->nxe * g->ny * g->nz));
@@ -354,6 +354,14 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
             const float* us = states + (size_t)s * N;
             if (!want) {   // g = P lam' by the (symmetric) forward operator
                 if ((rc = ch_apply_spectral(plan, lam, gbuf, gout, spec, P, st))) return rc;
+                if (fast_ok(g, {us, gout, lam, dst})) {   // the tile kernel with x ghosts
+                    int nbx = 0;
+                    if ((rc = ch_pullback_fast_launch(0, us, gout, lam, nullptr, nullptr, dst, part, plan->n_part, g, Gb,
+                                                      P, st, &nbx, nullptr)))
+                        return rc;
+                    lam = dst;
+                    continue;
+                }
                 EVX_TIMED("ch_pullback", st,
                           ch_pullback_kernel<false><<<sg, dim3(32, 8), 0, st>>>(us, gout, lam, nullptr, nullptr, dst,
                                                                                  nullptr, Gb, P, lx));
@@ -383,13 +391,20 @@ int evx_ch_adjoint_spectra(evx_ch_plan* plan, const float* states, const float* 
             }
             if ((rc = ch_c2r(plan, spec, gout, false, st))) return rc;
             if ((rc = ch_c2r(plan, spec_h, hout, false, st))) return rc;
-            EVX_TIMED("ch_pullback_grads", st,
-                      ch_pullback_kernel<true><<<sg, dim3(32, 8), 0, st>>>(us, gout, lam, hout, us + N, dst, part, Gb,
-                                                                            P, lx));
-            count_launch();
-            if ((rc = check_launch("ch_pullback_kernel"))) return rc;
+            int nbx = (int)(sg.x * sg.y * sg.z);   // partial sums of the generic kernel; the fast launcher sets its own
+            if (fast_ok(g, {us, gout, lam, hout, us + N, dst})) {   // the tile kernel with x ghosts
+                if ((rc = ch_pullback_fast_launch(1, us, gout, lam, hout, us + N, dst, part, plan->n_part, g, Gb, P, st,
+                                                  &nbx, nullptr)))
+                    return rc;
+            } else {
+                EVX_TIMED("ch_pullback_grads", st,
+                          ch_pullback_kernel<true><<<sg, dim3(32, 8), 0, st>>>(us, gout, lam, hout, us + N, dst, part, Gb,
+                                                                                P, lx));
+                count_launch();
+                if ((rc = check_launch("ch_pullback_kernel"))) return rc;
+            }
             EVX_TIMED("ch_grad_reduce", st, ch_grad_reduce_kernel<<<1, 256, 0, st>>>(
-                part, (int)(sg.x * sg.y * sg.z), grads, kA, DA));
+                part, nbx, grads, kA, DA));
             count_launch();
             if ((rc = check_launch("ch_grad_reduce_kernel"))) return rc;
             lam = dst;

@@ -154,7 +154,13 @@ __device__ __noinline__ void last_block_reduce(const double* part, int nblk, con
     }
 }
 
-template <class T, int GR, bool ONEBAR = true>
+// XB (one-barrier flow only): a Neumann or Dirichlet x axis, y and z periodic (the mirrored-x step).
+// As the reference pads c and mu with the ghost a*cell + b (a = 1 Neumann, -1 Dirichlet), the planes
+// beyond the grid are staged as the ghosts of the boundary planes with g = 0, the potential of a ghost
+// plane is the forward ghost of mu and a*mub of its boundary plane, the boundary plane's outer x face
+// enters mub with weight (1 - a) and the cbar face sum with weight (1 + a) (the ghosts' cotangents
+// folded back into the boundary cell, as in the generic kernel).
+template <class T, int GR, bool ONEBAR = true, bool XB = false>
 __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const float* __restrict__ gfield,
                                               const float* __restrict__ lam, const float* __restrict__ hfield,
                                               const float* __restrict__ u1, float* __restrict__ lam_out,
@@ -197,9 +203,15 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     const int pa = ra * W + rc, pb = pa + W;   // field offsets of the patch rows
     float2 aD = f2s(0.f), aK = f2s(0.f), aW = f2s(0.f), aH = f2s(0.f);   // gradient partial sums
 
+    static_assert(!XB || ONEBAR, "x boundaries: one-barrier flow only");
+    const float ax = (XB && G.kind[0] == EVX_BC_DIRICHLET) ? -1.f : 1.f;
+    auto xghost = [&](float2 v, bool lo) -> float2 {   // Neumann the values, Dirichlet 2v - values
+        if (G.kind[0] == EVX_BC_NEUMANN) return v;
+        return sub2(f2s(lo ? G.lo[0] : G.hi[0]), v);
+    };
     float4 pc[2], pg[2];
     auto fetch = [&](int p) {
-        const size_t base = (size_t)pmod(p, nx) * plane;
+        const size_t base = (size_t)(XB ? min(max(p, 0), nx - 1) : pmod(p, nx)) * plane;
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
             if (!LP.valid[s]) continue;
@@ -207,14 +219,22 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             pg[s] = ldg4(gfield + base + LP.goff[s]);
         }
     };
-    auto stash = [&](int slot) {
+    auto stash = [&](int slot, int p) {
         float* dc = cs + slot * T::FIELD;
         float* dg = gs + slot * T::FIELD;
+        const bool ghost = XB && (p < 0 || p >= nx);
 #pragma unroll
         for (int s = 0; s < 2; ++s)
             if (LP.valid[s]) {
-                sts4(dc + LP.soff[s], clip4(pc[s]));
-                sts4(dg + LP.soff[s], pg[s]);
+                float4 c = clip4(pc[s]);
+                float4 g = pg[s];
+                if (ghost) {   // the boundary plane's ghost, with no cotangent
+                    const float2 lo = xghost(make_float2(c.x, c.y), p < 0), hi = xghost(make_float2(c.z, c.w), p < 0);
+                    c = make_float4(lo.x, lo.y, hi.x, hi.y);
+                    g = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                sts4(dc + LP.soff[s], c);
+                sts4(dg + LP.soff[s], g);
             }
     };
 
@@ -230,7 +250,10 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     // mu and mub of plane p: field slots cm (p-1), cc (p), cp (p+1) and g slots gc (p), gp (p+1);
     // writes potential slots mo / bo
     auto compute_mu = [&](const float* cm, const float* cc, const float* cp, const float* gc, const float* gp,
-                          float* mo, float* bo) {
+                          float* mo, float* bo, int q) {
+        // XB: weights of the boundary plane's outer x face in mub
+        const bool wlo = XB && q == 0, whi = XB && q == nx - 1;
+        const float2 fw = f2s(1.f - ax);
 #pragma unroll
         for (int m = 0; m < 1; ++m) {
             if (!mv[m]) continue;
@@ -246,8 +269,14 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             // mub = sum_faces (Gb''_minus - Gb''_plus)
             float2 gxp[2];
             gx_faces(cc, cp, gc, gp, m, gxp);
-            float2 bA = sub2(gxm[m][0], gxp[0]);
-            float2 bB = sub2(gxm[m][1], gxp[1]);
+            float2 bA, bB;
+            if (XB && (wlo || whi)) {
+                bA = sub2(wlo ? mul2(fw, gxm[m][0]) : gxm[m][0], whi ? mul2(fw, gxp[0]) : gxp[0]);
+                bB = sub2(wlo ? mul2(fw, gxm[m][1]) : gxm[m][1], whi ? mul2(fw, gxp[1]) : gxp[1]);
+            } else {
+                bA = sub2(gxm[m][0], gxp[0]);
+                bB = sub2(gxm[m][1], gxp[1]);
+            }
             gxm[m][0] = gxp[0];
             gxm[m][1] = gxp[1];
             const float2 gup = lds2(gc + a - W), gA = lds2(gc + a), gB = lds2(gc + b), gdn = lds2(gc + b + W);
@@ -274,7 +303,9 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
                 fma2(K.w, phi2(A), lapw(K.lk, K.lkc, A, lds2(cm + a), lds2(cp + a), up, dn, zmA, zpA));
             const float2 gA = lds2(gc + a);
             const float2 gxp = gb2<0>(K, A, lds2(cp + a), gA, lds2(gp + a));
-            float2 bA = sub2(gxh, gxp);
+            float2 bA;
+            if (XB && (wlo || whi)) bA = sub2(wlo ? mul2(fw, gxh) : gxh, whi ? mul2(fw, gxp) : gxp);
+            else bA = sub2(gxh, gxp);
             gxh = gxp;
             const float2 gup = lds2(gc + a - W), gdn = lds2(gc + a + W);
             const float2 gzmA = make_float2(gc[a - 1], gA.x), gzpA = make_float2(gA.y, gc[a + 2]);
@@ -312,8 +343,14 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         {
             float2 cfx_p[2];
             x_faces_b(cx, gx, mx, cfx_p);
-            accA = add2(cfx_m[0], cfx_p[0]);
-            accB = add2(cfx_m[1], cfx_p[1]);
+            if (XB && (i == 0 || i == nx - 1)) {   // the boundary plane's outer face, weight 1 + a
+                const float2 fw = f2s(1.f + ax);
+                accA = add2(i == 0 ? mul2(fw, cfx_m[0]) : cfx_m[0], i == nx - 1 ? mul2(fw, cfx_p[0]) : cfx_p[0]);
+                accB = add2(i == 0 ? mul2(fw, cfx_m[1]) : cfx_m[1], i == nx - 1 ? mul2(fw, cfx_p[1]) : cfx_p[1]);
+            } else {
+                accA = add2(cfx_m[0], cfx_p[0]);
+                accB = add2(cfx_m[1], cfx_p[1]);
+            }
             cfx_m[0] = cfx_p[0];
             cfx_m[1] = cfx_p[1];
         }
@@ -391,10 +428,33 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     auto gf = [&](int slot) { return Gf + slot * T::FIELD; };
     auto mp = [&](int slot) { return ms + slot * T::POT; };
     auto bp = [&](int slot) { return bs + slot * T::POT; };
+    // XB: the potential of ghost plane p from its boundary plane q at this thread's stage-A points (the
+    // thread wrote plane q's values there itself): the forward ghost of mu and a*mub
+    auto ghost_pot = [&](int p, int q) {
+        const bool lo = p < 0;
+        const float* mq = mp(mslt(q));
+        const float* bq = bp(mslt(q));
+        float* mg = mp(mslt(p));
+        float* bg = bp(mslt(p));
+        const float2 a2 = f2s(ax);
+        auto row = [&](int o) {
+            *reinterpret_cast<float2*>(mg + o - W) = xghost(lds2(mq + o - W), lo);
+            *reinterpret_cast<float2*>(bg + o - W) = mul2(a2, lds2(bq + o - W));
+        };
+        if (mv[0]) {
+            row(mo_[0]);
+            row(mo_[0] + W);
+        }
+        if (hv) row(ho);
+    };
     // potential of plane p from the field slots of p-1, p, p+1
     auto mu_of = [&](int p) {
+        if (XB && (p < 0 || p >= nx)) {
+            ghost_pot(p, p < 0 ? 0 : nx - 1);
+            return;
+        }
         const int s0 = cslt(p - 1), s1 = cslt(p), s2 = cslt(p + 1), t = mslt(p);
-        compute_mu(cf(s0), cf(s1), cf(s2), gf(s1), gf(s2), mp(t), bp(t));
+        compute_mu(cf(s0), cf(s1), cf(s2), gf(s1), gf(s2), mp(t), bp(t), p);
     };
 
     if (ONEBAR) {
@@ -403,24 +463,34 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         // x1+1 and potentials up to x1 are needed.
         for (int p = x0 - 2; p <= x0 + 2; ++p) {
             fetch(p);
-            stash(cslt(p));
+            stash(cslt(p), p);
         }
         fetch(x0 + 3);
         __syncthreads();
-        if (mv[0]) gx_faces(cf(cslt(x0 - 2)), cf(cslt(x0 - 1)), gf(cslt(x0 - 2)), gf(cslt(x0 - 1)), 0, gxm[0]);
-        if (hv) gxh = gb2<0>(K, lds2(cf(cslt(x0 - 2)) + ho), lds2(cf(cslt(x0 - 1)) + ho), lds2(gf(cslt(x0 - 2)) + ho),
-                             lds2(gf(cslt(x0 - 1)) + ho));
-        mu_of(x0 - 1);
-        mu_of(x0);
-        mu_of(x0 + 1);
+        if (XB && x0 == 0) {
+            // the face below plane 0 against the staged ghost plane; the ghost potential after plane 0's
+            if (mv[0]) gx_faces(cf(cslt(-1)), cf(cslt(0)), gf(cslt(-1)), gf(cslt(0)), 0, gxm[0]);
+            if (hv) gxh = gb2<0>(K, lds2(cf(cslt(-1)) + ho), lds2(cf(cslt(0)) + ho), lds2(gf(cslt(-1)) + ho),
+                                 lds2(gf(cslt(0)) + ho));
+            mu_of(0);
+            mu_of(1);
+            mu_of(-1);
+        } else {
+            if (mv[0]) gx_faces(cf(cslt(x0 - 2)), cf(cslt(x0 - 1)), gf(cslt(x0 - 2)), gf(cslt(x0 - 1)), 0, gxm[0]);
+            if (hv) gxh = gb2<0>(K, lds2(cf(cslt(x0 - 2)) + ho), lds2(cf(cslt(x0 - 1)) + ho),
+                                 lds2(gf(cslt(x0 - 2)) + ho), lds2(gf(cslt(x0 - 1)) + ho));
+            mu_of(x0 - 1);
+            mu_of(x0);
+            mu_of(x0 + 1);
+        }
         __syncthreads();
-        if (x0 + 3 <= x1 + 1) stash(cslt(x0 + 3));
+        if (x0 + 3 <= x1 + 1) stash(cslt(x0 + 3), x0 + 3);
         if (x0 + 4 <= x1 + 1) fetch(x0 + 4);
     } else {
         // prologue: planes x0-2 .. x0+1 staged; potentials x0-1, x0
         for (int p = x0 - 2; p <= x0 + 1; ++p) {
             fetch(p);
-            stash(cslt(p));
+            stash(cslt(p), p);
         }
         fetch(x0 + 2);
         __syncthreads();
@@ -456,8 +526,11 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
             const int c3 = c2 + 1 == NC ? 0 : c2 + 1, c4 = c3 + 1 == NC ? 0 : c3 + 1;
             const int m1 = m0 + 1 == NM ? 0 : m0 + 1, m2 = m1 + 1 == NM ? 0 : m1 + 1;
             compute_lam(i, cf(c0), cf(c1), gf(c0), gf(c1), mp(m0), mp(m1), bp(m0), bp(m1));
-            if (i + 2 <= x1) compute_mu(cf(c1), cf(c2), cf(c3), gf(c2), gf(c3), mp(m2), bp(m2));
-            if (i + 4 <= x1 + 1) stash(c4);
+            if (i + 2 <= x1) {
+                if (XB && i + 2 >= nx) ghost_pot(i + 2, nx - 1);
+                else compute_mu(cf(c1), cf(c2), cf(c3), gf(c2), gf(c3), mp(m2), bp(m2), i + 2);
+            }
+            if (i + 4 <= x1 + 1) stash(c4, i + 4);
             if (i + 5 <= x1 + 1) fetch(i + 5);
             __syncthreads();
             c0 = c1;
@@ -465,7 +538,7 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         }
     } else {
         for (int i = x0; i < x1; ++i) {
-            stash(cslt(i + 2));
+            stash(cslt(i + 2), i + 2);
             if (i + 3 <= x1 + 1) fetch(i + 3);
             __syncthreads();
             mu_of(i + 1);
@@ -480,7 +553,7 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
     sH += aH.x + aH.y;
 }
 
-template <class T, int GR>
+template <class T, int GR, bool XB = false>
 __global__ void __launch_bounds__(THREADS, EVX_PULLBACK_MIN_BLOCKS)
 ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ gfield, const float* __restrict__ lam,
                         const float* __restrict__ hfield, const float* __restrict__ u1, float* __restrict__ lam_out,
@@ -503,7 +576,7 @@ ch_pullback_fast_kernel(const float* __restrict__ u, const float* __restrict__ g
         const int t = (int)(s0 / G.nx);
         const int xa = (int)(s0 - (long)t * G.nx);
         const int xb = (int)min((long)G.nx, xa + (s1 - s0));
-        pullback_tile<T, GR, PB_ONEBAR>(u, gfield, lam, hfield, u1, lam_out, G, P, (t % ntz) * T::TZ, (t / ntz) * T::TY, xa,
+        pullback_tile<T, GR, PB_ONEBAR, XB>(u, gfield, lam, hfield, u1, lam_out, G, P, (t % ntz) * T::TZ, (t / ntz) * T::TY, xa,
                              xb, cs, gs, ms, bs, sD, sK, sW, sH);
         s0 += xb - xa;   // the tile's last barrier protects the rings from the next tile's prologue
     }
@@ -587,6 +660,11 @@ void init_occupancy() {
     setup(ch_pullback_fast_kernel<TileSquare, 0>, &g_bps[1][0], PbRings::SMEM);
     setup(ch_pullback_fast_kernel<TileSquare, 1>, &g_bps[1][1], PbRings::SMEM);
     setup(ch_pullback_fast_kernel<TileSquare, 2>, &g_bps[1][2], PbRings::SMEM);
+    int xb_bps = 0;   // the mirrored-x variants: the same resources as their periodic counterparts
+    setup(ch_pullback_fast_kernel<TileWide, 0, true>, &xb_bps, PbRings::SMEM);
+    setup(ch_pullback_fast_kernel<TileWide, 1, true>, &xb_bps, PbRings::SMEM);
+    setup(ch_pullback_fast_kernel<TileSquare, 0, true>, &xb_bps, PbRings::SMEM);
+    setup(ch_pullback_fast_kernel<TileSquare, 1, true>, &xb_bps, PbRings::SMEM);
     setup(ch_pullback_batch_kernel<0>, &g_batch_bps[0], BatchRings::SMEM);
     setup(ch_pullback_batch_kernel<1>, &g_batch_bps[1], BatchRings::SMEM);
     setup(ch_pullback_batch_kernel<2>, &g_batch_bps[2], BatchRings::SMEM);
@@ -618,7 +696,17 @@ int pb_launch_t(int grads, const float* u, const float* g, const float* lam, con
     const int nb = (int)grid.x;
     if (grads && nb > n_part_cap) return fail(EVX_ERR_WORKSPACE, "partial-sum buffer too small (%d > %d)", nb, n_part_cap);
     if (n_part_used) *n_part_used = nb;
-    if (grads == 1)
+    if (G.kind[0] != EVX_BC_PERIODIC) {   // mirrored-x step (y and z periodic): x ghosts, no stored spectra
+        if (grads == 2) return fail(EVX_ERR_UNSUPPORTED, "fast pullback: spectral sums need a periodic x axis");
+        if (grads == 1)
+            EVX_TIMED("ch_pullback_grads", st,
+                      ch_pullback_fast_kernel<T, 1, true><<<grid, THREADS, PbRings::SMEM, st>>>(u, g, lam, h, u1, lam_out,
+                                                                                         part, G, P, seg, S));
+        else
+            EVX_TIMED("ch_pullback", st,
+                      ch_pullback_fast_kernel<T, 0, true><<<grid, THREADS, PbRings::SMEM, st>>>(u, g, lam, nullptr, nullptr,
+                                                                                         lam_out, nullptr, G, P, seg, S));
+    } else if (grads == 1)
         EVX_TIMED("ch_pullback_grads", st,
                   ch_pullback_fast_kernel<T, 1><<<grid, THREADS, PbRings::SMEM, st>>>(u, g, lam, h, u1, lam_out, part, G, P, seg, S));
     else if (grads == 2)
