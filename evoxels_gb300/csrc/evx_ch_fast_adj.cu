@@ -468,7 +468,8 @@ __device__ __forceinline__ void pullback_tile(const float* __restrict__ u, const
         fetch(x0 + 3);
         __syncthreads();
         if (XB && x0 == 0) {
-            // the face below plane 0 against the staged ghost plane; the ghost potential after plane 0's
+            // the face below plane 0 against the staged ghost plane; the ghost plane's potential is
+            // derived from plane 0's, so it comes after it
             if (mv[0]) gx_faces(cf(cslt(-1)), cf(cslt(0)), gf(cslt(-1)), gf(cslt(0)), 0, gxm[0]);
             if (hv) gxh = gb2<0>(K, lds2(cf(cslt(-1)) + ho), lds2(cf(cslt(0)) + ho), lds2(gf(cslt(-1)) + ho),
                                  lds2(gf(cslt(0)) + ho));
